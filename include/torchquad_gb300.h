@@ -1,0 +1,170 @@
+/*
+ * torchquad_gb300 — C ABI of the GB300 (sm_103a) integration kernels.
+ *
+ * Every entry point:
+ *   - takes plain device pointers, sizes and a cudaStream_t passed as void*;
+ *   - never allocates device memory except where a comment says so (the
+ *     caller passes every buffer, scratch included, sized by the matching
+ *     *_workspace_size() query);
+ *   - never throws and never synchronises the stream; it returns an int
+ *     status (TQ_OK or a negative TQ_ERR_* code, see tq_status_string()).
+ *
+ * Arrays are row-major.  "dtype" selects the arithmetic type of points,
+ * integrand values and integration domain: TQ_F32 or TQ_F64.  Sums are
+ * accumulated in fp64 with compensated (Neumaier/Kahan) summation whatever
+ * the dtype.
+ *
+ * Each declaration names the reference torchquad (v0.5.0) function it
+ * replaces as file:line within the reference project.
+ */
+#ifndef TORCHQUAD_GB300_H
+#define TORCHQUAD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+  TQ_OK = 0,
+  TQ_ERR_ARG = -1,         /* null pointer / inconsistent sizes            */
+  TQ_ERR_DIM = -2,         /* dim < 1 or dim > TQ_MAX_DIM on a fused path  */
+  TQ_ERR_RULE = -3,        /* unknown rule or n invalid for the rule       */
+  TQ_ERR_FAMILY = -4,      /* unknown built-in integrand family            */
+  TQ_ERR_TOO_LARGE = -5,   /* point count overflows the index arithmetic   */
+  TQ_ERR_WORKSPACE = -6,   /* workspace smaller than *_workspace_size()    */
+  TQ_ERR_CUDA = -7,        /* a CUDA runtime call failed (tq_last_cuda_error) */
+  TQ_ERR_DTYPE = -8,       /* unknown dtype code                           */
+  TQ_ERR_TIMEOUT = -9      /* a bounded device-side wait gave up           */
+};
+
+enum { TQ_F32 = 0, TQ_F64 = 1 };
+
+/* Quadrature rules (reference: trapezoid.py:27-37, simpson.py:29-46,
+ * boole.py:29-48, gaussian.py:131-144; TQ_RULE_MC is the plain mean of
+ * monte_carlo.py:60-82). */
+enum {
+  TQ_RULE_TRAPEZOID = 0,
+  TQ_RULE_SIMPSON = 1,
+  TQ_RULE_BOOLE = 2,
+  TQ_RULE_GAUSS = 3,
+  TQ_RULE_MC = 4
+};
+
+/* Built-in fused integrand families.  Every family has the separable-sum
+ * form f(x) = F(sum_k g_k(x_k)); params is a device fp64 array
+ *   params[0] = c, params[1] = b, params[2 .. 2+dim) = a_k,
+ *   params[2+dim .. 2+2*dim) = u_k   (only TQ_FN_GAUSSIAN reads u_k)
+ *
+ *   TQ_FN_EXP_SUM      f = c * exp(sum_k a_k x_k + b)
+ *   TQ_FN_GAUSSIAN     f = c * exp(-sum_k a_k (x_k - u_k)^2)
+ *   TQ_FN_OSCILLATORY  f = c * cos(2*pi*b + sum_k a_k x_k)
+ *   TQ_FN_SUM_SIN      f = c * sum_k sin(a_k x_k)
+ */
+enum {
+  TQ_FN_EXP_SUM = 1,
+  TQ_FN_GAUSSIAN = 2,
+  TQ_FN_OSCILLATORY = 3,
+  TQ_FN_SUM_SIN = 4
+};
+
+#define TQ_MAX_DIM 16
+
+/* ---- library ------------------------------------------------------------- */
+const char* tq_status_string(int status);
+/* The cudaError_t of the last TQ_ERR_CUDA on the calling thread. */
+int tq_last_cuda_error(void);
+/* Number of SMs and resident CTAs the grids are sized with (device current). */
+int tq_device_sm_count(void);
+
+/* ---- grid rules: fused (node generation + integrand + weighted sum) ------ */
+
+/* Workspace bytes needed by tq_grid_fused for this problem. */
+size_t tq_grid_fused_workspace_size(int rule, int dim, int64_t n_per_dim);
+
+/* Tensor-product rule over n_per_dim^dim nodes with a built-in integrand,
+ * written to out[0] (dtype out_dtype) and, if out64 != NULL, to out64[0].
+ * Replaces GridIntegrator.integrate (grid_integrator.py:32-55) for the
+ * Trapezoid/Simpson/Boole/GaussLegendre subclasses: IntegrationGrid
+ * (integration_grid.py:28-103) + evaluate_integrand (base_integrator.py:43-91)
+ * + calculate_result/_apply_composite_rule (grid_integrator.py:57-91).
+ * domain: device [dim][2] of dtype; gl_nodes/gl_weights: device fp64 [n]
+ * Gauss-Legendre roots/weights on [-1,1] (only for TQ_RULE_GAUSS, whose
+ * nodes are computed in fp64 as in gaussian.py:159-162). */
+int tq_grid_fused(int dtype, int rule, int dim, int64_t n_per_dim,
+                  const void* domain, const double* gl_nodes,
+                  const double* gl_weights, int family, const double* params,
+                  void* out, int out_dtype, double* out64,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- grid rules: materialised path for arbitrary integrands -------------- */
+
+/* Writes points[count][dim] (dtype; fp64 for TQ_RULE_GAUSS) for the flat
+ * node indices [start, start+count) of the tensor-product grid, last
+ * dimension fastest, exactly as IntegrationGrid builds them
+ * (integration_grid.py:95-99 meshgrid(indexing="ij") + stack). */
+int tq_grid_points(int dtype, int rule, int dim, int64_t n_per_dim,
+                   const void* domain, const double* gl_nodes,
+                   int64_t start, int64_t count, void* points, void* stream);
+
+/* Writes the tensor-product quadrature weight of each node in
+ * [start, start+count) to weights[count] (fp64).  Used by the backward pass
+ * of the differentiable materialised path (d result / d f_i). */
+int tq_grid_weights(int dtype, int rule, int dim, int64_t n_per_dim,
+                    const void* domain, const double* gl_weights,
+                    int64_t start, int64_t count, double* weights, void* stream);
+
+size_t tq_weighted_sum_workspace_size(int64_t count, int64_t n_values);
+
+/* acc[2*s], acc[2*s+1] (a compensated fp64 running sum, s < n_values) +=
+ * sum_i w_i * f[i][s] over the nodes [start, start+count) of the grid;
+ * f is [count][n_values] of f_dtype (complex integrands are passed as their
+ * real view).  For TQ_RULE_MC w_i = 1.  Replaces the weight multiply of
+ * base_integrator.py:77-89 and the per-dimension collapse of
+ * grid_integrator.py:57-91 / the sum of monte_carlo.py:77. */
+int tq_weighted_sum(int dtype, int rule, int dim, int64_t n_per_dim,
+                    const void* domain, const double* gl_weights,
+                    int64_t start, int64_t count, const void* f, int f_dtype,
+                    int64_t n_values, double* acc, void* workspace,
+                    size_t workspace_bytes, void* stream);
+
+/* out[s] = (out_dtype)(scale * (acc[2s] + acc[2s+1])) where scale is 1 for
+ * grid rules and prod_k(b_k - a_k) / n_points (computed in dtype, as
+ * monte_carlo.py:72-77) for TQ_RULE_MC. */
+int tq_finalize_sum(int dtype, int rule, int dim, const void* domain,
+                    int64_t n_points, const double* acc, int64_t n_values,
+                    void* out, int out_dtype, void* stream);
+
+/* ---- random numbers ------------------------------------------------------ */
+
+/* Counter-based Philox4x32-10 (Salmon et al., SC'11).  Element e of a
+ * request with block offset `offset` is drawn from counter
+ * {lo(offset+e/4), hi(offset+e/4), lo(stream_id), hi(stream_id)} lane e%4 for
+ * fp32 (u = (r >> 8) * 2^-24) and from lanes 2(e%2), 2(e%2)+1 of block
+ * offset+e/2 for fp64 (u = ((hi<<32|lo) >> 11) * 2^-53), key = seed.
+ * All values lie in [0, 1).  A request of numel values consumes
+ * ceil(numel/4) (fp32) or ceil(numel/2) (fp64) blocks.
+ * Replaces RNG.uniform (rng.py:120-125, torch.rand). */
+int tq_uniform(int dtype, uint64_t seed, uint64_t stream_id, uint64_t offset,
+               int64_t numel, void* out, void* stream);
+
+/* ---- Monte Carlo: fused ------------------------------------------------- */
+
+size_t tq_mc_fused_workspace_size(int dim, int64_t n_points);
+
+/* MonteCarlo.integrate (monte_carlo.py:20-106) for a built-in integrand:
+ * x = u * (b - a) + a with u from tq_uniform(seed, stream_id, offset) over
+ * [n_points][dim], result = prod(b - a) * sum f(x) / n_points -> out[0]. */
+int tq_mc_fused(int dtype, int dim, int64_t n_points, const void* domain,
+                int family, const double* params, uint64_t seed,
+                uint64_t stream_id, uint64_t offset, void* out, double* out64,
+                void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TORCHQUAD_GB300_H */

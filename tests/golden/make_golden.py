@@ -1,0 +1,203 @@
+"""Record golden fixtures from the unmodified reference torchquad.
+
+Run in a container where the reference source is present:
+
+    python tests/golden/make_golden.py /root/reference
+
+The reference's hard dependencies autoray and loguru are replaced by the
+small stand-ins in ``tests/golden/refshim`` (dispatch only, no arithmetic).
+The reference runs on torch CPU in this process; uniform draws for Monte
+Carlo / VEGAS are injected from the Philox stream of ``oracle.philox`` through
+the reference's own ``rng=`` argument.  Outputs (JSON, floats as hex) are
+written next to this script and committed; tests read them on any machine.
+"""
+from __future__ import annotations
+
+import json
+import math
+import sys
+import warnings
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+
+
+def _import_reference(ref_root: str):
+    sys.path[:0] = [str(HERE / "refshim"), ref_root, str(REPO)]
+    import torchquad  # noqa: F401  (the reference)
+
+    return torchquad
+
+
+def hexf(x) -> str:
+    return float(x).hex()
+
+
+def hexarr(a):
+    import numpy as np
+
+    return [float(v).hex() for v in np.asarray(a, dtype=np.float64).ravel()]
+
+
+class ReplayRNG:
+    """RNG stand-in handed to the reference (``rng=``): draws come from the
+    counter-based Philox stream the GB300 build uses, as torch tensors, and
+    every draw is recorded."""
+
+    def __init__(self, seed, stream_id=0):
+        from oracle.philox import ReplayStream
+
+        self.stream = ReplayStream(seed, stream_id)
+        self.log = []
+
+    def uniform(self, size, dtype):
+        import numpy as np
+        import torch
+
+        nd = np.float32 if dtype == torch.float32 else np.float64
+        a = self.stream.uniform(list(size), nd)
+        self.log.append(a)
+        return torch.from_numpy(a.copy())
+
+
+def grid_cases():
+    """(name, rule class, dim, N, family spec, domain, dtype)."""
+    cases = []
+    fams = [
+        ("expsum1", 1, dict(kind="ExpSum", a=[1.0], b=0.0), [[-2.0, 1.0]], 101),
+        ("expsum3", 3, dict(kind="ExpSum", a=[1.0, 1.0, 1.0], b=0.0), [[0.0, 1.0]] * 3, 21**3),
+        ("gauss2", 2, dict(kind="GaussianPeak", a=[2.0, 3.0], u=[0.3, 0.6], c=1.5), [[-1.0, 1.0], [0.0, 2.0]], 33**2),
+        ("osc4", 4, dict(kind="Oscillatory", a=[1.0, -2.0, 0.5, 1.5], b=0.3), [[0.0, 1.0]] * 4, 9**4),
+        ("sumsin5", 5, dict(kind="SumSin", a=[1.0] * 5), [[0.0, 1.0]] * 5, 5**5),
+        ("adjust3", 3, dict(kind="ExpSum", a=[0.5, -1.0, 2.0], b=0.25), [[0.0, 1.0], [-1.0, 0.5], [0.2, 0.4]], 1000),
+    ]
+    for rule in ["Trapezoid", "Simpson", "Boole", "GaussLegendre"]:
+        for dtype in ["float32", "float64"]:
+            for name, dim, fam, dom, N in fams:
+                cases.append((f"{rule}-{name}-{dtype}", rule, dim, N, fam, dom, dtype))
+    cases.append(("C1-Simpson-expsum3-101", "Simpson", 3, 1030301,
+                  dict(kind="ExpSum", a=[1.0] * 3, b=0.0), [[0.0, 1.0]] * 3, "float64"))
+    cases.append(("C4-GaussLegendre-osc4-32", "GaussLegendre", 4, 32**4,
+                  dict(kind="Oscillatory", a=[1.2, -2.1, 0.7, 2.6], b=0.37), [[0.0, 1.0]] * 4, "float64"))
+    cases.append(("Simpson-N1076890-expsum3", "Simpson", 3, 1076890,
+                  dict(kind="ExpSum", a=[1.0] * 3, b=0.0), [[0.0, 1.0]] * 3, "float64"))
+    return cases
+
+
+def make_integrand(spec, dim):
+    import torchquad_gb300.integrands as I
+
+    kw = {k: v for k, v in spec.items() if k != "kind"}
+    return getattr(I, spec["kind"])(dim, **kw)
+
+
+def gen_grid(tq):
+    import torch
+
+    out = []
+    for name, rule, dim, N, fam, dom, dtype in grid_cases():
+        dt = getattr(torch, dtype)
+        f = make_integrand(fam, dim)
+        domain = torch.tensor(dom, dtype=dt)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            integ = getattr(tq, rule)()
+            val = integ.integrate(f, dim, N=N, integration_domain=domain)
+        out.append(dict(name=name, rule=rule, dim=dim, N=N, family=fam, domain=dom, dtype=dtype,
+                        value=hexf(val.item()), result_dtype=str(val.dtype).replace("torch.", ""),
+                        n_per_dim=int(integ._nr_of_fevals ** (1.0 / dim) + 0.5),
+                        fevals=int(integ._nr_of_fevals),
+                        params=hexarr(f.params_vector().numpy())))
+    return out
+
+
+def gen_multidim(tq):
+    """Vector-valued and complex integrands on the materialised path."""
+    import torch
+
+    out = []
+    dom = [[0.0, 1.0], [-1.0, 2.0]]
+    for rule in ["Trapezoid", "Simpson", "Boole", "GaussLegendre"]:
+        domain = torch.tensor(dom, dtype=torch.float64)
+
+        def vec(x):
+            base = torch.exp(0.3 * x[:, 0] - 0.2 * x[:, 1])
+            scale = torch.arange(6, dtype=x.dtype).reshape(2, 3) + 1.0
+            return base[:, None, None] * scale[None] + x[:, 0:1, None] * x[:, 1:2, None]
+
+        def cplx(x):
+            return torch.exp(1j * (x[:, 0] + 0.5 * x[:, 1]))
+
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            v = getattr(tq, rule)().integrate(vec, 2, N=17**2, integration_domain=domain)
+            c = getattr(tq, rule)().integrate(cplx, 2, N=17**2, integration_domain=domain)
+        out.append(dict(rule=rule, domain=dom, N=17**2, vec=hexarr(v.numpy()), vec_shape=list(v.shape),
+                        cplx=[hexf(c.real.item()), hexf(c.imag.item())]))
+    return out
+
+
+def gen_linspace():
+    import numpy as np
+    import torch
+
+    rng = np.random.default_rng(7)
+    out = []
+    for i in range(24):
+        dt = torch.float32 if i % 2 == 0 else torch.float64
+        n = int(rng.integers(2, 400))
+        a = float(rng.uniform(-3, 1))
+        b = a + float(rng.uniform(0.1, 5))
+        x = torch.linspace(torch.tensor(a, dtype=dt), torch.tensor(b, dtype=dt), n, dtype=dt)
+        out.append(dict(a=hexf(torch.tensor(a, dtype=dt).item()), b=hexf(torch.tensor(b, dtype=dt).item()),
+                        n=n, dtype=str(dt).replace("torch.", ""), values=hexarr(x.numpy())))
+    return out
+
+
+def gen_mc(tq):
+    import torch
+
+    out = []
+    cases = [
+        (1, 1000, [[-2.0, 1.0]], dict(kind="ExpSum", a=[1.0], b=0.0), 0),
+        (3, 100000, [[0.0, 1.0]] * 3, dict(kind="ExpSum", a=[1.0] * 3, b=0.0), 1),
+        (4, 50000, [[0.0, 1.0], [-1.0, 1.0], [0.5, 2.0], [0.0, 3.0]],
+         dict(kind="GaussianPeak", a=[1.0, 2.0, 0.5, 3.0], u=[0.5, 0.1, 1.0, 2.0], c=2.0), 2),
+        (6, 20000, [[0.0, 1.0]] * 6, dict(kind="Oscillatory", a=[1.0] * 6, b=0.1), 3),
+    ]
+    for dim, N, dom, fam, seed in cases:
+        for dtype in ["float32", "float64"]:
+            dt = getattr(torch, dtype)
+            rng = ReplayRNG(seed)
+            f = make_integrand(fam, dim)
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                val = tq.MonteCarlo().integrate(f, dim, N=N, integration_domain=torch.tensor(dom, dtype=dt), rng=rng)
+            out.append(dict(dim=dim, N=N, domain=dom, family=fam, seed=seed, dtype=dtype,
+                            value=hexf(val.item()), params=hexarr(f.params_vector().numpy()),
+                            first_uniforms=hexarr(rng.log[0].ravel()[:16])))
+    return out
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    tq = _import_reference(ref_root)
+    import torch
+
+    torch.set_num_threads(4)
+    data = {
+        "reference_version": tq.__version__,
+        "torch": torch.__version__,
+        "grid": gen_grid(tq),
+        "multidim": gen_multidim(tq),
+        "linspace": gen_linspace(),
+        "mc": gen_mc(tq),
+    }
+    with open(HERE / "grid_mc_golden.json", "w") as fh:
+        json.dump(data, fh, indent=0)
+    print("wrote", HERE / "grid_mc_golden.json", len(data["grid"]), "grid cases")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+"""ctypes binding of the C ABI declared in ``include/torchquad_gb300.h``.
+
+The library is loaded on first use.  There is no fallback: if the library is
+missing or no CUDA device is present, every integration call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from ctypes import POINTER, c_double, c_int, c_int64, c_size_t, c_uint64, c_void_p, c_char_p
+
+import torch
+
+from .build import lib_path
+
+# status codes (include/torchquad_gb300.h)
+TQ_OK = 0
+TQ_ERR_ARG = -1
+TQ_ERR_DIM = -2
+TQ_ERR_RULE = -3
+TQ_ERR_FAMILY = -4
+TQ_ERR_TOO_LARGE = -5
+TQ_ERR_WORKSPACE = -6
+TQ_ERR_CUDA = -7
+TQ_ERR_DTYPE = -8
+TQ_ERR_TIMEOUT = -9
+
+TQ_F32, TQ_F64 = 0, 1
+
+TQ_RULE_TRAPEZOID, TQ_RULE_SIMPSON, TQ_RULE_BOOLE, TQ_RULE_GAUSS, TQ_RULE_MC = 0, 1, 2, 3, 4
+
+TQ_FN_EXP_SUM, TQ_FN_GAUSSIAN, TQ_FN_OSCILLATORY, TQ_FN_SUM_SIN = 1, 2, 3, 4
+
+TQ_MAX_DIM = 16
+
+# name -> (restype, argtypes); every symbol the header declares.
+SIGNATURES = {
+    "tq_status_string": (c_char_p, [c_int]),
+    "tq_last_cuda_error": (c_int, []),
+    "tq_device_sm_count": (c_int, []),
+    "tq_grid_fused_workspace_size": (c_size_t, [c_int, c_int, c_int64]),
+    "tq_grid_fused": (
+        c_int,
+        [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+         c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
+    "tq_grid_points": (
+        c_int,
+        [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p],
+    ),
+    "tq_grid_weights": (
+        c_int,
+        [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p],
+    ),
+    "tq_weighted_sum_workspace_size": (c_size_t, [c_int64, c_int64]),
+    "tq_weighted_sum": (
+        c_int,
+        [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_int,
+         c_int64, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
+    "tq_finalize_sum": (
+        c_int,
+        [c_int, c_int, c_int, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int, c_void_p],
+    ),
+    "tq_uniform": (c_int, [c_int, c_uint64, c_uint64, c_uint64, c_int64, c_void_p, c_void_p]),
+    "tq_mc_fused_workspace_size": (c_size_t, [c_int, c_int64]),
+    "tq_mc_fused": (
+        c_int,
+        [c_int, c_int, c_int64, c_void_p, c_int, c_void_p, c_uint64, c_uint64, c_uint64,
+         c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+class TorchquadGB300Error(RuntimeError):
+    """A kernel entry point returned a non-zero status."""
+
+    def __init__(self, status: int, where: str):
+        self.status = status
+        msg = f"{where}: {status_string(status)} (status {status})"
+        if status == TQ_ERR_CUDA:
+            msg += f", cudaError {lib().tq_last_cuda_error()}"
+        super().__init__(msg)
+
+
+def load(path=None):
+    """Load the shared library and declare every exported signature."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = str(path or lib_path())
+        try:
+            handle = ctypes.CDLL(p)
+        except OSError as e:
+            raise RuntimeError(
+                f"torchquad_gb300 CUDA library not loadable at {p} ({e}). "
+                "Build it with `python -m torchquad_gb300.build`; there is no CPU fallback."
+            ) from None
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        if path is None:
+            _lib = handle
+        return handle
+
+
+def lib():
+    return _lib if _lib is not None else load()
+
+
+def status_string(status: int) -> str:
+    return lib().tq_status_string(status).decode()
+
+
+def check(status: int, where: str) -> None:
+    if status != TQ_OK:
+        raise TorchquadGB300Error(status, where)
+
+
+def require_cuda() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError(
+            "torchquad_gb300 runs its integration kernels on a CUDA device only "
+            "and no CUDA device is available (there is no CPU fallback)."
+        )
+    lib()
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream_handle() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def dtype_code(dtype: torch.dtype) -> int:
+    if dtype == torch.float32:
+        return TQ_F32
+    if dtype == torch.float64:
+        return TQ_F64
+    raise TypeError(f"unsupported dtype {dtype}; float32 and float64 are supported")
+
+
+def ptr(t) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+class _Workspace:
+    """Per-device, per-stream grow-only scratch buffers owned by torch."""
+
+    def __init__(self):
+        self._bufs = {}
+
+    def get(self, nbytes: int, slot: str = "main") -> torch.Tensor:
+        dev = torch.cuda.current_device()
+        key = (dev, torch.cuda.current_stream().cuda_stream, slot)
+        buf = self._bufs.get(key)
+        if buf is None or buf.numel() < nbytes:
+            # tickets in the first 16 bytes must start at zero
+            buf = torch.zeros(max(int(nbytes), 4096), dtype=torch.uint8, device=f"cuda:{dev}")
+            self._bufs[key] = buf
+        return buf
+
+
+workspace = _Workspace()

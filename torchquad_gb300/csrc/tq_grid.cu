@@ -1,0 +1,638 @@
+// Tensor-product quadrature on GB300: fused node generation + integrand +
+// weighted sum for built-in integrands, and the node / weight / weighted-sum
+// kernels of the materialised path used for arbitrary torch integrands.
+//
+// The reference builds the full [n^d, d] point tensor (integration_grid.py:
+// 95-99), evaluates the integrand on it, transposes the values
+// (grid_integrator.py:80) and collapses one dimension at a time
+// (trapezoid.py:27-37, simpson.py:29-46, boole.py:29-48, gaussian.py:131-144).
+// Here a thread walks a strip of consecutive flat node indices (last
+// dimension fastest, the reference's meshgrid "ij" order), keeps the
+// outer-dimension coordinates and weight product in registers, and sums
+// w_i * f(x_i) directly; the per-dimension collapse becomes the product of
+// 1-D weights, which is the same quadrature.
+
+#include "tq_common.cuh"
+
+namespace tq {
+
+// Per-dimension geometry of the grid, computed once per CTA from the domain.
+template <typename T>
+struct Geo {
+  T a[kMaxDim], b[kMaxDim], step[kMaxDim];
+  // weight scale of a dimension: NC rules h * (1/2 | 1/3 | 1/22.5), Gauss
+  // 0.5 * (b - a); both rounded as the reference rounds them, then widened.
+  double wscale[kMaxDim];
+  double half[kMaxDim], mid[kMaxDim];  // Gauss node map (b-a)/2 * r + (a+b)/2
+};
+
+// Integer part of the Newton-Cotes weights (exact in any float type).
+__device__ __forceinline__ int nc_int(int rule, int64_t i, int64_t n) {
+  if (rule == TQ_RULE_TRAPEZOID) return (i == 0 || i == n - 1) ? 1 : 2;
+  if (rule == TQ_RULE_SIMPSON) return (i == 0 || i == n - 1) ? 1 : ((i & 1) ? 4 : 2);
+  if (i == 0 || i == n - 1) return 7;
+  const int m = (int)(i & 3);
+  return (m & 1) ? 32 : (m == 2 ? 12 : 14);
+}
+__host__ __device__ __forceinline__ double nc_den(int rule) {
+  return rule == TQ_RULE_TRAPEZOID ? 2.0 : (rule == TQ_RULE_SIMPSON ? 3.0 : 22.5);
+}
+
+// D = domain type.  Fills g from domain[dim][2] (device, read by thread 0).
+template <typename T, typename D>
+__device__ void geo_setup(Geo<T>& g, int rule, int dim, int64_t n, const D* __restrict__ dom) {
+  for (int k = 0; k < dim; ++k) {
+    const D a = dom[2 * k], b = dom[2 * k + 1];
+    g.a[k] = (T)a;
+    g.b[k] = (T)b;
+    if (rule == TQ_RULE_GAUSS) {
+      // gaussian.py:159-162 in the domain type, then fp64 with the roots
+      const D hw = (D)(b - a) / (D)2;
+      const D md = (D)(a + b) / (D)2;
+      g.half[k] = (double)hw;
+      g.mid[k] = (double)md;
+      g.wscale[k] = (double)((D)0.5 * (D)(b - a));  // gaussian.py:141-143
+      g.step[k] = (T)0;
+    } else if (rule == TQ_RULE_MC) {
+      g.step[k] = (T)0;
+      g.wscale[k] = 1.0;
+    } else {
+      const T ta = (T)a, tb = (T)b;
+      const T st = (tb - ta) / (T)(n - 1);
+      g.step[k] = st;
+      // h = grid[1] - grid[0] in the working type (integration_grid.py:90-93)
+      const T h = linspace_node<T>(ta, tb, st, n, 1) - linspace_node<T>(ta, tb, st, n, 0);
+      g.wscale[k] = (double)h / nc_den(rule);
+      g.half[k] = g.mid[k] = 0.0;
+    }
+  }
+}
+
+template <typename T, bool GL>
+__device__ __forceinline__ T node_at(const Geo<T>& g, int k, int64_t n, int64_t i,
+                                     const double* __restrict__ gl_nodes) {
+  if (GL) return (T)__dadd_rn(__dmul_rn(g.half[k], __ldg(gl_nodes + i)), g.mid[k]);
+  return linspace_node<T>(g.a[k], g.b[k], g.step[k], n, i);
+}
+// Unscaled 1-D weight (integer NC coefficient or Gauss weight).
+template <bool GL>
+__device__ __forceinline__ double wunit_at(int rule, int64_t n, int64_t i,
+                                           const double* __restrict__ gl_w) {
+  if (GL) return __ldg(gl_w + i);
+  return (double)nc_int(rule, i, n);
+}
+
+// ------------------------------------------------------------------ fused
+struct FusedArgs {
+  int rule, dim, family;
+  int64_t n, total;
+  const void* domain;
+  const double* gl_nodes;
+  const double* gl_weights;
+  const double* params;
+  Acc* partials;
+  unsigned* ticket;
+  void* out;
+  int out_dtype;
+  double* out64;
+};
+
+template <typename T, int P>
+struct StripAcc;  // inner accumulation type of a strip
+template <int P>
+struct StripAcc<float, P> {
+  AccF a{0.f, 0.f};
+  __device__ void add(float x) { accf_add(a, x); }
+  __device__ double take() {
+    const double r = (double)a.s + (double)a.c;
+    a.s = a.c = 0.f;
+    return r;
+  }
+};
+template <int P>
+struct StripAcc<double, P> {
+  double a = 0.0;
+  __device__ void add(double x) { a += x; }
+  __device__ double take() {
+    const double r = a;
+    a = 0.0;
+    return r;
+  }
+};
+
+__device__ __forceinline__ void write_result(void* out, int out_dtype, double* out64,
+                                             double v) {
+  if (out) {
+    if (out_dtype == TQ_F64)
+      *(double*)out = v;
+    else
+      *(float*)out = (float)v;
+  }
+  if (out64) *out64 = v;
+}
+
+// Decodes flat row index `row` (= node index / n) into the outer digits and
+// returns (s_outer, w_outer): s_outer = g_0 + ... + g_{d-2} summed in
+// dimension order, w_outer = prod of the outer 1-D weights.
+template <typename T, bool GL, int FAM>
+__device__ __forceinline__ void outer_state(const Geo<T>& g, const Family<T>& fam, int rule,
+                                            int dim, int64_t n, uint64_t row,
+                                            const double* gl_nodes, const double* gl_w,
+                                            bool small, T& s_outer, double& w_outer) {
+  T terms[kMaxDim];
+  double w = 1.0;
+#pragma unroll
+  for (int k = kMaxDim - 2; k >= 0; --k) {
+    if (k < dim - 1) {
+      uint64_t digit;
+      if (small) {
+        const uint32_t r32 = (uint32_t)row, q = r32 / (uint32_t)n;
+        digit = r32 - q * (uint32_t)n;
+        row = q;
+      } else {
+        const uint64_t q = row / (uint64_t)n;
+        digit = row - q * (uint64_t)n;
+        row = q;
+      }
+      const T x = node_at<T, GL>(g, k, n, (int64_t)digit, gl_nodes);
+      terms[k] = fam_term<FAM, T>(fam, k, x);
+      w *= g.wscale[k] * wunit_at<GL>(rule, n, (int64_t)digit, gl_w);
+    } else {
+      terms[k] = T(0);
+    }
+  }
+  T s = terms[0];
+#pragma unroll
+  for (int k = 1; k < kMaxDim - 1; ++k)
+    if (k < dim - 1) s = s + terms[k];
+  s_outer = s;
+  w_outer = w;
+}
+
+template <typename T, typename D, bool GL, int FAM, int P>
+__global__ void __launch_bounds__(kBlock) grid_fused_kernel(FusedArgs args) {
+  __shared__ Geo<T> g;
+  __shared__ Family<T> fam;
+  if (threadIdx.x == 0) {
+    geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
+    load_family<T>(fam, args.family, args.dim, args.params);
+  }
+  __syncthreads();
+  const int dim = args.dim, rule = args.rule, last = dim - 1;
+  const int64_t n = args.n, total = args.total;
+  const bool small = total < (int64_t(1) << 32);
+  const double* gl_nodes = args.gl_nodes;
+  const double* gl_w = args.gl_weights;
+  const double wlast = g.wscale[last];
+
+  Acc acc{0.0, 0.0};
+  StripAcc<T, P> inner;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * P; base < total;
+       base += nthreads * P) {
+    uint64_t row;
+    int64_t jl;
+    if (small) {
+      const uint32_t b32 = (uint32_t)base, q = b32 / (uint32_t)n;
+      row = q;
+      jl = b32 - q * (uint32_t)n;
+    } else {
+      row = (uint64_t)base / (uint64_t)n;
+      jl = base - (int64_t)row * n;
+    }
+    T s_outer;
+    double w_outer;
+    outer_state<T, GL, FAM>(g, fam, rule, dim, n, row, gl_nodes, gl_w, small, s_outer,
+                            w_outer);
+    const int64_t end = min(base + P, total);
+    for (int64_t idx = base; idx < end; ++idx) {
+      if (jl == n) {  // carry into the outer dimensions
+        acc_add(acc, inner.take() * (w_outer * wlast));
+        ++row;
+        jl = 0;
+        outer_state<T, GL, FAM>(g, fam, rule, dim, n, row, gl_nodes, gl_w, small, s_outer,
+                                w_outer);
+      }
+      const T x = node_at<T, GL>(g, last, n, jl, gl_nodes);
+      const T f = fam_outer<FAM, T>(fam, s_outer + fam_term<FAM, T>(fam, last, x));
+      inner.add((T)wunit_at<GL>(rule, n, jl, gl_w) * f);
+      ++jl;
+    }
+    acc_add(acc, inner.take() * (w_outer * wlast));
+  }
+
+  acc = block_reduce<kBlock>(acc);
+  if (threadIdx.x == 0) args.partials[blockIdx.x] = acc;
+  if (last_block_arrives(args.ticket)) {
+    Acc t{0.0, 0.0};
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc_merge(t, args.partials[i]);
+    t = block_reduce<kBlock>(t);
+    if (threadIdx.x == 0) {
+      write_result(args.out, args.out_dtype, args.out64, t.s + t.c);
+      *args.ticket = 0u;
+    }
+  }
+}
+
+// ------------------------------------------------------ materialised path
+struct PointsArgs {
+  int rule, dim;
+  int64_t n, start, count;
+  const void* domain;
+  const double* gl_nodes;
+  void* points;
+};
+
+// One thread per output element (point p, dimension k): coalesced stores of
+// the [count, dim] row-major point tensor.
+template <typename T, typename D, bool GL>
+__global__ void __launch_bounds__(kBlock) grid_points_kernel(PointsArgs args) {
+  __shared__ Geo<T> g;
+  __shared__ uint64_t stride[kMaxDim];
+  if (threadIdx.x == 0) {
+    geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
+    uint64_t s = 1;
+    for (int k = args.dim - 1; k >= 0; --k) {
+      stride[k] = s;
+      s *= (uint64_t)args.n;
+    }
+  }
+  __syncthreads();
+  const int dim = args.dim;
+  const uint64_t n = (uint64_t)args.n;
+  const uint64_t numel = (uint64_t)args.count * dim;
+  T* out = (T*)args.points;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < numel;
+       e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t p = e / (uint64_t)dim;
+    const int k = (int)(e - p * dim);
+    const uint64_t digit = ((args.start + p) / stride[k]) % n;
+    out[e] = node_at<T, GL>(g, k, (int64_t)n, (int64_t)digit, args.gl_nodes);
+  }
+}
+
+struct WeightsArgs {
+  int rule, dim;
+  int64_t n, start, count;
+  const void* domain;
+  const double* gl_weights;
+  double* weights;
+};
+
+template <typename T, typename D, bool GL>
+__global__ void __launch_bounds__(kBlock) grid_weights_kernel(WeightsArgs args) {
+  __shared__ Geo<T> g;
+  if (threadIdx.x == 0) geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
+  __syncthreads();
+  const int dim = args.dim;
+  const uint64_t n = (uint64_t)args.n;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < (uint64_t)args.count;
+       p += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t r = args.start + p;
+    double w = 1.0;
+    for (int k = dim - 1; k >= 0; --k) {
+      const uint64_t q = r / n, digit = r - q * n;
+      r = q;
+      w *= g.wscale[k] * wunit_at<GL>(args.rule, (int64_t)n, (int64_t)digit, args.gl_weights);
+    }
+    args.weights[p] = w;
+  }
+}
+
+// Weighted sum of materialised integrand values.  A thread walks a strip of
+// consecutive nodes (weights by the same odometer as the fused kernel) and
+// accumulates up to kVals integrand components; gridDim.y covers the
+// components in groups of kVals.  Partials are reduced in fixed order by the
+// last CTA and added to the running compensated sums acc[].
+constexpr int kVals = 4;
+struct WsumArgs {
+  int rule, dim;
+  int64_t n, start, count, n_values;
+  const void* domain;
+  const double* gl_weights;
+  const void* f;
+  double* acc;
+  Acc* partials;  // [gridDim.x * gridDim.y][kVals]
+  unsigned* ticket;
+};
+
+template <typename T, typename D, bool GL, typename F, int P>
+__global__ void __launch_bounds__(kBlock) weighted_sum_kernel(WsumArgs args) {
+  __shared__ Geo<T> g;
+  if (threadIdx.x == 0) geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
+  __syncthreads();
+  const int dim = args.dim, rule = args.rule;
+  const uint64_t n = (uint64_t)args.n;
+  const int64_t S = args.n_values;
+  const int64_t s0 = (int64_t)blockIdx.y * kVals;
+  const int nv = (int)min((int64_t)kVals, S - s0);
+  const F* __restrict__ f = (const F*)args.f;
+  Acc acc[kVals];
+#pragma unroll
+  for (int v = 0; v < kVals; ++v) acc[v] = Acc{0.0, 0.0};
+
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * P; base < args.count;
+       base += nthreads * P) {
+    const int64_t end = min(base + P, args.count);
+    for (int64_t p = base; p < end; ++p) {
+      double w = 1.0;
+      if (rule != TQ_RULE_MC) {
+        uint64_t r = (uint64_t)(args.start + p);
+        for (int k = dim - 1; k >= 0; --k) {
+          const uint64_t q = r / n, digit = r - q * n;
+          r = q;
+          w *= g.wscale[k] * wunit_at<GL>(rule, (int64_t)n, (int64_t)digit, args.gl_weights);
+        }
+      }
+      const F* row = f + p * S + s0;
+#pragma unroll
+      for (int v = 0; v < kVals; ++v)
+        if (v < nv) acc_add(acc[v], w * (double)row[v]);
+    }
+  }
+  const int slot = blockIdx.y * gridDim.x + blockIdx.x;
+#pragma unroll
+  for (int v = 0; v < kVals; ++v) {
+    Acc r = block_reduce<kBlock>(acc[v]);
+    if (threadIdx.x == 0) args.partials[(int64_t)slot * kVals + v] = r;
+  }
+  if (last_block_arrives(args.ticket)) {
+    // one component at a time, partials in index order
+    for (int64_t s = 0; s < S; ++s) {
+      const int64_t by = s / kVals;
+      const int v = (int)(s - by * kVals);
+      Acc t{0.0, 0.0};
+      for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+        acc_merge(t, args.partials[((int64_t)by * gridDim.x + i) * kVals + v]);
+      t = block_reduce<kBlock>(t);
+      if (threadIdx.x == 0) {
+        Acc run{args.acc[2 * s], args.acc[2 * s + 1]};
+        acc_merge(run, t);
+        args.acc[2 * s] = run.s;
+        args.acc[2 * s + 1] = run.c;
+      }
+    }
+    if (threadIdx.x == 0) *args.ticket = 0u;
+  }
+}
+
+template <typename D>
+__global__ void finalize_kernel(int rule, int dim, const D* __restrict__ dom, int64_t npts,
+                                const double* __restrict__ acc, int64_t S, void* out,
+                                int out_dtype) {
+  double scale = 1.0;
+  if (rule == TQ_RULE_MC) {
+    // monte_carlo.py:72-77: volume = prod(b - a) in the domain type
+    D vol = (D)1;
+    for (int k = 0; k < dim; ++k) vol = vol * (D)(dom[2 * k + 1] - dom[2 * k]);
+    scale = (double)vol / (double)npts;
+  }
+  for (int64_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+    const double v = scale * (acc[2 * s] + acc[2 * s + 1]);
+    if (out_dtype == TQ_F64)
+      ((double*)out)[s] = v;
+    else
+      ((float*)out)[s] = (float)v;
+  }
+}
+
+}  // namespace tq
+
+using namespace tq;
+
+// --------------------------------------------------------------- C ABI
+static bool valid_rule(int rule, int64_t n) {
+  switch (rule) {
+    case TQ_RULE_TRAPEZOID:
+    case TQ_RULE_GAUSS:
+      return n >= 2;
+    case TQ_RULE_SIMPSON:
+      return n >= 3 && (n & 1) == 1;
+    case TQ_RULE_BOOLE:
+      return n >= 5 && (n - 1) % 4 == 0;
+    default:
+      return false;
+  }
+}
+
+static bool grid_total(int dim, int64_t n, int64_t* total) {
+  int64_t t = 1;
+  for (int k = 0; k < dim; ++k) {
+    if (t > (int64_t(1) << 62) / n) return false;
+    t *= n;
+  }
+  *total = t;
+  return true;
+}
+
+static constexpr int kStripF = 16, kStripD = 8;
+
+static int64_t fused_blocks(int64_t total, int strip) {
+  const int64_t need = (total + (int64_t)kBlock * strip - 1) / ((int64_t)kBlock * strip);
+  const int64_t cap = (int64_t)sm_count() * 8;
+  return need < 1 ? 1 : (need < cap ? need : cap);
+}
+
+extern "C" size_t tq_grid_fused_workspace_size(int rule, int dim, int64_t n_per_dim) {
+  (void)rule;
+  (void)dim;
+  (void)n_per_dim;
+  return reduce_ws_bytes((int64_t)sm_count() * 8);
+}
+
+extern "C" int tq_grid_fused(int dtype, int rule, int dim, int64_t n_per_dim, const void* domain,
+                             const double* gl_nodes, const double* gl_weights, int family,
+                             const double* params, void* out, int out_dtype, double* out64,
+                             void* workspace, size_t workspace_bytes, void* stream) {
+  if (!valid_dtype(dtype) || !valid_dtype(out_dtype)) return TQ_ERR_DTYPE;
+  if (dim < 1 || dim > kMaxDim) return TQ_ERR_DIM;
+  if (!valid_rule(rule, n_per_dim)) return TQ_ERR_RULE;
+  if (!domain || !params || !workspace || (!out && !out64)) return TQ_ERR_ARG;
+  if (rule == TQ_RULE_GAUSS && (!gl_nodes || !gl_weights)) return TQ_ERR_ARG;
+  int64_t total;
+  if (!grid_total(dim, n_per_dim, &total)) return TQ_ERR_TOO_LARGE;
+  const bool gl = rule == TQ_RULE_GAUSS;
+  const bool f64 = gl || dtype == TQ_F64;
+  const int64_t blocks = fused_blocks(total, f64 ? kStripD : kStripF);
+  if (workspace_bytes < reduce_ws_bytes(blocks)) return TQ_ERR_WORKSPACE;
+  FusedArgs a;
+  a.rule = rule;
+  a.dim = dim;
+  a.family = family;
+  a.n = n_per_dim;
+  a.total = total;
+  a.domain = domain;
+  a.gl_nodes = gl_nodes;
+  a.gl_weights = gl_weights;
+  a.params = params;
+  a.ticket = (unsigned*)workspace;
+  a.partials = (Acc*)((char*)workspace + 256);
+  a.out = out;
+  a.out_dtype = out_dtype;
+  a.out64 = out64;
+  cudaStream_t s = (cudaStream_t)stream;
+  const dim3 grid((unsigned)blocks);
+  TQ_DISPATCH_FAMILY(family, FAM, {
+    if (gl) {
+      if (dtype == TQ_F64)
+        grid_fused_kernel<double, double, true, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);
+      else
+        grid_fused_kernel<double, float, true, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);
+    } else if (dtype == TQ_F64) {
+      grid_fused_kernel<double, double, false, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);
+    } else {
+      grid_fused_kernel<float, float, false, FAM, kStripF><<<grid, kBlock, 0, s>>>(a);
+    }
+  });
+  return launch_status();
+}
+
+static int64_t stream_blocks(int64_t work) {
+  const int64_t need = (work + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)sm_count() * 16;
+  return need < 1 ? 1 : (need < cap ? need : cap);
+}
+
+extern "C" int tq_grid_points(int dtype, int rule, int dim, int64_t n_per_dim,
+                              const void* domain, const double* gl_nodes, int64_t start,
+                              int64_t count, void* points, void* stream) {
+  if (!valid_dtype(dtype)) return TQ_ERR_DTYPE;
+  if (dim < 1 || dim > kMaxDim) return TQ_ERR_DIM;
+  if (!valid_rule(rule, n_per_dim)) return TQ_ERR_RULE;
+  if (!domain || !points || start < 0 || count < 0) return TQ_ERR_ARG;
+  if (rule == TQ_RULE_GAUSS && !gl_nodes) return TQ_ERR_ARG;
+  int64_t total;
+  if (!grid_total(dim, n_per_dim, &total)) return TQ_ERR_TOO_LARGE;
+  if (start + count > total) return TQ_ERR_ARG;
+  if (count == 0) return TQ_OK;
+  PointsArgs a{rule, dim, n_per_dim, start, count, domain, gl_nodes, points};
+  cudaStream_t s = (cudaStream_t)stream;
+  const dim3 grid((unsigned)stream_blocks(count * dim));
+  if (rule == TQ_RULE_GAUSS) {
+    if (dtype == TQ_F64)
+      grid_points_kernel<double, double, true><<<grid, kBlock, 0, s>>>(a);
+    else
+      grid_points_kernel<double, float, true><<<grid, kBlock, 0, s>>>(a);
+  } else if (dtype == TQ_F64) {
+    grid_points_kernel<double, double, false><<<grid, kBlock, 0, s>>>(a);
+  } else {
+    grid_points_kernel<float, float, false><<<grid, kBlock, 0, s>>>(a);
+  }
+  return launch_status();
+}
+
+extern "C" int tq_grid_weights(int dtype, int rule, int dim, int64_t n_per_dim,
+                               const void* domain, const double* gl_weights, int64_t start,
+                               int64_t count, double* weights, void* stream) {
+  if (!valid_dtype(dtype)) return TQ_ERR_DTYPE;
+  if (dim < 1 || dim > kMaxDim) return TQ_ERR_DIM;
+  if (!valid_rule(rule, n_per_dim)) return TQ_ERR_RULE;
+  if (!domain || !weights || start < 0 || count < 0) return TQ_ERR_ARG;
+  if (rule == TQ_RULE_GAUSS && !gl_weights) return TQ_ERR_ARG;
+  int64_t total;
+  if (!grid_total(dim, n_per_dim, &total)) return TQ_ERR_TOO_LARGE;
+  if (start + count > total) return TQ_ERR_ARG;
+  if (count == 0) return TQ_OK;
+  WeightsArgs a{rule, dim, n_per_dim, start, count, domain, gl_weights, weights};
+  cudaStream_t s = (cudaStream_t)stream;
+  const dim3 grid((unsigned)stream_blocks(count));
+  if (rule == TQ_RULE_GAUSS) {
+    if (dtype == TQ_F64)
+      grid_weights_kernel<double, double, true><<<grid, kBlock, 0, s>>>(a);
+    else
+      grid_weights_kernel<double, float, true><<<grid, kBlock, 0, s>>>(a);
+  } else if (dtype == TQ_F64) {
+    grid_weights_kernel<double, double, false><<<grid, kBlock, 0, s>>>(a);
+  } else {
+    grid_weights_kernel<float, float, false><<<grid, kBlock, 0, s>>>(a);
+  }
+  return launch_status();
+}
+
+static constexpr int kStripW = 8;
+
+static int64_t wsum_blocks_x(int64_t count) {
+  const int64_t need = (count + (int64_t)kBlock * kStripW - 1) / ((int64_t)kBlock * kStripW);
+  const int64_t cap = (int64_t)sm_count() * 8;
+  return need < 1 ? 1 : (need < cap ? need : cap);
+}
+
+extern "C" size_t tq_weighted_sum_workspace_size(int64_t count, int64_t n_values) {
+  const int64_t gy = (n_values + kVals - 1) / kVals;
+  return reduce_ws_bytes(wsum_blocks_x(count) * gy * kVals);
+}
+
+extern "C" int tq_weighted_sum(int dtype, int rule, int dim, int64_t n_per_dim,
+                               const void* domain, const double* gl_weights, int64_t start,
+                               int64_t count, const void* f, int f_dtype, int64_t n_values,
+                               double* acc, void* workspace, size_t workspace_bytes,
+                               void* stream) {
+  if (!valid_dtype(dtype) || !valid_dtype(f_dtype)) return TQ_ERR_DTYPE;
+  if (dim < 1 || dim > kMaxDim) return TQ_ERR_DIM;
+  if (rule != TQ_RULE_MC && !valid_rule(rule, n_per_dim)) return TQ_ERR_RULE;
+  if (!domain || !f || !acc || !workspace || start < 0 || count < 0 || n_values < 1)
+    return TQ_ERR_ARG;
+  if (rule == TQ_RULE_GAUSS && !gl_weights) return TQ_ERR_ARG;
+  if (rule != TQ_RULE_MC) {
+    int64_t total;
+    if (!grid_total(dim, n_per_dim, &total)) return TQ_ERR_TOO_LARGE;
+    if (start + count > total) return TQ_ERR_ARG;
+  }
+  if (count == 0) return TQ_OK;
+  const int64_t gy = (n_values + kVals - 1) / kVals;
+  if (gy > 65535) return TQ_ERR_TOO_LARGE;
+  const int64_t gx = wsum_blocks_x(count);
+  if (workspace_bytes < reduce_ws_bytes(gx * gy * kVals)) return TQ_ERR_WORKSPACE;
+  WsumArgs a;
+  a.rule = rule;
+  a.dim = dim;
+  a.n = n_per_dim;
+  a.start = start;
+  a.count = count;
+  a.n_values = n_values;
+  a.domain = domain;
+  a.gl_weights = gl_weights;
+  a.f = f;
+  a.acc = acc;
+  a.ticket = (unsigned*)workspace;
+  a.partials = (Acc*)((char*)workspace + 256);
+  cudaStream_t s = (cudaStream_t)stream;
+  const dim3 grid((unsigned)gx, (unsigned)gy);
+  const bool gl = rule == TQ_RULE_GAUSS;
+#define TQ_WSUM(T, D, GLB)                                                             \
+  if (f_dtype == TQ_F64)                                                               \
+    weighted_sum_kernel<T, D, GLB, double, kStripW><<<grid, kBlock, 0, s>>>(a);        \
+  else                                                                                 \
+    weighted_sum_kernel<T, D, GLB, float, kStripW><<<grid, kBlock, 0, s>>>(a);
+  if (gl) {
+    if (dtype == TQ_F64) {
+      TQ_WSUM(double, double, true)
+    } else {
+      TQ_WSUM(double, float, true)
+    }
+  } else if (dtype == TQ_F64) {
+    TQ_WSUM(double, double, false)
+  } else {
+    TQ_WSUM(float, float, false)
+  }
+#undef TQ_WSUM
+  return launch_status();
+}
+
+extern "C" int tq_finalize_sum(int dtype, int rule, int dim, const void* domain, int64_t n_points,
+                               const double* acc, int64_t n_values, void* out, int out_dtype,
+                               void* stream) {
+  if (!valid_dtype(dtype) || !valid_dtype(out_dtype)) return TQ_ERR_DTYPE;
+  if (dim < 1) return TQ_ERR_DIM;
+  if (!domain || !acc || !out || n_values < 1 || n_points < 1) return TQ_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned blocks = (unsigned)((n_values + kBlock - 1) / kBlock);
+  if (dtype == TQ_F64)
+    finalize_kernel<double><<<blocks, kBlock, 0, s>>>(rule, dim, (const double*)domain, n_points,
+                                                      acc, n_values, out, out_dtype);
+  else
+    finalize_kernel<float><<<blocks, kBlock, 0, s>>>(rule, dim, (const float*)domain, n_points,
+                                                     acc, n_values, out, out_dtype);
+  return launch_status();
+}

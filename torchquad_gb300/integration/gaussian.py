@@ -1,0 +1,175 @@
+"""Gaussian and GaussLegendre (reference: integration/gaussian.py:6-162).
+
+Roots and weights come from ``numpy.polynomial.legendre.leggauss`` on the
+host in fp64, cached per N as the reference does (:110-129), and are
+uploaded once per device into a cached fp64 table that the kernels read.
+Nodes are ``(b-a)/2 * r + (a+b)/2`` computed in fp64 (the reference promotes
+to the fp64 roots), so results are fp64 whatever the domain dtype, as in the
+reference.
+
+A subclass that overrides ``_resize_roots``, ``_apply_composite_rule`` or
+``_grid_func`` (custom Gaussian rules) runs the reference's algorithm with
+torch operations on the device instead of the fused kernel.
+"""
+from __future__ import annotations
+
+import numpy
+import torch
+
+from .. import _lib as L
+from .grid_integrator import GridIntegrator
+
+
+class Gaussian(GridIntegrator):
+    """Gauss-Legendre on [-1, 1] by default; base of custom Gaussian rules.
+
+    As in the reference, the base class does not move the roots into the
+    domain (``_resize_roots`` is the identity) but scales each dimension's
+    sum by 0.5 * (b - a)."""
+
+    _rule = L.TQ_RULE_GAUSS
+    _rescales_nodes = False
+
+    def __init__(self):
+        super().__init__()
+        self.name = "Gauss-Legendre"
+        self._root_fn = numpy.polynomial.legendre.leggauss
+        self._root_args = ()
+        self._cache = {}
+        self._dev_cache = {}
+
+    def integrate(self, fn, dim, N=8, integration_domain=None, backend=None):
+        """Integrate fn with a tensor-product Gaussian rule of about N points."""
+        if self._is_custom():
+            return self._integrate_generic(fn, dim, N, integration_domain, backend)
+        return super().integrate(fn, dim, N, integration_domain, backend)
+
+    # ---- reference helper API (gaussian.py:44-129)
+    def _weights(self, N, dim, backend=None, requires_grad=False):
+        w = torch.as_tensor(self._cached_points_and_weights(N)[1], device=L.require_cuda())
+        w.requires_grad = requires_grad
+        return torch.prod(torch.stack(list(torch.meshgrid(*([w] * dim), indexing="ij")), dim=0), dim=0).ravel()
+
+    def _roots(self, N, backend=None, requires_grad=False):
+        roots = torch.as_tensor(self._cached_points_and_weights(N)[0], device=L.require_cuda())
+        if requires_grad:
+            roots.requires_grad = True
+        return roots
+
+    @property
+    def _grid_func(self):
+        def f(integration_domain, N, requires_grad=False, backend=None):
+            return self._resize_roots(integration_domain, self._roots(N, backend, requires_grad))
+
+        return f
+
+    def _resize_roots(self, integration_domain, roots):
+        return roots
+
+    def _cached_points_and_weights(self, N):
+        root_args = (N, *self._root_args)
+        if not isinstance(N, int):
+            if hasattr(N, "item"):
+                root_args = (N.item(), *self._root_args)
+            else:
+                raise NotImplementedError(f"N {N} is not an int and lacks an `item` method")
+        if root_args in self._cache:
+            return self._cache[root_args]
+        self._cache[root_args] = self._root_fn(*root_args)
+        return self._cache[root_args]
+
+    @staticmethod
+    def _apply_composite_rule(cur_dim_areas, dim, hs, domain):
+        for cur_dim in range(dim):
+            cur_dim_areas = 0.5 * (domain[cur_dim][1] - domain[cur_dim][0]) * torch.sum(
+                cur_dim_areas, dim=len(cur_dim_areas.shape) - 1
+            )
+        return cur_dim_areas
+
+    # ---- kernel plumbing
+    def _gl_tables(self, n, device):
+        key = (n, self._root_args, str(device))
+        t = self._dev_cache.get(key)
+        if t is None:
+            r, w = self._cached_points_and_weights(n)
+            t = (
+                torch.as_tensor(numpy.asarray(r, dtype=numpy.float64)).to(device),
+                torch.as_tensor(numpy.asarray(w, dtype=numpy.float64)).to(device),
+            )
+            self._dev_cache[key] = t
+        return t
+
+    def _result_dtype(self, domain):
+        return torch.float64
+
+    def _unit_domain(self, domain):
+        z = torch.empty_like(domain.detach())
+        z[:, 0] = -1.0
+        z[:, 1] = 1.0
+        return z
+
+    def _weight_scale(self, domain, dim):
+        return torch.prod(0.5 * (domain[:, 1] - domain[:, 0]))
+
+    def _points_from_unit(self, unit_pts, domain):
+        if not self._rescales_nodes:
+            return unit_pts
+        a, b = domain[:, 0], domain[:, 1]
+        return ((b - a) / 2).to(unit_pts.dtype) * unit_pts + ((a + b) / 2).to(unit_pts.dtype)
+
+    def _kernel_domain(self, domain):
+        # The base class keeps the roots on [-1, 1]: run the kernels there and
+        # scale the result by prod 0.5 (b - a) afterwards.
+        return domain if self._rescales_nodes else self._unit_domain(domain)
+
+    def _integrate_fused(self, fn, dim, n, domain):
+        out = super()._integrate_fused(fn, dim, n, self._kernel_domain(domain))
+        return out if self._rescales_nodes else out * self._weight_scale(domain, dim).to(out.dtype)
+
+    def _integrate_materialised(self, fn, dim, n, domain):
+        if self._rescales_nodes or (torch.is_grad_enabled() and domain.requires_grad):
+            return super()._integrate_materialised(fn, dim, n, domain)
+        out = super()._integrate_materialised(fn, dim, n, self._unit_domain(domain))
+        return out * self._weight_scale(domain, dim).to(out.dtype)
+
+    # ---- custom subclasses: the reference algorithm in torch operations
+    def _is_custom(self):
+        cls = type(self)
+        base = GaussLegendre if isinstance(self, GaussLegendre) else Gaussian
+        return (
+            cls._resize_roots is not base._resize_roots
+            or cls._apply_composite_rule is not Gaussian._apply_composite_rule
+            or type(self)._grid_func is not Gaussian._grid_func
+        )
+
+    def _integrate_generic(self, fn, dim, N, integration_domain, backend):
+        from .utils import _assemble_result
+
+        if N is None:
+            N = self._get_minimal_N(dim)
+        domain = self._prepare_domain(dim, N, integration_domain, backend)
+        n = int(N ** (1.0 / dim) + 1e-8)
+        grid_1d = [self._grid_func(domain[d], n, domain.requires_grad) for d in range(dim)]
+        hs = torch.stack([g[1] - g[0] for g in grid_1d])
+        mesh = torch.meshgrid(*grid_1d, indexing="ij")
+        points = torch.stack([m.ravel() for m in mesh], dim=1)
+        values, num = self.evaluate_integrand(fn, points, weights=self._weights(n, dim))
+        self._nr_of_fevals = num
+        shape = tuple(values.shape[1:])
+        v = values.reshape(num, -1).movedim(0, -1).reshape(-1, *([n] * dim))
+        out = self._apply_composite_rule(v, dim, hs, domain)
+        return _assemble_result(out.reshape(-1), shape, False) if not values.is_complex() else out.reshape(shape)
+
+
+class GaussLegendre(Gaussian):
+    """Gauss-Legendre quadrature on any domain [a, b]^dim."""
+
+    _rescales_nodes = True
+
+    def __init__(self):
+        super().__init__()
+
+    def _resize_roots(self, integration_domain, roots):
+        a = integration_domain[0]
+        b = integration_domain[1]
+        return ((b - a) / 2) * roots + ((a + b) / 2)
