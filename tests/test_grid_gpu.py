@@ -114,7 +114,7 @@ def test_non_vectorised_integrand_raises(cuda):
 
 def test_chunked_materialised_path_equals_single_chunk(cuda):
     f = tq.GaussianPeak(3, a=[2.0, 1.0, 3.0], u=[0.2, 0.5, 0.7])
-    dom = [[0.0, 1.0]] * 3
+    dom = torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float64, device=cuda)
     full = tq.Boole().integrate(lambda x: f(x), 3, N=41**3, integration_domain=dom)
     tq.set_materialise_budget(1 << 16)
     try:
@@ -126,5 +126,6 @@ def test_chunked_materialised_path_equals_single_chunk(cuda):
 
 def test_large_fused_c1_full_size(cuda):
     # plain Simpson at its full 101^3 fp64 size against the reference value
-    v = tq.Simpson().integrate(tq.ExpSum(3), 3, N=1030301, integration_domain=[[0.0, 1.0]] * 3)
+    dom = torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float64, device=cuda)
+    v = tq.Simpson().integrate(tq.ExpSum(3), 3, N=1030301, integration_domain=dom)
     assert abs(v.item() - 5.073214112618379) <= 1e-12 * 5.08

@@ -97,29 +97,6 @@ struct FusedArgs {
   double* out64;
 };
 
-template <typename T, int P>
-struct StripAcc;  // inner accumulation type of a strip
-template <int P>
-struct StripAcc<float, P> {
-  AccF a{0.f, 0.f};
-  __device__ void add(float x) { accf_add(a, x); }
-  __device__ double take() {
-    const double r = (double)a.s + (double)a.c;
-    a.s = a.c = 0.f;
-    return r;
-  }
-};
-template <int P>
-struct StripAcc<double, P> {
-  double a = 0.0;
-  __device__ void add(double x) { a += x; }
-  __device__ double take() {
-    const double r = a;
-    a = 0.0;
-    return r;
-  }
-};
-
 __device__ __forceinline__ void write_result(void* out, int out_dtype, double* out64,
                                              double v) {
   if (out) {
@@ -131,94 +108,133 @@ __device__ __forceinline__ void write_result(void* out, int out_dtype, double* o
   if (out64) *out64 = v;
 }
 
-// Decodes flat row index `row` (= node index / n) into the outer digits and
-// returns (s_outer, w_outer): s_outer = g_0 + ... + g_{d-2} summed in
-// dimension order, w_outer = prod of the outer 1-D weights.
-template <typename T, bool GL, int FAM>
-__device__ __forceinline__ void outer_state(const Geo<T>& g, const Family<T>& fam, int rule,
-                                            int dim, int64_t n, uint64_t row,
-                                            const double* gl_nodes, const double* gl_w,
-                                            bool small, T& s_outer, double& w_outer) {
-  T terms[kMaxDim];
-  double w = 1.0;
-#pragma unroll
-  for (int k = kMaxDim - 2; k >= 0; --k) {
-    if (k < dim - 1) {
-      uint64_t digit;
-      if (small) {
-        const uint32_t r32 = (uint32_t)row, q = r32 / (uint32_t)n;
-        digit = r32 - q * (uint32_t)n;
-        row = q;
-      } else {
-        const uint64_t q = row / (uint64_t)n;
-        digit = row - q * (uint64_t)n;
-        row = q;
-      }
-      const T x = node_at<T, GL>(g, k, n, (int64_t)digit, gl_nodes);
-      terms[k] = fam_term<FAM, T>(fam, k, x);
-      w *= g.wscale[k] * wunit_at<GL>(rule, n, (int64_t)digit, gl_w);
-    } else {
-      terms[k] = T(0);
-    }
-  }
-  T s = terms[0];
-#pragma unroll
-  for (int k = 1; k < kMaxDim - 1; ++k)
-    if (k < dim - 1) s = s + terms[k];
-  s_outer = s;
-  w_outer = w;
+// Integer Newton-Cotes coefficient of node j, the rule fixed at compile time.
+template <int RULE>
+__device__ __forceinline__ int nc_int_t(int j, int n) {
+  if (j == 0 || j == n - 1) return RULE == TQ_RULE_TRAPEZOID ? 1 : (RULE == TQ_RULE_SIMPSON ? 1 : 7);
+  if (RULE == TQ_RULE_TRAPEZOID) return 2;
+  if (RULE == TQ_RULE_SIMPSON) return (j & 1) ? 4 : 2;
+  const int m = j & 3;
+  return (m & 1) ? 32 : (m == 2 ? 12 : 14);
 }
 
-template <typename T, typename D, bool GL, int FAM, int P>
-__global__ void __launch_bounds__(kBlock) grid_fused_kernel(FusedArgs args) {
+// Compensated sum of one row segment in the working type: Kahan's original
+// four-operation update for fp32, plain accumulation for fp64 (a segment is
+// at most n terms of one row).
+template <typename T>
+struct SegSum;
+template <>
+struct SegSum<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <>
+struct SegSum<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+// Outer-dimension state of a grid row (flat node index / n): the partial
+// separable sum g_0 + ... + g_{d-2} in dimension order and the product of
+// the outer 1-D weights.  rstride[k] = n^(dim-2-k).
+template <typename T, int RULE, int FAM>
+__device__ __forceinline__ void outer_state(const Geo<T>& g, const Family<T>& fam,
+                                            const uint64_t* rstride, int dim, int64_t n,
+                                            uint64_t row, const double* gl_nodes,
+                                            const double* gl_w, bool small, T& s_out,
+                                            double& w_out) {
+  constexpr bool GL = RULE == TQ_RULE_GAUSS;
+  T s = T(0);
+  double w = 1.0;
+#pragma unroll 1
+  for (int k = 0; k < dim - 1; ++k) {
+    uint64_t digit;
+    if (small) {
+      const uint32_t q = (uint32_t)row / (uint32_t)rstride[k];
+      digit = q % (uint32_t)n;
+    } else {
+      digit = (row / rstride[k]) % (uint64_t)n;
+    }
+    const T x = node_at<T, GL>(g, k, n, (int64_t)digit, gl_nodes);
+    const T t = fam_term<FAM, T>(fam, k, x);
+    s = (k == 0) ? t : s + t;
+    w *= g.wscale[k] *
+         (GL ? __ldg(gl_w + digit) : (double)nc_int_t<RULE>((int)digit, (int)n));
+  }
+  s_out = s;
+  w_out = w;
+}
+
+template <typename T, typename D, int RULE, int FAM, int P>
+__global__ void __launch_bounds__(kBlock, 2) grid_fused_kernel(FusedArgs args) {
+  constexpr bool GL = RULE == TQ_RULE_GAUSS;
   __shared__ Geo<T> g;
   __shared__ Family<T> fam;
+  __shared__ uint64_t rstride[kMaxDim];
   if (threadIdx.x == 0) {
-    geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
+    geo_setup<T, D>(g, RULE, args.dim, args.n, (const D*)args.domain);
     load_family<T>(fam, args.family, args.dim, args.params);
+    uint64_t st = 1;
+    for (int k = args.dim - 2; k >= 0; --k) {
+      rstride[k] = st;
+      st *= (uint64_t)args.n;
+    }
   }
   __syncthreads();
-  const int dim = args.dim, rule = args.rule, last = dim - 1;
+  const int dim = args.dim, last = dim - 1;
   const int64_t n = args.n, total = args.total;
+  const int n32 = (int)n;  // n <= total < 2^62 but a row index fits int for n < 2^31
   const bool small = total < (int64_t(1) << 32);
   const double* gl_nodes = args.gl_nodes;
   const double* gl_w = args.gl_weights;
   const double wlast = g.wscale[last];
+  const T a_l = g.a[last], b_l = g.b[last], st_l = g.step[last];
+  const int half = n32 / 2;
 
   Acc acc{0.0, 0.0};
-  StripAcc<T, P> inner;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * P; base < total;
        base += nthreads * P) {
     uint64_t row;
-    int64_t jl;
+    int jl;
     if (small) {
-      const uint32_t b32 = (uint32_t)base, q = b32 / (uint32_t)n;
+      const uint32_t q = (uint32_t)base / (uint32_t)n;
       row = q;
-      jl = b32 - q * (uint32_t)n;
+      jl = (int)((uint32_t)base - q * (uint32_t)n);
     } else {
       row = (uint64_t)base / (uint64_t)n;
-      jl = base - (int64_t)row * n;
+      jl = (int)(base - (int64_t)row * n);
     }
-    T s_outer;
-    double w_outer;
-    outer_state<T, GL, FAM>(g, fam, rule, dim, n, row, gl_nodes, gl_w, small, s_outer,
-                            w_outer);
-    const int64_t end = min(base + P, total);
-    for (int64_t idx = base; idx < end; ++idx) {
-      if (jl == n) {  // carry into the outer dimensions
-        acc_add(acc, inner.take() * (w_outer * wlast));
-        ++row;
-        jl = 0;
-        outer_state<T, GL, FAM>(g, fam, rule, dim, n, row, gl_nodes, gl_w, small, s_outer,
+    int64_t left = min((int64_t)P, total - base);
+    while (left > 0) {
+      T s_outer;
+      double w_outer;
+      outer_state<T, RULE, FAM>(g, fam, rstride, dim, n, row, gl_nodes, gl_w, small, s_outer,
                                 w_outer);
+      const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
+      SegSum<T> seg;
+      for (int j = jl; j < seg_end; ++j) {
+        T x;
+        if (GL)
+          x = (T)__dadd_rn(__dmul_rn(g.half[last], __ldg(gl_nodes + j)), g.mid[last]);
+        else
+          x = (j < half) ? fma(st_l, (T)j, a_l) : fma(-st_l, (T)(n32 - 1 - j), b_l);
+        const T f = fam_outer<FAM, T>(fam, s_outer + fam_term<FAM, T>(fam, last, x));
+        const T wj = GL ? (T)__ldg(gl_w + j) : (T)nc_int_t<RULE>(j, n32);
+        seg.add(wj * f);
       }
-      const T x = node_at<T, GL>(g, last, n, jl, gl_nodes);
-      const T f = fam_outer<FAM, T>(fam, s_outer + fam_term<FAM, T>(fam, last, x));
-      inner.add((T)wunit_at<GL>(rule, n, jl, gl_w) * f);
-      ++jl;
+      acc_add(acc, seg.value() * (w_outer * wlast));
+      left -= seg_end - jl;
+      jl = 0;
+      ++row;
     }
-    acc_add(acc, inner.take() * (w_outer * wlast));
   }
 
   acc = block_reduce<kBlock>(acc);
@@ -426,7 +442,7 @@ static bool grid_total(int dim, int64_t n, int64_t* total) {
   return true;
 }
 
-static constexpr int kStripF = 16, kStripD = 8;
+static constexpr int kStripF = 32, kStripD = 16;
 
 static int64_t fused_blocks(int64_t total, int strip) {
   const int64_t need = (total + (int64_t)kBlock * strip - 1) / ((int64_t)kBlock * strip);
@@ -473,18 +489,31 @@ extern "C" int tq_grid_fused(int dtype, int rule, int dim, int64_t n_per_dim, co
   a.out64 = out64;
   cudaStream_t s = (cudaStream_t)stream;
   const dim3 grid((unsigned)blocks);
+#define TQ_FUSED_RULE(RULEC)                                                              \
+  if (gl) {                                                                                \
+    if (dtype == TQ_F64)                                                                   \
+      grid_fused_kernel<double, double, RULEC, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);   \
+    else                                                                                   \
+      grid_fused_kernel<double, float, RULEC, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);    \
+  } else if (dtype == TQ_F64) {                                                            \
+    grid_fused_kernel<double, double, RULEC, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);     \
+  } else {                                                                                 \
+    grid_fused_kernel<float, float, RULEC, FAM, kStripF><<<grid, kBlock, 0, s>>>(a);       \
+  }
   TQ_DISPATCH_FAMILY(family, FAM, {
-    if (gl) {
-      if (dtype == TQ_F64)
-        grid_fused_kernel<double, double, true, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);
-      else
-        grid_fused_kernel<double, float, true, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);
-    } else if (dtype == TQ_F64) {
-      grid_fused_kernel<double, double, false, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);
-    } else {
-      grid_fused_kernel<float, float, false, FAM, kStripF><<<grid, kBlock, 0, s>>>(a);
+    switch (rule) {
+      case TQ_RULE_TRAPEZOID: { TQ_FUSED_RULE(TQ_RULE_TRAPEZOID) } break;
+      case TQ_RULE_SIMPSON: { TQ_FUSED_RULE(TQ_RULE_SIMPSON) } break;
+      case TQ_RULE_BOOLE: { TQ_FUSED_RULE(TQ_RULE_BOOLE) } break;
+      default: {
+        if (dtype == TQ_F64)
+          grid_fused_kernel<double, double, TQ_RULE_GAUSS, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);
+        else
+          grid_fused_kernel<double, float, TQ_RULE_GAUSS, FAM, kStripD><<<grid, kBlock, 0, s>>>(a);
+      }
     }
   });
+#undef TQ_FUSED_RULE
   return launch_status();
 }
 
