@@ -1,0 +1,396 @@
+"""Benchmark: plain VEGAS on one GB300 (and N independent replicas on N GPUs).
+
+Workload (the configuration the headline metric is quoted on): VEGAS+,
+dim 6, N = 1e7 evaluations budget (max_iterations 20), 50 map intervals per
+dimension, default stratification (6^6 cubes), fp32 points with fp64
+compensated sums, integrand prod_i N(x_i; 0.5, 0.05) on [0,1]^6 (value ~1),
+seeds 0, 1, 2, ... per step.  A step is one full VEGAS integration.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Our arm prints one JSON line: ``value`` = integrand evaluations per second
+over the timed steps with inputs resident on the device; ``e2e`` = the same
+metric through the public API with the domain given as a host list and the
+result read back to the host every step; ``roofline`` for the dominant
+kernel (the fused VEGAS sampler) against an FP32 FMA peak measured in the
+same run; ``cpu_baseline`` = the CPU oracle (numpy restatement of the
+reference) on the host, one process.
+
+``--impl reference`` times the reference algorithm on the host cores
+instead (the numpy restatement; the reference itself is pure Python over
+torch and not installable on the GPU host): each step runs one integration
+per host core in parallel processes.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DIM, N_EVALS, N_BINS, SIGMA = 6, 10_000_000, 50, 0.05
+METRIC = "integrand evals/s (plain VEGAS, dim 6, N=1e7, 50 bins, fp32 + fp64 sums)"
+UNIT = "evals/s"
+CONFIG = {
+    "workload": "plain VEGAS+ dim=6 N=1e7 budget, 50 map bins/dim, default stratification (6^6 cubes), "
+                "Gaussian peak sigma=0.05 on [0,1]^6, fp32 points with fp64 compensated sums, one integration per step",
+    "dim": DIM,
+    "N": N_EVALS,
+    "n_bins": N_BINS,
+    "max_iterations": 20,
+    "integrand": "prod_i exp(-(x_i-0.5)^2/(2*0.05^2))/(0.05*sqrt(2*pi))",
+    "l2": "flushed (256 MiB write) between timed steps, outside the per-step CUDA events",
+}
+
+
+def _dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ----------------------------------------------------------- CPU (oracle)
+def _oracle_one(seed):
+    import numpy as np
+
+    from oracle import integrands as OI
+    from oracle import philox as OP
+    from oracle import vegas as OV
+
+    a = 1.0 / (2.0 * SIGMA * SIGMA)
+    c = (1.0 / (SIGMA * math.sqrt(2.0 * math.pi))) ** DIM
+    params = np.array([c, 0.0] + [a] * DIM + [0.5] * DIM)
+    v = OV.Vegas()
+    t0 = time.perf_counter()
+    r = v.integrate(lambda x: OI.evaluate(2, params, x), DIM, N_EVALS, [[0.0, 1.0]] * DIM,
+                    OP.ReplayStream(seed), dt=np.float32, n_intervals=N_BINS)
+    return v.fevals, time.perf_counter() - t0, r
+
+
+def run_reference(args):
+    """CPU arm: the reference algorithm (numpy restatement) on all host cores."""
+    ws, rank, _ = _dist_env()
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for w in range(args.warmup):
+            pool.map(_oracle_one, [1000 + w * cores + i for i in range(cores)])
+        times, evals = [], 0
+        t_all = time.perf_counter()
+        for k in range(args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_oracle_one, [k * cores + i for i in range(cores)])
+            times.append(time.perf_counter() - t0)
+            evals += sum(r[0] for r in res)
+        total = time.perf_counter() - t_all
+    value = evals / total
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": CONFIG,
+        "cpu_baseline": {
+            "value": value,
+            "unit": UNIT,
+            "cores": cores,
+            "kind": "port",
+            "sample": f"each step: {cores} full integrations of the workload in parallel processes "
+                      "(numpy restatement of the reference, one per host core)",
+        },
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def cpu_baseline_sample(budget_s=20.0):
+    evals, t = 0, 0.0
+    n = 0
+    while t < budget_s and n < 8:
+        e, dt, _ = _oracle_one(500 + n)
+        evals += e
+        t += dt
+        n += 1
+    return {
+        "value": evals / t,
+        "unit": UNIT,
+        "cores": 1,
+        "kind": "port",
+        "sample": f"{n} full integrations of the workload, numpy restatement of the reference, one process",
+    }
+
+
+# --------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, path, index):
+        self.path, self.index, self.proc = path, index, None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# --------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import torchquad_gb300 as tq
+    from torchquad_gb300 import _lib as L
+    from torchquad_gb300.integration import vegas as V
+
+    dev = torch.device("cuda", local)
+    f = tq.GaussianPeak.normal(DIM, 0.5, SIGMA)
+    domain_dev = torch.tensor([[0.0, 1.0]] * DIM, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def one(seed, domain):
+        v = tq.VEGAS()
+        r = v.integrate(f, DIM, N=N_EVALS, integration_domain=domain, seed=seed, n_intervals=N_BINS)
+        return v, r
+
+    # kernel timing on the sampler's stream (the current stream)
+    sampler_events = []
+    orig_iter = V.VegasDevice.iterate_fused
+
+    def timed_iterate(self, *a, **k):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        orig_iter(self, *a, **k)
+        e1.record()
+        sampler_events.append((e0, e1, self))
+
+    for w in range(args.warmup):
+        one(10_000 + w, domain_dev)
+    barrier()
+
+    # ---- device-resident inputs
+    V.VegasDevice.iterate_fused = timed_iterate
+    clocks = ClockSampler(str(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv") if (ROOT / "gpurun_out").is_dir()
+                          else f"/tmp/tq_clocks_{rank}.csv", local)
+    step_ms, evals, sampler_points = [], 0, []
+    launches0 = L.launches[0]
+    with clocks:
+        barrier()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            n_before = len(sampler_events)
+            e0.record()
+            v, r = one(rank * 1_000_003 + k, domain_dev)
+            e1.record()
+            torch.cuda.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            evals += v._nr_of_fevals
+            stats = v._dev.stats[: v.it, 2].cpu()
+            for j, (_, _, _) in enumerate(sampler_events[n_before:]):
+                sampler_points.append(float(stats[j]))
+        barrier()
+    launches = L.launches[0] - launches0
+    V.VegasDevice.iterate_fused = orig_iter
+    t_local = sum(step_ms) / 1000.0
+    sampler_ms = [a.elapsed_time(b) for a, b, _ in sampler_events]
+
+    # ---- end to end through the public API with host inputs
+    e2e_ms, e2e_evals = [], 0
+    h2d = 2 * DIM * 4 + (2 + 2 * DIM) * 8 + 8  # domain, integrand parameters, RNG offset
+    d2h_per = []
+    barrier()
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f_host = tq.GaussianPeak.normal(DIM, 0.5, SIGMA)  # parameters uploaded inside the step
+        v = tq.VEGAS()
+        r = v.integrate(f_host, DIM, N=N_EVALS, integration_domain=[[0.0, 1.0]] * DIM, seed=rank * 7 + k,
+                        n_intervals=N_BINS)
+        val = r.item()
+        e2e_ms.append((time.perf_counter() - t0) * 1000.0)
+        e2e_evals += v._nr_of_fevals
+        # per abort test: stats of all iterations so far + flags; then offset and result
+        checks = v.it // 5
+        d2h_per.append(sum(32 * 5 * (i + 1) + 16 for i in range(checks)) + 8 + 4)
+        assert math.isfinite(val)
+    barrier()
+
+    # ---- FP32 FMA peak (measured in this run)
+    out = torch.zeros(1, dtype=torch.float32, device=dev)
+    import ctypes
+
+    flops = ctypes.c_double(0.0)
+    peaks = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        L.check(L.lib().tq_fp32_fma_probe(4096, 8, out.data_ptr(), ctypes.byref(flops), L.stream_handle()),
+                "tq_fp32_fma_probe")
+        e1.record()
+        torch.cuda.synchronize()
+        peaks.append(flops.value / (e0.elapsed_time(e1) / 1000.0) / 1e12)
+    fp32_peak = max(peaks)
+
+    # ---- reduce over ranks
+    t_max = t_local
+    e2e_t = sum(e2e_ms) / 1000.0
+    tot_evals, tot_e2e = evals, e2e_evals
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([t_local, e2e_t], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        n = torch.tensor([float(evals), float(e2e_evals)], dtype=torch.float64, device=dev)
+        dist.all_reduce(n, op=dist.ReduceOp.SUM)
+        t_max, e2e_t = float(t[0]), float(t[1])
+        tot_evals, tot_e2e = int(n[0]), int(n[1])
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+        return 0
+
+    # algorithmic FP32 work of one sampled point (d = 6); see the design doc
+    flops_per_point = 16 * DIM + 7
+    pts = sum(sampler_points) / max(1, len(sampler_points))
+    avg_ms = sum(sampler_ms) / max(1, len(sampler_ms))
+    achieved = flops_per_point * pts / (avg_ms / 1000.0) / 1e12
+    line = {
+        "metric": METRIC,
+        "value": tot_evals / t_max,
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * t_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {**CONFIG, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "e2e": {
+            "value": tot_e2e / e2e_t,
+            "unit": UNIT,
+            "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": int(statistics.mean(d2h_per)),
+            "ms_per_step": statistics.mean(e2e_ms),
+        },
+        "roofline": {
+            "kernel": "vegas_sample_kernel (fused stratified iteration)",
+            "bound": "fp32",
+            "achieved": achieved,
+            "peak": fp32_peak,
+            "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak,
+            "traffic": None,
+            "peak_source": "FP32 FMA probe kernel measured in this run (MEASURED_PEAKS.json has HBM and bf16 only)",
+            "points_per_launch": pts,
+            "avg_launch_us": avg_ms * 1000.0,
+            "flops_per_point": flops_per_point,
+        },
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "evals_per_step": tot_evals / (args.steps * ws),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=20.0)
+    args = p.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    from __graft_entry__ import build
+
+    build()
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

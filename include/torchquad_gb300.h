@@ -163,6 +163,118 @@ int tq_mc_fused(int dtype, int dim, int64_t n_points, const void* domain,
                 uint64_t stream_id, uint64_t offset, void* out, double* out64,
                 void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- VEGAS+ (vegas.py, vegas_map.py, vegas_stratification.py) ---------- */
+
+/* Device state of one VEGAS integration.  All arrays are caller-owned
+ * device memory; "dtype" arrays use the state's dtype.  The adaptive map
+ * lives on the unit cube [0,1]^dim; `domain` maps it onto the integration
+ * domain as vegas.py:105-112 does. */
+typedef struct tq_vegas_state {
+  int32_t dim;          /* d, 1..TQ_MAX_DIM                                    */
+  int32_t dtype;        /* TQ_F32 / TQ_F64                                     */
+  int64_t n_bins;       /* B, map intervals per dimension (vegas.py:117)       */
+  int64_t n_strat;      /* stratification steps per dimension                 */
+  int64_t n_cubes;      /* n_strat^dim                                         */
+  void* x_edges;        /* [d][B+1] dtype    VEGASMap.x_edges                  */
+  void* dx_edges;       /* [d][B]   dtype    VEGASMap.dx_edges                 */
+  double* weights;      /* [d][B]   sum of (f*jac)^2 per interval (fp64)       */
+  int64_t* counts;      /* [d][B]   samples per interval                       */
+  void* dh;             /* [n_cubes] dtype   VEGASStratification.dh            */
+  double* jf;           /* [n_cubes] sum of f*jac per cube (fp64)              */
+  double* jf2;          /* [n_cubes] sum of (f*jac)^2 per cube (fp64)          */
+  int64_t* neval;       /* [n_cubes] evaluations per cube                     */
+  int64_t* cube_start;  /* [n_cubes+1] exclusive prefix of neval; last = total */
+  uint64_t* rng_offset; /* [1] Philox block offset; the sampling kernels
+                         * advance it by the blocks their draws consumed       */
+  double* stats;        /* [n_slots][4]: result, sigma2, points, (unused)      */
+  int32_t* flags;       /* [4]: [0] map updates skipped (all-zero weights),
+                         * [1] infinite edges repaired, [2] unrepairable edges */
+  double* scalars;      /* [4]: [0] sum of the unnormalised dh              */
+  const void* domain;   /* [d][2] dtype                                        */
+} tq_vegas_state;
+
+/* Scratch bytes the VEGAS entry points need for this state. */
+size_t tq_vegas_workspace_size(const tq_vegas_state* st);
+
+/* VEGASMap.__init__/_reset_weight (vegas_map.py:15-42,174-183) and the
+ * initial VEGASStratification.dh (vegas_stratification.py:13-44). */
+int tq_vegas_init(const tq_vegas_state* st, void* stream);
+
+/* One warm-up iteration, fused (vegas.py:228-256 without the map update):
+ * y = u * 0.999999 with u from the Philox stream (seed, stream_id,
+ * *st->rng_offset), x = map(y), f = integrand(domain(x)) * volume,
+ * accumulate (f*jac)^2 into the map.  Advances *st->rng_offset. */
+int tq_vegas_warmup_fused(const tq_vegas_state* st, int family, const double* params,
+                          int64_t n_samples, uint64_t seed, uint64_t stream_id,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
+/* VEGASMap.update_map (vegas_map.py:185-261) incl. _smooth_map (:113-172);
+ * resets weights and counts.  Sets flags[0] if a dimension's weights are all
+ * zero (map left unchanged), flags[1]/[2] for repaired/unrepairable
+ * infinite edges. */
+int tq_vegas_update_map(const tq_vegas_state* st, double alpha, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/* VEGASMap._smooth_map (vegas_map.py:113-172) alone: writes the smoothed,
+ * range-compressed weights [d][B] (dtype) of the current weights/counts to
+ * `smoothed`; map, weights and counts are left unchanged. */
+int tq_vegas_smooth_weights(const tq_vegas_state* st, double alpha, void* smoothed,
+                            void* workspace, size_t workspace_bytes, void* stream);
+
+/* VEGASStratification.get_NH (vegas_stratification.py:92-103):
+ * neval = max(2, floor(dh * nevals_exp)), cube_start = exclusive prefix,
+ * cube_start[n_cubes] = total; zeroes jf/jf2.  If `normalize` != 0 the dh
+ * left unnormalised by tq_vegas_finish_iteration is first divided by its sum
+ * (vegas_stratification.py:88-90). */
+int tq_vegas_get_nh(const tq_vegas_state* st, int64_t nevals_exp, int normalize,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
+/* One stratified iteration, fused (vegas.py:274-291): for every point of
+ * every cube (cube_start order), y = (cube position + u) / n_strat
+ * (get_Y, vegas_stratification.py:140-165), x and jac from the map
+ * (get_X/get_Jac, vegas_map.py:44-74), f = integrand(domain(x)) * volume;
+ * accumulates the map weights/counts (if use_grid_improve) and the per-cube
+ * sums jf/jf2 (accumulate_weight, vegas_stratification.py:46-70).
+ * max_points bounds cube_start[n_cubes] for sizing the launch.
+ * Advances *st->rng_offset. */
+int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, const double* params,
+                           uint64_t seed, uint64_t stream_id, int use_grid_improve,
+                           int64_t max_points, void* workspace, size_t workspace_bytes,
+                           void* stream);
+
+/* Per-cube estimates -> stats[slot] = {sum ih, sum sig2/n, points}
+ * (vegas.py:293-303, fp64 compensated sums) and the unnormalised dampened
+ * counts dh (update_DH, vegas_stratification.py:72-90; the division by the
+ * sum happens in the next tq_vegas_get_nh). */
+int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, int64_t slot,
+                              void* workspace, size_t workspace_bytes, void* stream);
+
+/* Materialised path (arbitrary torch integrands, injected uniforms). */
+
+/* y[M][d] = stratified points from uniforms u[M][d] (get_Y); M must equal
+ * cube_start[n_cubes]. */
+int tq_vegas_strat_points(const tq_vegas_state* st, const void* u, int64_t n_points, void* y,
+                          void* stream);
+/* x[M][d] = map(y), jac[M] = Jacobian (get_X, get_Jac), both dtype. */
+int tq_vegas_map_points(const tq_vegas_state* st, const void* y, int64_t n_points, void* x,
+                        void* jac, void* stream);
+/* accumulate_map: weights[k][ID_k(y)] += vals, counts += 1
+ * (VEGASMap.accumulate_weight, vegas_map.py:99-111, which receives (f*jac)^2);
+ * stratified: jf[c] += vals, jf2[c] += vals^2 over the cubes in cube_start
+ * order (VEGASStratification.accumulate_weight, :46-70, which receives
+ * f*jac).  vals is dtype [M]. */
+int tq_vegas_accumulate(const tq_vegas_state* st, const void* y, const void* vals,
+                        int64_t n_points, int accumulate_map, int stratified,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- measurement ---------------------------------------------------------- */
+
+/* FP32 FMA throughput probe (no reference counterpart; used by the benchmark
+ * to measure the FP32 roofline): launches sm_count*blocks_per_sm CTAs doing
+ * iters*128 dependent-free FMAs per thread; *flops receives the flop count. */
+int tq_fp32_fma_probe(int64_t iters, int blocks_per_sm, float* out, double* flops,
+                      void* stream);
+
 #ifdef __cplusplus
 }
 #endif

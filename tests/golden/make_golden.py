@@ -180,6 +180,131 @@ def gen_mc(tq):
     return out
 
 
+def _vegas_spec():
+    return dict(kind="GaussianPeak", a=[5.0, 8.0, 3.0], u=[0.3, 0.5, 0.7], c=1.0)
+
+
+def gen_vegas_steps(tq):
+    """Reference VEGAS state before/after stratified iterations, on the
+    Philox draws, for step-wise parity (d=3, N=20000)."""
+    import torch
+    from torchquad.integration import vegas as V
+
+    out = []
+    dom = [[0.0, 1.0], [-1.0, 1.0], [0.0, 2.0]]
+    for dtype in ["float32", "float64"]:
+        dt = getattr(torch, dtype)
+        f = make_integrand(_vegas_spec(), 3)
+        integ = tq.VEGAS()
+        records = []
+        orig_run = V.VEGAS._run_iteration
+
+        def run(self):
+            pre = dict(x_edges=self.map.x_edges.clone(), dx_edges=self.map.dx_edges.clone(),
+                       dh=self.strat.dh.clone(), starting_N=self._starting_N, it=self.it,
+                       rng_offset=self.rng.stream.offset)
+            snap = {}
+            orig_update = self.map.update_map
+
+            def upd():
+                snap["counts"] = self.map.counts.clone()
+                snap["weights"] = self.map.weights.clone()
+                orig_update()
+
+            self.map.update_map = upd
+            acc = orig_run(self)
+            del self.map.update_map
+            rec = dict(pre=pre, counts=snap["counts"], weights=snap["weights"],
+                       neval=self.strat.strat_counts.to(torch.int64).clone(), JF=self.strat.JF.clone(),
+                       JF2=self.strat.JF2.clone(), result=self.results[-1].item(), sigma2=self.sigma2[-1].item(),
+                       x_edges_new=self.map.x_edges.clone(), dh_new=self.strat.dh.clone())
+            records.append(rec)
+            return acc
+
+        V.VEGAS._run_iteration = run
+        try:
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                val = integ.integrate(f, 3, N=20000, integration_domain=torch.tensor(dom, dtype=dt),
+                                      rng=ReplayRNG(11))
+        finally:
+            V.VEGAS._run_iteration = orig_run
+
+        def pack(t):
+            return dict(shape=list(t.shape), values=hexarr(t.double().numpy()))
+
+        steps = []
+        for i in (0, 1, 5):
+            r = records[i]
+            steps.append(dict(
+                it=r["pre"]["it"] + 1, starting_N=r["pre"]["starting_N"], rng_offset=r["pre"]["rng_offset"],
+                x_edges=pack(r["pre"]["x_edges"]), dx_edges=pack(r["pre"]["dx_edges"]), dh=pack(r["pre"]["dh"]),
+                neval=[int(v) for v in r["neval"]], counts=[int(v) for v in r["counts"].ravel()],
+                weights=pack(r["weights"]), JF=pack(r["JF"]), JF2=pack(r["JF2"]),
+                result=hexf(r["result"]), sigma2=hexf(r["sigma2"]),
+                x_edges_new=pack(r["x_edges_new"]), dh_new=pack(r["dh_new"])))
+        out.append(dict(dtype=dtype, domain=dom, N=20000, seed=11, family=_vegas_spec(),
+                        params=hexarr(f.params_vector().numpy()), n_bins=integ.map.N_intervals,
+                        n_strat=integ.strat.N_strat, value=hexf(val.item()), fevals=int(integ._nr_of_fevals),
+                        iterations=int(integ.it), steps=steps))
+    return out
+
+
+def gen_vegas_c2(tq):
+    """Plain VEGAS at full size: dim 6, N = 1e7, 50 map intervals, fp32,
+    normal peak sigma 0.05, seed 0, draws from the Philox stream."""
+    import torch
+    import torchquad_gb300.integrands as I
+    from torchquad.integration import vegas as V
+
+    class Map50(V.VEGASMap):
+        def __init__(self, N_intervals, dim, backend, dtype, alpha=0.5):
+            super().__init__(50, dim, backend, dtype, alpha)
+
+    f = I.GaussianPeak.normal(6, 0.5, 0.05)
+    iters = []
+    orig_run = V.VEGAS._run_iteration
+
+    def run(self):
+        acc = orig_run(self)
+        iters.append(dict(M=int(self.strat.strat_counts.sum().item()), result=hexf(self.results[-1].item()),
+                          sigma2=hexf(self.sigma2[-1].item())))
+        return acc
+
+    V.VEGAS._run_iteration = run
+    orig_map = V.VEGASMap
+    V.VEGASMap = Map50
+    try:
+        integ = tq.VEGAS()
+        dom = torch.tensor([[0.0, 1.0]] * 6, dtype=torch.float32)
+        val = integ.integrate(f, 6, N=10_000_000, integration_domain=dom, rng=ReplayRNG(0))
+    finally:
+        V.VEGAS._run_iteration = orig_run
+        V.VEGASMap = orig_map
+    return dict(dim=6, N=10_000_000, n_bins=50, dtype="float32", seed=0, sigma=0.05,
+                params=hexarr(f.params_vector().numpy()), value=hexf(val.item()),
+                fevals=int(integ._nr_of_fevals), iterations=int(integ.it), iters=iters)
+
+
+def gen_vegas_special(tq):
+    """Zero and constant integrands (reference vegas_test.py:159-184) on
+    the Philox draws."""
+    import torch
+
+    out = {}
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        z = tq.VEGAS().integrate(lambda x: x[:, 0] * 0.0, 2, N=10000,
+                                 integration_domain=torch.tensor([[0.0, 3.0]] * 2, dtype=torch.float64),
+                                 rng=ReplayRNG(0))
+        c = tq.VEGAS().integrate(lambda x: x[:, 0] * 0.0 + 10.0, 2, N=10000,
+                                 integration_domain=torch.tensor([[0.0, 3.0]] * 2, dtype=torch.float64),
+                                 rng=ReplayRNG(0))
+    out["zero"] = hexf(z.item())
+    out["constant"] = hexf(c.item())
+    return out
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     tq = _import_reference(ref_root)
@@ -197,6 +322,16 @@ def main():
     with open(HERE / "grid_mc_golden.json", "w") as fh:
         json.dump(data, fh, indent=0)
     print("wrote", HERE / "grid_mc_golden.json", len(data["grid"]), "grid cases")
+    vdata = {
+        "reference_version": tq.__version__,
+        "torch": torch.__version__,
+        "steps": gen_vegas_steps(tq),
+        "special": gen_vegas_special(tq),
+        "c2": gen_vegas_c2(tq),
+    }
+    with open(HERE / "vegas_golden.json", "w") as fh:
+        json.dump(vdata, fh, indent=0)
+    print("wrote", HERE / "vegas_golden.json")
 
 
 if __name__ == "__main__":

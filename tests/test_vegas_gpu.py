@@ -1,0 +1,241 @@
+"""GPU parity of VEGAS: the reference unit tests' golden vectors, step-wise
+states recorded from the reference on the same Philox draws (bin indices,
+counts and evaluations per cube bit-exact), the full-size plain VEGAS
+configuration, and the reference's special-case and accuracy tests."""
+import math
+import warnings
+
+import numpy as np
+import pytest
+import torch
+
+import torchquad_gb300 as tq
+from torchquad_gb300 import _lib as L
+from torchquad_gb300.integration._vegas_state import VegasDevice
+from tests import golden as G
+
+pytestmark = pytest.mark.gpu
+
+VG = G.load("vegas_golden.json")
+DT = {"float32": torch.float32, "float64": torch.float64}
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_map_reference_golden_vectors(dtype, cuda):
+    # vegas_map_test.py:19-128
+    m = tq.VEGASMap(20, 3, "torch", dtype)
+    y = torch.tensor([[0.8121, 0.4319, 0.1612], [0.4746, 0.6501, 0.9241], [0.6143, 0.0724, 0.5818]],
+                     dtype=dtype, device=cuda)
+    assert m._get_interval_ID(y).cpu().tolist() == [[16, 8, 3], [9, 13, 18], [12, 1, 11]]
+    off = torch.tensor([[0.2420, 0.6380, 0.2240], [0.4920, 0.0020, 0.4820], [0.2860, 0.4480, 0.6360]],
+                       dtype=dtype, device=cuda)
+    assert float((m._get_interval_offset(y) - off).abs().max()) <= 6e-5
+    assert float((m.get_X(y) - y).abs().max()) <= 3e-7
+    g = torch.linspace(0.0, 0.99999, 100, dtype=dtype, device=cuda)
+    yy = torch.stack([a.ravel() for a in torch.meshgrid(g, g, g, indexing="ij")], dim=1)
+    f = torch.prod(torch.exp(yy), dim=1)
+    jac = m.get_Jac(yy)
+    assert jac.shape == (100**3,) and jac.dtype == dtype
+    assert float((jac - 1.0).abs().max()) < 1e-14
+    m.accumulate_weight(yy, (f * jac) ** 2)
+    assert m.weights.shape == (3, 20)
+    assert float((m.weights[:, 1:] - m.weights[:, :-1]).min()) > 0.0
+    assert m.counts.dtype == torch.int64 and int((m.counts - 50000).abs().max()) == 0
+    w = torch.tensor([[0.0, 0.0, 0.0, 1.0, 1.0, 1.0], [0.0, 0.0, 0.0, 1.0, 0.0, 0.0]], dtype=dtype)
+    want = torch.tensor([[0.0, 0.0, 0.54913316, 0.75820765, 0.77899047, 0.77899047],
+                         [-0.0, -0.0, 0.64868024, 0.93220967, 0.64868024, -0.0]], dtype=dtype)
+    sm = tq.VEGASMap._smooth_map(w, torch.ones(w.shape, dtype=torch.int64), 0.5)
+    assert float((sm.cpu() - want).abs().max()) <= 3e-7
+    m.update_map()
+    xe = m.x_edges.cpu()
+    assert torch.equal(xe[:, [0, -1]], torch.tensor([[0.0, 1.0]] * 3, dtype=dtype))
+    dx = m.dx_edges.cpu()
+    assert float((dx.sum(dim=1) - 1.0).abs().max()) < 3e-7
+    assert float(dx.min()) > 0.0 and float((dx[:, 1:] - dx[:, :-1]).max()) < 0.0
+    assert float(m.get_X(yy)[0].abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_stratification_reference_invariants(dtype, cuda):
+    # vegas_stratification_test.py:10-62
+    s = tq.VEGASStratification(1000, dim=3, rng=tq.RNG(seed=0), backend="torch", dtype=dtype)
+    neval = s.get_NH(4000)
+    assert neval.dtype == torch.int64 and neval.shape == (s.N_cubes,)
+    assert int((neval - neval[0]).abs().max()) == 0
+    y = s.get_Y(neval)
+    assert y.dtype == dtype and y.shape == (int(neval.sum()), 3)
+    assert bool((y >= 0).all()) and bool((y <= 1).all())
+    f = torch.prod(torch.exp(y), dim=1)
+    jf, jf2 = s.accumulate_weight(neval, f)
+    assert float(jf2.min()) >= 0.0 and float((jf**2 - jf2).min()) >= 0.0
+    s.update_DH()
+    assert float(s.dh.min()) >= 0.0
+    assert abs(float(s.dh.sum()) - 1.0) < 4e-7
+    assert float(s.dh[-1]) > float(s.dh[0])
+    neval = s.get_NH(4000)
+    assert int(neval[-1]) > int(neval[0])
+    y = s.get_Y(neval)
+    assert y.shape == (int(neval.sum()), 3) and bool((y >= 0).all()) and bool((y <= 1).all())
+
+
+def _load(p, dtype, cuda):
+    return torch.tensor(G.arr(p["values"]).reshape(p["shape"]), dtype=dtype, device=cuda)
+
+
+def _step_state(case, st, cuda):
+    dtype = DT[case["dtype"]]
+    dom = torch.tensor(case["domain"], dtype=dtype, device=cuda)
+    dev = VegasDevice(3, dtype, case["n_bins"], case["n_strat"], cuda, dom)
+    dev.x_edges.copy_(_load(st["x_edges"], dtype, cuda))
+    dev.dx_edges.copy_(_load(st["dx_edges"], dtype, cuda))
+    dev.dh.copy_(_load(st["dh"], dtype, cuda))
+    dev.rng_offset.fill_(st["rng_offset"])
+    return dev, dtype
+
+
+def _check_step(case, st, dev, dtype, cuda, weights_before_update):
+    f32 = dtype == torch.float32
+    rtol = 2e-5 if f32 else 1e-11
+    assert dev.counts.cpu().ravel().tolist() == st["counts"]  # bit-exact
+    assert torch.allclose(weights_before_update, _load(st["weights"], torch.float64, cuda), rtol=rtol, atol=0)
+    assert torch.allclose(dev.jf, _load(st["JF"], torch.float64, cuda), rtol=rtol, atol=1e-30)
+    assert torch.allclose(dev.jf2, _load(st["JF2"], torch.float64, cuda), rtol=rtol, atol=1e-30)
+
+
+@pytest.mark.parametrize("case", VG["steps"], ids=lambda c: c["dtype"])
+def test_fused_iteration_matches_reference_state(case, cuda):
+    f = tq.GaussianPeak(3, **{k: v for k, v in case["family"].items() if k != "kind"})
+    params = f.device_params(cuda)
+    for st in case["steps"]:
+        dev, dtype = _step_state(case, st, cuda)
+        dev.get_nh(st["starting_N"], normalize=False)
+        assert dev.neval.cpu().tolist() == st["neval"]  # bit-exact
+        M = sum(st["neval"])
+        dev.iterate_fused(f.family, params, case["seed"], 0, True, M)
+        w = dev.weights.clone()
+        _check_step(case, st, dev, dtype, cuda, w)
+        assert int(dev.rng_offset.item()) == st["rng_offset"] + tq.RNG.blocks_for(3 * M, dtype)
+        dev.finish(0.75, 0)
+        stats = dev.stats[0].cpu()
+        tol = 2e-5 if dtype == torch.float32 else 1e-11
+        assert abs(float(stats[0]) - G.f(st["result"])) <= tol * abs(G.f(st["result"]))
+        assert abs(float(stats[1]) - G.f(st["sigma2"])) <= 50 * tol * abs(G.f(st["sigma2"]))
+        assert int(stats[2]) == M
+        dev.update_map(0.5)
+        xe_tol = 5e-6 if dtype == torch.float32 else 1e-12
+        assert float((dev.x_edges - _load(st["x_edges_new"], dtype, cuda)).abs().max()) <= xe_tol
+        dev.get_nh(st["starting_N"], normalize=True)  # normalises dh as update_DH does
+        want = _load(st["dh_new"], dtype, cuda)
+        dtol = 2e-3 if dtype == torch.float32 else 1e-9
+        assert float((dev.dh - want).abs().max()) <= dtol * float(want.max())
+
+
+@pytest.mark.parametrize("case", VG["steps"], ids=lambda c: c["dtype"])
+def test_materialised_iteration_matches_reference_state(case, cuda):
+    f = tq.GaussianPeak(3, **{k: v for k, v in case["family"].items() if k != "kind"})
+    for st in case["steps"][:2]:
+        dev, dtype = _step_state(case, st, cuda)
+        rng = tq.RNG(seed=case["seed"])
+        rng.offset = st["rng_offset"]
+        s = tq.VEGASStratification(case["N"] // 25, 3, rng, "torch", dtype, _device_state=dev)
+        m = tq.VEGASMap(case["n_bins"], 3, "torch", dtype, _device_state=dev)
+        neval = s.get_NH(st["starting_N"])
+        assert neval.cpu().tolist() == st["neval"]
+        y = s.get_Y(neval)
+        x, jac = m.get_X_and_Jac(y)
+        dom = dev.domain
+        sizes = dom[:, 1] - dom[:, 0]
+        jf = f(x * sizes + dom[:, 0]) * torch.prod(sizes) * jac
+        m.accumulate_weight(y, jf**2)
+        s.accumulate_weight(neval, jf)
+        _check_step(case, st, dev, dtype, cuda, dev.weights.clone())
+
+
+def test_plain_vegas_full_size_matches_reference(cuda):
+    """dim 6, N = 1e7, 50 intervals, fp32 normal peak, seed 0."""
+    c = VG["c2"]
+    f = tq.GaussianPeak.normal(6, 0.5, c["sigma"])
+    v = tq.VEGAS()
+    dom = torch.tensor([[0.0, 1.0]] * 6, dtype=torch.float32, device=cuda)
+    r = v.integrate(f, 6, N=c["N"], integration_domain=dom, seed=c["seed"], n_intervals=c["n_bins"])
+    assert r.dtype == torch.float32
+    assert v.it == c["iterations"]
+    Ms = [int(m) for m in v._dev.stats[: v.it, 2].cpu()]
+    ref_Ms = [it["M"] for it in c["iters"]]
+    # the first iteration starts from identical state: identical cube counts
+    assert Ms[0] == ref_Ms[0]
+    assert abs(v._nr_of_fevals - c["fevals"]) <= 2000
+    want = G.f(c["value"])
+    assert abs(r.item() - want) <= 5 * v._get_error() + 1e-6
+    assert abs(r.item() - 1.0) < 5e-3
+
+
+def test_fused_and_materialised_paths_agree(cuda):
+    f = tq.GaussianPeak(3, a=[5.0, 8.0, 3.0], u=[0.3, 0.5, 0.7])
+    dom = torch.tensor([[0.0, 1.0], [-1.0, 1.0], [0.0, 2.0]], dtype=torch.float64, device=cuda)
+    a, b = tq.VEGAS(), tq.VEGAS()
+    ra = a.integrate(f, 3, N=20000, integration_domain=dom, seed=11)
+    rb = b.integrate(lambda x: f(x), 3, N=20000, integration_domain=dom, seed=11)
+    assert a._nr_of_fevals == b._nr_of_fevals and a.it == b.it
+    assert abs(ra.item() - rb.item()) <= 1e-9 * abs(ra.item())
+
+
+def test_reference_run_step_sequence(cuda):
+    case = [c for c in VG["steps"] if c["dtype"] == "float64"][0]
+    f = tq.GaussianPeak(3, **{k: v for k, v in case["family"].items() if k != "kind"})
+    dom = torch.tensor(case["domain"], dtype=torch.float64, device=cuda)
+    v = tq.VEGAS()
+    r = v.integrate(f, 3, N=case["N"], integration_domain=dom, seed=case["seed"])
+    assert v.it == case["iterations"] and v._nr_of_fevals == case["fevals"]
+    assert abs(r.item() - G.f(case["value"])) <= 1e-9 * abs(G.f(case["value"]))
+
+
+def test_zero_and_constant_integrands(cuda):
+    # vegas_test.py:159-184
+    dom = torch.tensor([[0.0, 3.0]] * 2, dtype=torch.float64, device=cuda)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        z = tq.VEGAS().integrate(lambda x: x[:, 0] * 0.0, 2, N=10000, integration_domain=dom, seed=0)
+    assert z.item() == 0.0
+    c = tq.VEGAS().integrate(lambda x: x[:, 0] * 0.0 + 10.0, 2, N=10000, integration_domain=dom, seed=0)
+    assert abs(c.item() - 90.0) < 1e-13
+    assert abs(c.item() - G.f(VG["special"]["constant"])) < 1e-13
+    with pytest.warns(RuntimeWarning, match="Cannot update the VEGASMap"):
+        tq.VEGAS().integrate(tq.ExpSum(2, c=0.0), 2, N=10000, integration_domain=dom, seed=0)
+
+
+class ModifiedRNG(tq.RNG):
+    """Replaces half of the draws with exactly 0.0 or 1.0 (vegas_test.py:143-156)."""
+
+    def uniform(self, size, dtype):
+        n = super().uniform(size, dtype)
+        return torch.where(n < 0.5, n * 2.0, torch.where(n < 0.75, torch.zeros_like(n), torch.ones_like(n)))
+
+
+def test_draws_of_exactly_zero_and_one(cuda):
+    dom = torch.tensor([[0.0, 1.0]] * 2, dtype=torch.float64, device=cuda)
+    r = tq.VEGAS().integrate(lambda x: torch.sum(x, dim=1), 2, N=10000, integration_domain=dom,
+                             rng=ModifiedRNG(seed=0))
+    assert abs(r.item() - 1.0) < 0.1
+
+
+def test_peak_accuracy_reference_cases(cuda):
+    # vegas_test.py:71-140
+    dom = torch.tensor([[1.0, 5.0], [-4.0, 4.0], [2.0, 6.0]], dtype=torch.float64, device=cuda)
+
+    def cube(x):
+        return torch.prod((x >= 3.0) * (x < 4.0), dim=1).to(torch.float64) + 0.001
+
+    ref = float(torch.prod(dom[:, 1] - dom[:, 0])) * 0.001 + 1.0
+    for seed in [0, 1, 2, 3, 41317]:
+        r = tq.VEGAS().integrate(cube, 3, N=30000, integration_domain=dom, seed=seed)
+        assert abs(r.item() - ref) < 0.03
+    d2 = torch.tensor([[1.0, 101.0], [-4.0, 96.0]], dtype=torch.float64, device=cuda)
+
+    def diag(x):
+        return torch.exp(torch.sum(d2[:, 0] - x, dim=1)) + torch.exp(torch.sum(x - d2[:, 1], dim=1))
+
+    ref2 = 2.0 - 4.0 * math.exp(-100.0) + 2.0 * math.exp(-200.0)
+    for seed in [0, 1, 2, 3, 41317]:
+        r = tq.VEGAS().integrate(diag, 2, N=30000, integration_domain=d2, seed=seed)
+        assert abs(r.item() - ref2) < 0.03

@@ -17,6 +17,9 @@ from .integration.gaussian import GaussLegendre, Gaussian
 from .integration.grid_integrator import GridIntegrator
 from .integration.base_integrator import BaseIntegrator
 from .integration.rng import RNG
+from .integration.vegas import VEGAS
+from .integration.vegas_map import VEGASMap
+from .integration.vegas_stratification import VEGASStratification
 from .integration._kernels import set_materialise_budget
 
 from .utils.set_log_level import set_log_level
@@ -33,6 +36,9 @@ __all__ = [
     "BaseIntegrator",
     "IntegrationGrid",
     "MonteCarlo",
+    "VEGAS",
+    "VEGASMap",
+    "VEGASStratification",
     "Trapezoid",
     "Simpson",
     "Boole",

@@ -33,6 +33,34 @@ TQ_FN_EXP_SUM, TQ_FN_GAUSSIAN, TQ_FN_OSCILLATORY, TQ_FN_SUM_SIN = 1, 2, 3, 4
 
 TQ_MAX_DIM = 16
 
+class VegasState(ctypes.Structure):
+    """Mirror of ``tq_vegas_state`` (include/torchquad_gb300.h)."""
+
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("dtype", ctypes.c_int32),
+        ("n_bins", c_int64),
+        ("n_strat", c_int64),
+        ("n_cubes", c_int64),
+        ("x_edges", c_void_p),
+        ("dx_edges", c_void_p),
+        ("weights", c_void_p),
+        ("counts", c_void_p),
+        ("dh", c_void_p),
+        ("jf", c_void_p),
+        ("jf2", c_void_p),
+        ("neval", c_void_p),
+        ("cube_start", c_void_p),
+        ("rng_offset", c_void_p),
+        ("stats", c_void_p),
+        ("flags", c_void_p),
+        ("scalars", c_void_p),
+        ("domain", c_void_p),
+    ]
+
+
+_VS = POINTER(VegasState)
+
 # name -> (restype, argtypes); every symbol the header declares.
 SIGNATURES = {
     "tq_status_string": (c_char_p, [c_int]),
@@ -64,6 +92,21 @@ SIGNATURES = {
     ),
     "tq_uniform": (c_int, [c_int, c_uint64, c_uint64, c_uint64, c_int64, c_void_p, c_void_p]),
     "tq_mc_fused_workspace_size": (c_size_t, [c_int, c_int64]),
+    "tq_vegas_workspace_size": (c_size_t, [_VS]),
+    "tq_vegas_init": (c_int, [_VS, c_void_p]),
+    "tq_vegas_warmup_fused": (
+        c_int, [_VS, c_int, c_void_p, c_int64, c_uint64, c_uint64, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_update_map": (c_int, [_VS, c_double, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_smooth_weights": (c_int, [_VS, c_double, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_get_nh": (c_int, [_VS, c_int64, c_int, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_iterate_fused": (
+        c_int, [_VS, c_int, c_void_p, c_uint64, c_uint64, c_int, c_int64, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_finish_iteration": (c_int, [_VS, c_double, c_int64, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_strat_points": (c_int, [_VS, c_void_p, c_int64, c_void_p, c_void_p]),
+    "tq_vegas_map_points": (c_int, [_VS, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "tq_vegas_accumulate": (
+        c_int, [_VS, c_void_p, c_void_p, c_int64, c_int, c_int, c_void_p, c_size_t, c_void_p]),
+    "tq_fp32_fma_probe": (c_int, [c_int64, c_int, c_void_p, c_void_p, c_void_p]),
     "tq_mc_fused": (
         c_int,
         [c_int, c_int, c_int64, c_void_p, c_int, c_void_p, c_uint64, c_uint64, c_uint64,
@@ -73,6 +116,13 @@ SIGNATURES = {
 
 _lock = threading.Lock()
 _lib = None
+
+# Kernel launches issued through this binding (benchmark bookkeeping).
+launches = [0]
+
+
+def count_launches(n: int = 1) -> None:
+    launches[0] += n
 
 
 class TorchquadGB300Error(RuntimeError):

@@ -1,0 +1,985 @@
+// VEGAS+ on GB300: fused stratified sampling (Philox -> stratified y ->
+// adaptive-map x, jac -> integrand -> map histogram and per-cube sums), the
+// map update and the stratification update.
+//
+// Reference (torchquad v0.5.0): vegas.py (driver), vegas_map.py (adaptive
+// map), vegas_stratification.py (stratified sampling).  The reference
+// materialises y, x, f and jac for every point and scatter-adds them into
+// the map and the cubes with global atomics (utils.py:61-76).  Here one
+// kernel does a whole iteration: points of a 256-point tile are generated
+// in registers, the map histogram is privatised in shared memory per CTA and
+// flushed once, and per-cube sums use the cube-contiguous point order
+// (repeat_interleave order of vegas_stratification.py:154): a tile spans at
+// most 130 cubes because every cube has >= 2 points, so they get shared
+// memory slots and one flush per tile.
+//
+// The arithmetic that decides interval indices and points (y, ID, offset,
+// x, jac) is written with explicitly rounded operations in the state's
+// dtype, in the reference's operation order, so that indices and counts
+// match the reference bit for bit given the same uniforms and map.
+
+#include "tq_common.cuh"
+
+namespace tq {
+
+constexpr int kTile = 256;                  // points per tile = threads per CTA
+constexpr int kCubeSlots = kTile / 2 + 2;   // cubes a tile can touch
+
+// ---- explicitly rounded arithmetic (no FMA contraction)
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+
+template <typename T>
+__device__ __forceinline__ T warm_scale() {
+  return (T)0.999999;  // vegas.py:236 (and the clamp of vegas_stratification.py:165)
+}
+
+// Map one coordinate: interval ID = floor(y*B), offset = y*B - floor(y*B)
+// (vegas_map.py:76-97), x = x_edges[ID] + dx_edges[ID]*offset (:57),
+// Jacobian factor B * dx_edges[ID] (:73).
+template <typename T>
+__device__ __forceinline__ int map_coord(const T* __restrict__ xe, const T* __restrict__ dxe,
+                                         int64_t B, T y, T& x, T& jac_factor) {
+  const T Bf = (T)B;
+  const T yB = mul_rn(y, Bf);
+  const T fl = floor(yB);
+  int id = (int)fl;
+  // y < 1 keeps id <= B-1; the clamp only guards memory for pathological B
+  id = id < 0 ? 0 : (id >= (int)B ? (int)B - 1 : id);
+  const T off = sub_rn(yB, fl);
+  x = add_rn(xe[id], mul_rn(dxe[id], off));
+  jac_factor = mul_rn(Bf, dxe[id]);
+  return id;
+}
+
+// Coordinate k of the position of cube c: (c / n_strat^k) mod n_strat,
+// dimension 0 fastest (vegas_stratification.py:105-138).
+__device__ __forceinline__ int64_t cube_digit(int64_t c, int64_t n_strat, int k) {
+  for (int i = 0; i < k; ++i) c /= n_strat;
+  return c % n_strat;
+}
+
+// y = (pos + u) / n_strat, values >= 1 replaced by 0.999999 (:159-165).
+template <typename T>
+__device__ __forceinline__ T strat_y(int64_t pos, T u, int64_t n_strat) {
+  T y = div_rn(add_rn((T)pos, u), (T)n_strat);
+  return y >= (T)1 ? warm_scale<T>() : y;
+}
+
+// Largest c in [0, n) with cs[c] <= target; cs strictly increasing, cs[0] = 0.
+// One warp, 32-ary search with coalesced probes.
+__device__ __forceinline__ int64_t warp_find_cube(const int64_t* __restrict__ cs, int64_t n,
+                                                  int64_t target) {
+  const int lane = threadIdx.x & 31;
+  int64_t lo = 0, hi = n;
+  while (hi - lo > 32) {
+    const int64_t step = (hi - lo + 31) / 32;
+    const int64_t pos = lo + lane * step;
+    const bool ok = pos < hi && cs[pos] <= target;
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    const int last = 31 - __clz(m);
+    lo = lo + last * step;
+    hi = min(hi, lo + step);
+  }
+  const int64_t pos = lo + lane;
+  const bool ok = pos < hi && cs[pos] <= target;
+  const unsigned m = __ballot_sync(0xffffffffu, ok);
+  return lo + (31 - __clz(m));
+}
+
+// ------------------------------------------------------------ sampling
+struct SampleArgs {
+  tq_vegas_state st;
+  int family;
+  const double* params;
+  int64_t n_samples;  // warm-up: points; iterations: read from cube_start
+  uint64_t seed, sid;
+  int use_map;        // accumulate the map histogram
+  int edges_smem, hist_smem;
+  unsigned* ticket;
+};
+
+template <typename T>
+struct Smem {
+  T* xe;
+  T* dxe;
+  double* hw;
+  unsigned* hc;
+  double* sj;
+  double* sj2;
+  int64_t* cs;
+};
+
+template <typename T>
+__device__ Smem<T> carve(unsigned char* base, const SampleArgs& a) {
+  Smem<T> s;
+  const int d = a.st.dim;
+  const int64_t B = a.st.n_bins;
+  size_t off = 0;
+  s.sj = (double*)(base + off);
+  off += sizeof(double) * kCubeSlots;
+  s.sj2 = (double*)(base + off);
+  off += sizeof(double) * kCubeSlots;
+  s.cs = (int64_t*)(base + off);
+  off += sizeof(int64_t) * (kCubeSlots + 1);
+  if (a.hist_smem) {
+    s.hw = (double*)(base + off);
+    off += sizeof(double) * d * B;
+  } else {
+    s.hw = a.st.weights;
+  }
+  if (a.edges_smem) {
+    s.xe = (T*)(base + off);
+    off += sizeof(T) * d * (B + 1);
+    s.dxe = (T*)(base + off);
+    off += sizeof(T) * d * B;
+  } else {
+    s.xe = (T*)a.st.x_edges;
+    s.dxe = (T*)a.st.dx_edges;
+  }
+  off = (off + 7) & ~size_t(7);
+  s.hc = a.hist_smem ? (unsigned*)(base + off) : nullptr;
+  return s;
+}
+
+__host__ __device__ inline size_t sample_smem_bytes(int d, int64_t B, size_t tsize, bool hist,
+                                                    bool edges) {
+  size_t off = sizeof(double) * 2 * kCubeSlots + sizeof(int64_t) * (kCubeSlots + 1);
+  if (hist) off += sizeof(double) * d * B;
+  if (edges) off += tsize * (d * (B + 1) + d * B);
+  off = (off + 7) & ~size_t(7);
+  if (hist) off += sizeof(unsigned) * d * B;
+  return off;
+}
+
+template <typename T, int FAM, bool WARM>
+__global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ Family<T> fam;
+  __shared__ T lo[kMaxDim], wid[kMaxDim];
+  __shared__ T volume;
+  __shared__ int64_t tile_c0, tile_c1;
+  const tq_vegas_state& st = a.st;
+  const int d = st.dim;
+  const int64_t B = st.n_bins;
+  Smem<T> sm = carve<T>(smem_raw, a);
+  if (threadIdx.x == 0) {
+    load_family<T>(fam, a.family, d, a.params);
+    const T* dom = (const T*)st.domain;
+    T v = (T)1;
+    for (int k = 0; k < d; ++k) {
+      lo[k] = dom[2 * k];
+      wid[k] = sub_rn(dom[2 * k + 1], dom[2 * k]);
+      v = mul_rn(v, wid[k]);
+    }
+    volume = v;
+  }
+  if (a.edges_smem) {
+    for (int64_t i = threadIdx.x; i < d * (B + 1); i += blockDim.x) sm.xe[i] = ((const T*)st.x_edges)[i];
+    for (int64_t i = threadIdx.x; i < d * B; i += blockDim.x) sm.dxe[i] = ((const T*)st.dx_edges)[i];
+  }
+  if (a.hist_smem) {
+    for (int64_t i = threadIdx.x; i < d * B; i += blockDim.x) {
+      sm.hw[i] = 0.0;
+      sm.hc[i] = 0u;
+    }
+  }
+  __syncthreads();
+
+  const int64_t M = WARM ? a.n_samples : st.cube_start[st.n_cubes];
+  const uint64_t offset = *st.rng_offset;
+  const int64_t ns = st.n_strat;
+  constexpr int PB = Uniform<T>::per_block;
+
+  for (int64_t tile = blockIdx.x; tile * kTile < M; tile += gridDim.x) {
+    const int64_t j0 = tile * kTile;
+    const int64_t j = j0 + threadIdx.x;
+    int nc = 0;
+    if (!WARM) {
+      const int warp = threadIdx.x >> 5;
+      if (warp == 0) {
+        const int64_t c = warp_find_cube(st.cube_start, st.n_cubes, j0);
+        if ((threadIdx.x & 31) == 0) tile_c0 = c;
+      } else if (warp == 1) {
+        const int64_t c = warp_find_cube(st.cube_start, st.n_cubes, min(M, j0 + kTile) - 1);
+        if ((threadIdx.x & 31) == 0) tile_c1 = c;
+      }
+      __syncthreads();
+      nc = (int)(tile_c1 - tile_c0 + 1);
+      for (int i = threadIdx.x; i <= nc; i += blockDim.x) sm.cs[i] = st.cube_start[tile_c0 + i];
+      for (int i = threadIdx.x; i < nc; i += blockDim.x) sm.sj[i] = sm.sj2[i] = 0.0;
+      __syncthreads();
+    }
+    if (j < M) {
+      int64_t c = 0;
+      int slot = 0;
+      if (!WARM) {
+        int l = 0, h = nc;  // largest l with cs[l] <= j
+        while (h - l > 1) {
+          const int mid = (l + h) >> 1;
+          if (sm.cs[mid] <= j) l = mid;
+          else h = mid;
+        }
+        slot = l;
+        c = tile_c0 + l;
+      }
+      uint64_t cur = ~0ull;
+      uint4 r = make_uint4(0, 0, 0, 0);
+      T jac = (T)1;
+      T s = T(0);
+      int ids[kMaxDim];
+      int64_t cc = c;
+#pragma unroll
+      for (int k = 0; k < kMaxDim; ++k) {
+        if (k < d) {
+          const uint64_t e = (uint64_t)j * d + k;
+          const uint64_t blk = e / PB;
+          if (blk != cur) {
+            r = philox_block(a.seed, a.sid, offset + blk);
+            cur = blk;
+          }
+          const T u = Uniform<T>::from(r, (int)(e - blk * PB));
+          T y;
+          if (WARM) {
+            y = mul_rn(u, warm_scale<T>());
+          } else {
+            const int64_t q = cc / ns;
+            y = strat_y<T>(cc - q * ns, u, ns);
+            cc = q;
+          }
+          T x, jf_k;
+          ids[k] = map_coord<T>(sm.xe + k * (B + 1), sm.dxe + k * B, B, y, x, jf_k);
+          jac = mul_rn(jac, jf_k);
+          // vegas.py:110: fn(x * domain_sizes + domain_starts) * domain_volume
+          const T xt = add_rn(mul_rn(x, wid[k]), lo[k]);
+          const T g = fam_term<FAM, T>(fam, k, xt);
+          s = (k == 0) ? g : s + g;
+        }
+      }
+      const T f = mul_rn(fam_outer<FAM, T>(fam, s), volume);
+      const T jfv = mul_rn(f, jac);
+      const double jf2 = (double)jfv * (double)jfv;
+      if (a.use_map) {
+#pragma unroll
+        for (int k = 0; k < kMaxDim; ++k) {
+          if (k < d) {
+            if (a.hist_smem) {
+              atomicAdd(sm.hw + k * B + ids[k], jf2);
+              atomicAdd(sm.hc + k * B + ids[k], 1u);
+            } else {
+              atomicAdd(st.weights + k * B + ids[k], jf2);
+              atomicAdd((unsigned long long*)(st.counts + k * B + ids[k]), 1ull);
+            }
+          }
+        }
+      }
+      if (!WARM) {
+        atomicAdd(sm.sj + slot, (double)jfv);
+        atomicAdd(sm.sj2 + slot, jf2);
+      }
+    }
+    if (!WARM) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+        atomicAdd(st.jf + tile_c0 + i, sm.sj[i]);
+        atomicAdd(st.jf2 + tile_c0 + i, sm.sj2[i]);
+      }
+      __syncthreads();
+    }
+  }
+  if (a.hist_smem && a.use_map) {
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < d * B; i += blockDim.x) {
+      if (sm.hc[i]) {
+        atomicAdd(st.weights + i, sm.hw[i]);
+        atomicAdd((unsigned long long*)(st.counts + i), (unsigned long long)sm.hc[i]);
+      }
+    }
+  }
+  if (last_block_arrives(a.ticket)) {
+    if (threadIdx.x == 0) {
+      *st.rng_offset = offset + ((uint64_t)M * d + PB - 1) / PB;
+      *a.ticket = 0u;
+    }
+  }
+}
+
+// ----------------------------------------------------------- get_NH
+struct NhArgs {
+  tq_vegas_state st;
+  int64_t nevals_exp;
+  int normalize;
+  int64_t* block_tot;  // [blocks]
+  unsigned* ticket;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) vegas_nh_kernel(NhArgs a) {
+  const tq_vegas_state& st = a.st;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t nh = 0;
+  if (c < st.n_cubes) {
+    T dh = ((T*)st.dh)[c];
+    if (a.normalize) {
+      const T sum = (T)st.scalars[0];
+      if (sum != (T)0) {
+        dh = div_rn(dh, sum);  // vegas_stratification.py:88-90
+        ((T*)st.dh)[c] = dh;
+      }
+    }
+    T f = floor(mul_rn(dh, (T)a.nevals_exp));  // :102
+    f = f < (T)2 ? (T)2 : f;                    // :103 clip(nh, 2, None)
+    nh = (int64_t)f;
+    st.neval[c] = nh;
+    st.jf[c] = 0.0;
+    st.jf2[c] = 0.0;
+  }
+  // block-wide exclusive scan of nh (deterministic)
+  __shared__ int64_t warp_tot[kBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t incl = nh;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int64_t w = lane < kBlock / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t v = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += v;
+    }
+    if (lane < kBlock / 32) warp_tot[lane] = w;  // inclusive warp prefix
+  }
+  __syncthreads();
+  const int64_t excl = incl - nh + (warp > 0 ? warp_tot[warp - 1] : 0);
+  if (c < st.n_cubes) st.cube_start[c] = excl;
+  if (threadIdx.x == 0) a.block_tot[blockIdx.x] = warp_tot[kBlock / 32 - 1];
+  if (last_block_arrives(a.ticket)) {
+    if (threadIdx.x == 0) {
+      int64_t run = 0;
+      for (unsigned b = 0; b < gridDim.x; ++b) {
+        const int64_t t = a.block_tot[b];
+        a.block_tot[b] = run;
+        run += t;
+      }
+      st.cube_start[st.n_cubes] = run;
+      *a.ticket = 0u;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) vegas_nh_fixup_kernel(tq_vegas_state st,
+                                                                const int64_t* block_pre) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < st.n_cubes) st.cube_start[c] += block_pre[blockIdx.x];
+}
+
+// ---------------------------------------------------- finish iteration
+struct FinishArgs {
+  tq_vegas_state st;
+  double beta;
+  int64_t slot;
+  Acc* partials;  // [blocks][3]
+  unsigned* ticket;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
+  const tq_vegas_state& st = a.st;
+  const int d = st.dim;
+  const double V = pow(1.0 / (double)st.n_strat, (double)d);  // V_cubes (:29)
+  const T Vt = (T)V, V2t = (T)(V * V);
+  Acc res{0, 0}, s2{0, 0}, dsum{0, 0};
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < st.n_cubes;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const double n = (double)st.neval[c];
+    const double J = st.jf[c], J2 = st.jf2[c];
+    const double inv = 1.0 / n;
+    const double ih = J * (inv * V);                     // vegas.py:294
+    const double sig2 = fabs(J2 * inv * (V * V) - ih * ih);  // :297-301
+    acc_add(res, ih);
+    acc_add(s2, sig2 * inv);
+    // update_DH (vegas_stratification.py:72-86) in the state's dtype
+    const T cnt = (T)n, jT = (T)J, j2T = (T)J2;
+    const T q = div_rn(mul_rn(Vt, jT), cnt);
+    T dt = sub_rn(div_rn(mul_rn(V2t, j2T), cnt), mul_rn(q, q));
+    if (dt < (T)0) dt = (T)0;
+    const T dh = pow(dt, (T)a.beta);
+    ((T*)st.dh)[c] = dh;
+    acc_add(dsum, (double)dh);
+  }
+  res = block_reduce<kBlock>(res);
+  s2 = block_reduce<kBlock>(s2);
+  dsum = block_reduce<kBlock>(dsum);
+  if (threadIdx.x == 0) {
+    a.partials[3 * blockIdx.x] = res;
+    a.partials[3 * blockIdx.x + 1] = s2;
+    a.partials[3 * blockIdx.x + 2] = dsum;
+  }
+  if (last_block_arrives(a.ticket)) {
+    Acc r{0, 0}, s{0, 0}, ds{0, 0};
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+      acc_merge(r, a.partials[3 * i]);
+      acc_merge(s, a.partials[3 * i + 1]);
+      acc_merge(ds, a.partials[3 * i + 2]);
+    }
+    r = block_reduce<kBlock>(r);
+    s = block_reduce<kBlock>(s);
+    ds = block_reduce<kBlock>(ds);
+    if (threadIdx.x == 0) {
+      double* out = st.stats + 4 * a.slot;
+      out[0] = r.s + r.c;
+      out[1] = s.s + s.c;
+      out[2] = (double)st.cube_start[st.n_cubes];
+      // the sum the reference normalises with is taken in the state dtype
+      st.scalars[0] = (double)(T)(ds.s + ds.c);
+      *a.ticket = 0u;
+    }
+  }
+}
+
+// --------------------------------------------------------- map update
+// One CTA updates every dimension: the "all weights zero" test of
+// vegas_map.py:151-155 spans the whole map.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state st, double alpha,
+                                                                  double* scratch,
+                                                                  void* smooth_out) {
+  const int d = st.dim;
+  const int64_t B = st.n_bins;
+  const int64_t DB = d * B;
+  T* w = (T*)scratch;                 // [d][B] averaged weights, then smoothed
+  T* wtmp = w + DB;                   // [d][B]
+  unsigned char* z = (unsigned char*)(wtmp + DB);        // [d][B] zero-count flags
+  unsigned char* ztmp = z + DB;                          // [d][B]
+  double* newx = (double*)(((uintptr_t)(ztmp + DB) + 15) & ~uintptr_t(15));  // [d][B+1]
+  int64_t* idx = (int64_t*)(newx + d * (B + 1));         // [d][B+1]
+  T* val = (T*)(idx + d * (B + 1));                      // [d][B+1]
+  __shared__ T sums[kMaxDim];
+  __shared__ T deltas[kMaxDim];
+
+  // EQ 17: average weights per interval; remember empty intervals
+  int any_zero = 0;
+  for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
+    const int64_t c = st.counts[i];
+    const T wi = (T)st.weights[i];
+    z[i] = c == 0;
+    any_zero |= (c == 0);
+    w[i] = c == 0 ? wi : div_rn(wi, (T)c);
+  }
+  any_zero = __syncthreads_or(any_zero);
+  if (any_zero) {
+    // fill empty intervals from their neighbours, up to 10 sweeps (:131-142)
+    for (int sweep = 0; sweep < 10; ++sweep) {
+      for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
+        const int64_t col = i % B;
+        wtmp[i] = (col < B - 1 && z[i]) ? w[i + 1] : w[i];
+        ztmp[i] = (col < B - 1) ? (z[i] && z[i + 1]) : z[i];
+      }
+      __syncthreads();
+      for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
+        const int64_t col = i % B;
+        w[i] = (col > 0 && ztmp[i]) ? wtmp[i - 1] : wtmp[i];
+        z[i] = (col > 0) ? (ztmp[i] && ztmp[i - 1]) : ztmp[i];
+      }
+      if (!__syncthreads_or([&] {
+            int zz = 0;
+            for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) zz |= z[i];
+            return zz;
+          }()))
+        break;
+    }
+  }
+  // row sums (:151)
+  if (threadIdx.x < d) {
+    double acc = 0.0;
+    for (int64_t b = 0; b < B; ++b) acc += (double)w[threadIdx.x * B + b];
+    sums[threadIdx.x] = (T)acc;
+  }
+  __syncthreads();
+  int zero_row = 0;
+  for (int k = threadIdx.x; k < d; k += blockDim.x) zero_row |= sums[k] == (T)0;
+  if (__syncthreads_or(zero_row)) {
+    // The map cannot be updated (:152-155, :187-196): reset and flag.
+    if (smooth_out) {
+      if (threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
+      return;
+    }
+    for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
+      st.weights[i] = 0.0;
+      st.counts[i] = 0;
+    }
+    if (threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
+    return;
+  }
+
+  // EQ 18: [1,6,1]/8 smoothing with repeated borders, normalised; EQ 19
+  for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
+    const int64_t k = i / B, b = i - k * B;
+    const T* r = w + k * B;
+    T v;
+    if (b == 0)
+      v = add_rn(mul_rn((T)7, r[0]), r[1]);
+    else if (b == B - 1)
+      v = add_rn(r[B - 2], mul_rn((T)7, r[B - 1]));
+    else
+      v = add_rn(add_rn(r[b - 1], mul_rn((T)6, r[b])), r[b + 1]);
+    v = div_rn(v, mul_rn((T)8, sums[k]));
+    if (v != (T)0) {
+      const T t = div_rn(sub_rn(v, (T)1), log(v));
+      v = alpha == 0.5 ? sqrt(t) : pow(t, (T)alpha);
+    }
+    wtmp[i] = v;
+    if (smooth_out) ((T*)smooth_out)[i] = v;
+  }
+  __syncthreads();
+  if (smooth_out) return;  // _smooth_map only: the map and its weights stay as they are
+  // EQ 20-22 per dimension, sequentially as the reference's cumsums run
+  if (threadIdx.x < d) {
+    const int k = threadIdx.x;
+    const T* sw = wtmp + k * B;
+    const T* xe = (const T*)st.x_edges + k * (B + 1);
+    const T* dxe = (const T*)st.dx_edges + k * B;
+    double tot = 0.0;
+    for (int64_t b = 0; b < B; ++b) tot += (double)sw[b];
+    const T delta = div_rn((T)tot, (T)B);  // :201
+    deltas[k] = delta;
+    int64_t* num = idx + k * (B + 1);
+    T* vv = val + k * (B + 1);
+    for (int64_t m = 0; m <= B; ++m) {
+      num[m] = 0;
+      vv[m] = (T)0;
+    }
+    // :210-226: multiples of delta in the fp64 cumulative sum
+    double cum = 0.0;
+    for (int64_t b = 0; b < B - 1; ++b) {
+      cum += (double)sw[b];
+      int64_t m = (int64_t)(cum / (double)delta);
+      m = m < 0 ? 0 : (m > B ? B : m);
+      num[m] += 1;
+      vv[m] = add_rn(vv[m], sw[b]);
+    }
+    // :230-239: new inner edges
+    int64_t ind = 0;
+    double daccu = 0.0;  // cumsum of (delta - val) accumulated in fp64, rounded per step
+    double* nx = newx + k * (B + 1);
+    nx[0] = (double)xe[0];
+    nx[B] = (double)xe[B];
+    for (int64_t e = 0; e < B - 1; ++e) {
+      ind += num[e];
+      daccu += (double)sub_rn(delta, vv[e]);
+      const int64_t ii = ind < 0 ? 0 : (ind > B - 1 ? B - 1 : ind);
+      const T da = (T)daccu;
+      const T ne = add_rn(xe[ii], mul_rn(div_rn(da, sw[ii]), dxe[ii]));
+      nx[e + 1] = (double)ne;
+    }
+    // :240-257: replace infinite edges by the mean of their (unrepaired)
+    // neighbours; vv (no longer needed) holds the means
+    bool bad = false;
+    for (int64_t e = 1; e < B; ++e) bad |= !isfinite(nx[e]);
+    if (bad) {
+      atomicAdd(st.flags + 1, 1);
+      for (int64_t e = 1; e < B; ++e)
+        vv[e] = mul_rn((T)0.5, add_rn((T)nx[e - 1], (T)nx[e + 1]));
+      for (int64_t e = 1; e < B; ++e)
+        if (!isfinite(nx[e])) nx[e] = (double)vv[e];
+      for (int64_t e = 1; e < B; ++e)
+        if (!isfinite(nx[e])) {
+          atomicAdd(st.flags + 2, 1);
+          break;
+        }
+    }
+  }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < d * (B + 1); i += blockDim.x)
+    ((T*)st.x_edges)[i] = (T)newx[i];
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
+    const int64_t k = i / B, b = i - k * B;
+    const T* xe = (const T*)st.x_edges + k * (B + 1);
+    ((T*)st.dx_edges)[i] = sub_rn(xe[b + 1], xe[b]);  // :259
+    st.weights[i] = 0.0;
+    st.counts[i] = 0;
+  }
+}
+
+// ----------------------------------------------------------- init
+template <typename T>
+__global__ void vegas_init_kernel(tq_vegas_state st) {
+  const int d = st.dim;
+  const int64_t B = st.n_bins;
+  const T step = div_rn((T)1, (T)B);  // linspace(0, 1, B+1) step
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < d * (B + 1);
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i % (B + 1);
+    ((T*)st.x_edges)[i] = linspace_node<T>((T)0, (T)1, step, B + 1, b);
+  }
+  const T inv = div_rn((T)1, (T)B);  // ones / N_intervals (vegas_map.py:34-37)
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < d * B;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    ((T*)st.dx_edges)[i] = inv;
+    st.weights[i] = 0.0;
+    st.counts[i] = 0;
+  }
+  // dh = ones * 1.0 / N_cubes (vegas_stratification.py:40)
+  const T dh0 = div_rn((T)1, (T)st.n_cubes);
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < st.n_cubes;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    ((T*)st.dh)[c] = dh0;
+    st.jf[c] = 0.0;
+    st.jf2[c] = 0.0;
+    st.neval[c] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 4) {
+    st.flags[threadIdx.x] = 0;
+    st.scalars[threadIdx.x] = 0.0;
+  }
+}
+
+// ------------------------------------------------ materialised kernels
+template <typename T>
+__global__ void __launch_bounds__(kTile) vegas_strat_points_kernel(tq_vegas_state st, const T* u,
+                                                                   int64_t M, T* y) {
+  const int d = st.dim;
+  const int64_t ns = st.n_strat;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < M;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    // cube of point j: binary search in cube_start
+    int64_t l = 0, h = st.n_cubes;
+    while (h - l > 1) {
+      const int64_t m = (l + h) >> 1;
+      if (st.cube_start[m] <= j) l = m;
+      else h = m;
+    }
+    int64_t cc = l;
+    for (int k = 0; k < d; ++k) {
+      const int64_t q = cc / ns;
+      y[j * d + k] = strat_y<T>(cc - q * ns, u[j * d + k], ns);
+      cc = q;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTile) vegas_map_points_kernel(tq_vegas_state st, const T* y,
+                                                                 int64_t M, T* x, T* jac) {
+  const int d = st.dim;
+  const int64_t B = st.n_bins;
+  const T* xe = (const T*)st.x_edges;
+  const T* dxe = (const T*)st.dx_edges;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < M;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    T jc = (T)1;
+    for (int k = 0; k < d; ++k) {
+      T xv, jf;
+      map_coord<T>(xe + k * (B + 1), dxe + k * B, B, y[j * d + k], xv, jf);
+      x[j * d + k] = xv;
+      jc = mul_rn(jc, jf);
+    }
+    jac[j] = jc;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTile) vegas_accumulate_kernel(tq_vegas_state st, const T* y,
+                                                                 const T* vals, int64_t M,
+                                                                 int acc_map, int stratified) {
+  const int d = st.dim;
+  const int64_t B = st.n_bins;
+  const T Bf = (T)B;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < M;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const T v = vals[j];
+    const double v2 = (double)v * (double)v;
+    if (acc_map) {
+      for (int k = 0; k < d; ++k) {
+        int id = (int)floor(mul_rn(y[j * d + k], Bf));
+        id = id < 0 ? 0 : (id >= (int)B ? (int)B - 1 : id);
+        atomicAdd(st.weights + k * B + id, (double)v);
+        atomicAdd((unsigned long long*)(st.counts + k * B + id), 1ull);
+      }
+    }
+    if (stratified) {
+      int64_t l = 0, h = st.n_cubes;
+      while (h - l > 1) {
+        const int64_t m = (l + h) >> 1;
+        if (st.cube_start[m] <= j) l = m;
+        else h = m;
+      }
+      atomicAdd(st.jf + l, (double)v);
+      atomicAdd(st.jf2 + l, v2);
+    }
+  }
+}
+
+}  // namespace tq
+
+using namespace tq;
+
+// ----------------------------------------------------------------- C ABI
+static int check_state(const tq_vegas_state* st) {
+  if (!st) return TQ_ERR_ARG;
+  if (!valid_dtype(st->dtype)) return TQ_ERR_DTYPE;
+  if (st->dim < 1 || st->dim > kMaxDim) return TQ_ERR_DIM;
+  if (st->n_bins < 2 || st->n_strat < 1 || st->n_cubes < 1 || st->n_bins > (int64_t(1) << 30))
+    return TQ_ERR_ARG;
+  int64_t nc = 1;
+  for (int k = 0; k < st->dim; ++k) {
+    if (nc > (int64_t(1) << 40) / st->n_strat) return TQ_ERR_TOO_LARGE;
+    nc *= st->n_strat;
+  }
+  if (nc != st->n_cubes) return TQ_ERR_ARG;
+  if (!st->x_edges || !st->dx_edges || !st->weights || !st->counts || !st->dh || !st->jf ||
+      !st->jf2 || !st->neval || !st->cube_start || !st->rng_offset || !st->stats || !st->flags ||
+      !st->scalars || !st->domain)
+    return TQ_ERR_ARG;
+  return TQ_OK;
+}
+
+static int64_t nh_blocks(const tq_vegas_state* st) { return (st->n_cubes + kBlock - 1) / kBlock; }
+static int64_t finish_blocks(const tq_vegas_state* st) {
+  const int64_t need = (st->n_cubes + kBlock - 1) / kBlock;
+  const int64_t cap = (int64_t)sm_count() * 4;
+  return need < cap ? need : cap;
+}
+static size_t map_scratch_bytes(const tq_vegas_state* st) {
+  const size_t DB = (size_t)st->dim * st->n_bins, DB1 = (size_t)st->dim * (st->n_bins + 1);
+  return 2 * DB * 8 + 2 * DB + 16 + DB1 * (8 + 8 + 8);
+}
+
+// Workspace: [0,256) tickets; then nh block totals, finish partials and the
+// map-update scratch, each 256-byte aligned.
+struct VegasWs {
+  unsigned* t_sample;
+  unsigned* t_nh;
+  unsigned* t_finish;
+  int64_t* block_tot;
+  Acc* partials;
+  double* map_scratch;
+  size_t total;
+};
+static VegasWs vegas_ws(const tq_vegas_state* st, void* base) {
+  VegasWs w;
+  char* p = (char*)base;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  w.t_sample = (unsigned*)(p + 0);
+  w.t_nh = (unsigned*)(p + 16);
+  w.t_finish = (unsigned*)(p + 32);
+  size_t off = 256;
+  w.block_tot = (int64_t*)(p + off);
+  off += al(sizeof(int64_t) * (size_t)nh_blocks(st));
+  w.partials = (Acc*)(p + off);
+  off += al(sizeof(Acc) * 3 * (size_t)finish_blocks(st));
+  w.map_scratch = (double*)(p + off);
+  off += al(map_scratch_bytes(st));
+  w.total = off;
+  return w;
+}
+
+extern "C" size_t tq_vegas_workspace_size(const tq_vegas_state* st) {
+  if (check_state(st) != TQ_OK) return 0;
+  return vegas_ws(st, nullptr).total;
+}
+
+#define TQ_VEGAS_WS()                                              \
+  int rc = check_state(st);                                        \
+  if (rc != TQ_OK) return rc;                                      \
+  if (!workspace) return TQ_ERR_ARG;                               \
+  VegasWs ws = vegas_ws(st, workspace);                            \
+  if (workspace_bytes < ws.total) return TQ_ERR_WORKSPACE;         \
+  cudaStream_t s = (cudaStream_t)stream;
+
+extern "C" int tq_vegas_init(const tq_vegas_state* st, void* stream) {
+  const int rc = check_state(st);
+  if (rc != TQ_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t work = st->n_cubes > st->dim * (st->n_bins + 1) ? st->n_cubes : st->dim * (st->n_bins + 1);
+  int64_t g = (work + kBlock - 1) / kBlock;
+  if (g > (int64_t)sm_count() * 8) g = (int64_t)sm_count() * 8;
+  if (st->dtype == TQ_F64)
+    vegas_init_kernel<double><<<(unsigned)g, kBlock, 0, s>>>(*st);
+  else
+    vegas_init_kernel<float><<<(unsigned)g, kBlock, 0, s>>>(*st);
+  return launch_status();
+}
+
+static int launch_sample(const tq_vegas_state* st, int family, const double* params,
+                         int64_t n_samples, uint64_t seed, uint64_t sid, int use_map,
+                         int64_t max_points, bool warm, unsigned* ticket, cudaStream_t s) {
+  SampleArgs a;
+  a.st = *st;
+  a.family = family;
+  a.params = params;
+  a.n_samples = n_samples;
+  a.seed = seed;
+  a.sid = sid;
+  a.use_map = use_map;
+  a.ticket = ticket;
+  const size_t tsize = dtype_size(st->dtype);
+  const size_t limit = 96 * 1024;
+  a.hist_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, true, false) <= limit / 2;
+  a.edges_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, true) <= limit;
+  const size_t smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, a.edges_smem);
+  int64_t tiles = (max_points + kTile - 1) / kTile;
+  const int64_t cap = (int64_t)sm_count() * 8;
+  if (tiles > cap) tiles = cap;
+  if (tiles < 1) tiles = 1;
+  const dim3 grid((unsigned)tiles);
+#define TQ_SAMPLE_LAUNCH(T, WARMB)                                                          \
+  {                                                                                         \
+    auto kfn = vegas_sample_kernel<T, FAM, WARMB>;                                          \
+    if (smem > 48 * 1024) {                                                                 \
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                           (int)smem);                                      \
+      if (e != cudaSuccess) return set_cuda_error(e);                                       \
+    }                                                                                       \
+    kfn<<<grid, kTile, smem, s>>>(a);                                                       \
+  }
+  TQ_DISPATCH_FAMILY(family, FAM, {
+    if (st->dtype == TQ_F64) {
+      if (warm) TQ_SAMPLE_LAUNCH(double, true) else TQ_SAMPLE_LAUNCH(double, false)
+    } else {
+      if (warm) TQ_SAMPLE_LAUNCH(float, true) else TQ_SAMPLE_LAUNCH(float, false)
+    }
+  });
+#undef TQ_SAMPLE_LAUNCH
+  return launch_status();
+}
+
+extern "C" int tq_vegas_warmup_fused(const tq_vegas_state* st, int family, const double* params,
+                                     int64_t n_samples, uint64_t seed, uint64_t stream_id,
+                                     void* workspace, size_t workspace_bytes, void* stream) {
+  TQ_VEGAS_WS();
+  if (!params || n_samples < 1) return TQ_ERR_ARG;
+  return launch_sample(st, family, params, n_samples, seed, stream_id, 1, n_samples, true,
+                       ws.t_sample, s);
+}
+
+extern "C" int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, const double* params,
+                                      uint64_t seed, uint64_t stream_id, int use_grid_improve,
+                                      int64_t max_points, void* workspace, size_t workspace_bytes,
+                                      void* stream) {
+  TQ_VEGAS_WS();
+  if (!params || max_points < 1) return TQ_ERR_ARG;
+  return launch_sample(st, family, params, 0, seed, stream_id, use_grid_improve ? 1 : 0,
+                       max_points, false, ws.t_sample, s);
+}
+
+static int launch_update_map(const tq_vegas_state* st, double alpha, void* workspace,
+                             size_t workspace_bytes, void* smooth_out, void* stream) {
+  TQ_VEGAS_WS();
+  if (st->dtype == TQ_F64)
+    vegas_update_map_kernel<double><<<1, kBlock, 0, s>>>(*st, alpha, ws.map_scratch, smooth_out);
+  else
+    vegas_update_map_kernel<float><<<1, kBlock, 0, s>>>(*st, alpha, ws.map_scratch, smooth_out);
+  return launch_status();
+}
+
+extern "C" int tq_vegas_update_map(const tq_vegas_state* st, double alpha, void* workspace,
+                                   size_t workspace_bytes, void* stream) {
+  return launch_update_map(st, alpha, workspace, workspace_bytes, nullptr, stream);
+}
+
+extern "C" int tq_vegas_smooth_weights(const tq_vegas_state* st, double alpha, void* smoothed,
+                                       void* workspace, size_t workspace_bytes, void* stream) {
+  if (!smoothed) return TQ_ERR_ARG;
+  return launch_update_map(st, alpha, workspace, workspace_bytes, smoothed, stream);
+}
+
+extern "C" int tq_vegas_get_nh(const tq_vegas_state* st, int64_t nevals_exp, int normalize,
+                               void* workspace, size_t workspace_bytes, void* stream) {
+  TQ_VEGAS_WS();
+  if (nevals_exp < 0) return TQ_ERR_ARG;
+  NhArgs a;
+  a.st = *st;
+  a.nevals_exp = nevals_exp;
+  a.normalize = normalize;
+  a.block_tot = ws.block_tot;
+  a.ticket = ws.t_nh;
+  const unsigned g = (unsigned)nh_blocks(st);
+  if (st->dtype == TQ_F64)
+    vegas_nh_kernel<double><<<g, kBlock, 0, s>>>(a);
+  else
+    vegas_nh_kernel<float><<<g, kBlock, 0, s>>>(a);
+  int e = launch_status();
+  if (e != TQ_OK) return e;
+  vegas_nh_fixup_kernel<<<g, kBlock, 0, s>>>(*st, ws.block_tot);
+  return launch_status();
+}
+
+extern "C" int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, int64_t slot,
+                                         void* workspace, size_t workspace_bytes, void* stream) {
+  TQ_VEGAS_WS();
+  if (slot < 0) return TQ_ERR_ARG;
+  FinishArgs a;
+  a.st = *st;
+  a.beta = beta;
+  a.slot = slot;
+  a.partials = ws.partials;
+  a.ticket = ws.t_finish;
+  const unsigned g = (unsigned)finish_blocks(st);
+  if (st->dtype == TQ_F64)
+    vegas_finish_kernel<double><<<g, kBlock, 0, s>>>(a);
+  else
+    vegas_finish_kernel<float><<<g, kBlock, 0, s>>>(a);
+  return launch_status();
+}
+
+static unsigned elem_grid(int64_t n) {
+  int64_t g = (n + kTile - 1) / kTile;
+  const int64_t cap = (int64_t)sm_count() * 16;
+  if (g > cap) g = cap;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+extern "C" int tq_vegas_strat_points(const tq_vegas_state* st, const void* u, int64_t n_points,
+                                     void* y, void* stream) {
+  const int rc = check_state(st);
+  if (rc != TQ_OK) return rc;
+  if (n_points < 0 || (n_points > 0 && (!u || !y))) return TQ_ERR_ARG;
+  if (n_points == 0) return TQ_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (st->dtype == TQ_F64)
+    vegas_strat_points_kernel<double><<<elem_grid(n_points), kTile, 0, s>>>(*st, (const double*)u, n_points, (double*)y);
+  else
+    vegas_strat_points_kernel<float><<<elem_grid(n_points), kTile, 0, s>>>(*st, (const float*)u, n_points, (float*)y);
+  return launch_status();
+}
+
+extern "C" int tq_vegas_map_points(const tq_vegas_state* st, const void* y, int64_t n_points,
+                                   void* x, void* jac, void* stream) {
+  const int rc = check_state(st);
+  if (rc != TQ_OK) return rc;
+  if (n_points < 0 || (n_points > 0 && (!y || !x || !jac))) return TQ_ERR_ARG;
+  if (n_points == 0) return TQ_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (st->dtype == TQ_F64)
+    vegas_map_points_kernel<double><<<elem_grid(n_points), kTile, 0, s>>>(*st, (const double*)y, n_points, (double*)x, (double*)jac);
+  else
+    vegas_map_points_kernel<float><<<elem_grid(n_points), kTile, 0, s>>>(*st, (const float*)y, n_points, (float*)x, (float*)jac);
+  return launch_status();
+}
+
+extern "C" int tq_vegas_accumulate(const tq_vegas_state* st, const void* y, const void* jf,
+                                   int64_t n_points, int accumulate_map, int stratified,
+                                   void* workspace, size_t workspace_bytes, void* stream) {
+  TQ_VEGAS_WS();
+  (void)ws;
+  if (n_points < 0 || (n_points > 0 && (!y || !jf))) return TQ_ERR_ARG;
+  if (n_points == 0) return TQ_OK;
+  if (st->dtype == TQ_F64)
+    vegas_accumulate_kernel<double><<<elem_grid(n_points), kTile, 0, s>>>(*st, (const double*)y, (const double*)jf, n_points, accumulate_map, stratified);
+  else
+    vegas_accumulate_kernel<float><<<elem_grid(n_points), kTile, 0, s>>>(*st, (const float*)y, (const float*)jf, n_points, accumulate_map, stratified);
+  return launch_status();
+}

@@ -37,6 +37,7 @@ def grid_points(rule, dim, n, domain, gl_nodes, start, count, dtype):
         ),
         "tq_grid_points",
     )
+    L.count_launches(1)
     return pts
 
 
@@ -49,6 +50,7 @@ def grid_weights(rule, dim, n, domain, gl_weights, start, count):
         ),
         "tq_grid_weights",
     )
+    L.count_launches(1)
     return w
 
 
@@ -65,6 +67,7 @@ def weighted_sum_into(acc, rule, dim, n, domain, gl_weights, start, values2d):
         ),
         "tq_weighted_sum",
     )
+    L.count_launches(1)
 
 
 def finalize(acc, rule, dim, domain, n_points, S, out_dtype):
@@ -76,6 +79,7 @@ def finalize(acc, rule, dim, domain, n_points, S, out_dtype):
         ),
         "tq_finalize_sum",
     )
+    L.count_launches(1)
     return out
 
 
@@ -117,6 +121,7 @@ def grid_fused(rule, dim, n, domain, gl_nodes, gl_weights, integrand, out_dtype)
         ),
         "tq_grid_fused",
     )
+    L.count_launches(1)
     return out
 
 
@@ -129,6 +134,7 @@ def uniform(seed, stream_id, offset, size, dtype, device):
         ),
         "tq_uniform",
     )
+    L.count_launches(1)
     return out
 
 
@@ -144,4 +150,5 @@ def mc_fused(dim, n_points, domain, integrand, seed, stream_id, offset):
         ),
         "tq_mc_fused",
     )
+    L.count_launches(1)
     return out

@@ -1,0 +1,242 @@
+"""VEGAS (VEGAS+ / "VEGAS Enhanced", reference: integration/vegas.py:13-362).
+
+Two drivers with the reference's algorithm and defaults:
+
+* fused — built-in integrand and this package's counter-based RNG: every
+  warm-up step and iteration is one sampling kernel (Philox draws,
+  stratified points, map transform, integrand, histograms and cube sums in
+  registers/shared memory) plus the small get_NH / finish / map-update
+  kernels.  The host reads results back only at the every-fifth-iteration
+  abort test (vegas.py:170), the only place the reference's control flow
+  depends on them.
+* materialised — any torch integrand or any ``rng`` object: points are
+  written to memory, the integrand runs on them, and the same kernels do the
+  map transform, histograms, cube sums and updates.
+"""
+from __future__ import annotations
+
+import math
+import warnings
+
+import torch
+
+from .. import _lib as L
+from ..integrands import BuiltinIntegrand
+from .base_integrator import BaseIntegrator
+from .rng import RNG
+from .utils import _setup_integration_domain
+from ._vegas_state import VegasDevice, n_strat_for
+from .vegas_map import VEGASMap
+from .vegas_stratification import VEGASStratification
+
+ALPHA = 0.5  # vegas.py:220
+BETA = 0.75  # vegas_stratification.py:13
+
+
+class VEGAS(BaseIntegrator):
+    """VEGAS Enhanced (arXiv:2009.05112) with adaptive map and stratification."""
+
+    def __init__(self):
+        super().__init__()
+
+    def integrate(self, fn, dim, N=10000, integration_domain=None, seed=None, rng=None,
+                  use_grid_improve=True, eps_rel=0, eps_abs=0, max_iterations=20,
+                  use_warmup=True, backend=None, n_intervals=None):
+        """Integrate fn with VEGAS+ using about N evaluations.
+
+        Arguments as the reference's VEGAS.integrate; ``n_intervals``
+        (extension, default None) overrides the number of map intervals per
+        dimension, which the reference fixes to max(2, N_increment // 10)."""
+        self._check_inputs(dim=dim, N=N, integration_domain=integration_domain)
+        self._dim = dim
+        self._nr_of_fevals = 0
+        self._max_iterations = max_iterations
+        self._eps_rel = eps_rel
+        self._eps_abs = eps_abs
+        self.use_grid_improve = use_grid_improve
+        self.N = N
+        self._starting_N = N // (self._max_iterations + 5)
+        self._N_increment = N // (self._max_iterations + 5)
+        self._fn = fn
+        domain = _setup_integration_domain(dim, integration_domain, backend)
+        self.backend = "torch"
+        self.dtype = domain.dtype
+        if self.dtype not in (torch.float32, torch.float64):
+            raise ValueError(f"unsupported domain dtype {self.dtype}")
+        if rng is None:
+            rng = RNG(backend="torch", seed=seed)
+        elif seed is not None:
+            raise ValueError("seed and rng cannot both be passed")
+        self.rng = rng
+
+        domain_starts = domain[:, 0]
+        domain_sizes = domain[:, 1] - domain_starts
+        domain_volume = torch.prod(domain_sizes)
+
+        def transformed_integrand(x):
+            return fn(x * domain_sizes + domain_starts) * domain_volume
+
+        self._fn = transformed_integrand
+
+        N_intervals = n_intervals if n_intervals is not None else max(2, self._N_increment // 10)
+        n_strat = n_strat_for(self._N_increment, dim)
+        self._dev = VegasDevice(dim, self.dtype, N_intervals, n_strat, domain.device, domain,
+                                stats_slots=max(8, max_iterations + 5))
+        self.map = VEGASMap(N_intervals, dim, None, self.dtype, _device_state=self._dev)
+        self.strat = VEGASStratification(self._N_increment, dim, rng, None, self.dtype,
+                                         _device_state=self._dev)
+        self.results = []
+        self.sigma2 = []
+        self.it = 0
+
+        fused = (
+            isinstance(fn, BuiltinIntegrand)
+            and type(rng) is RNG
+            and fn.dim == dim
+            and not (torch.is_grad_enabled() and (domain.requires_grad or fn.requires_grad()))
+        )
+        if fused:
+            return self._integrate_fused(fn, domain, use_warmup)
+        return self._integrate_materialised(domain, use_warmup)
+
+    # ------------------------------------------------------------ fused
+    def _integrate_fused(self, fn, domain, use_warmup):
+        dev = self._dev
+        rng = self.rng
+        params = fn.device_params(domain.device)
+        dev.rng_offset.fill_(rng.offset)
+        self.alpha = ALPHA
+        warm_evals = 0
+        if use_warmup:
+            ns = self._starting_N // 5
+            for _ in range(5):
+                if ns > 0:
+                    dev.warmup_fused(fn.family, params, ns, rng.seed, rng.stream_id)
+                dev.update_map(self.alpha)
+            warm_evals = 5 * ns
+        self._nr_of_fevals = warm_evals
+        normalize = False
+        max_pts = lambda: self._starting_N + self._starting_N // 64 + 2 * dev.n_cubes + 1024  # noqa: E731
+        while True:
+            self.it += 1
+            slot = self.it - 1
+            dev.ensure_slots(slot + 1)
+            dev.get_nh(self._starting_N, normalize)
+            dev.iterate_fused(fn.family, params, rng.seed, rng.stream_id, self.use_grid_improve, max_pts())
+            dev.finish(BETA, slot)
+            normalize = True
+            if self.use_grid_improve:
+                dev.update_map(self.alpha)
+            if self.it % 5 == 0:
+                stats = dev.stats[: self.it].cpu()  # one host sync per five iterations
+                self.map.check_flags()
+                first = self.it - 5
+                self.results = [float(v) for v in stats[first : self.it, 0]]
+                self.sigma2 = [float(v) for v in stats[first : self.it, 1]]
+                self._nr_of_fevals = warm_evals + int(stats[: self.it, 2].sum())
+                if self._check_abort_conditions():
+                    break
+        rng.offset = int(dev.rng_offset.item())
+        # leave dh normalised, as update_DH does
+        s = dev.scalars[0].to(self.dtype)
+        dev.dh.copy_(torch.where(s != 0, dev.dh / s, dev.dh))
+        return torch.tensor(self._get_result(), dtype=self.dtype, device=domain.device)
+
+    # ----------------------------------------------------- materialised
+    def _integrate_materialised(self, domain, use_warmup):
+        if use_warmup:
+            self._warmup_grid(5, self._starting_N // 5)
+        while True:
+            self.it = self.it + 1
+            self.results.append(0)
+            self.sigma2.append(0)
+            self._run_iteration()
+            if self._check_abort_conditions():
+                break
+        return torch.tensor(self._get_result(), dtype=self.dtype, device=domain.device)
+
+    def _warmup_grid(self, warmup_N_it=5, N_samples=1000):
+        """Warm up the map: warmup_N_it rounds of N_samples uniform points
+        (vegas.py:211-266)."""
+        self.alpha = ALPHA
+        for _ in range(warmup_N_it):
+            yrnd = self.rng.uniform(size=[N_samples, self._dim], dtype=self.dtype)
+            yrnd = torch.as_tensor(yrnd).to(self._dev.device, self.dtype) * 0.999999
+            x, jac = self.map.get_X_and_Jac(yrnd)
+            f_eval = self._eval(x).squeeze()
+            jf_vec = f_eval * jac
+            jf_vec2 = (jf_vec**2).detach()
+            if N_samples > 0:
+                self.map.accumulate_weight(yrnd, jf_vec2)
+            self.map.update_map()
+
+    def _run_iteration(self):
+        """One stratified iteration (vegas.py:268-315)."""
+        neval = self.strat.get_NH(self._starting_N)
+        y = self.strat.get_Y(neval)
+        x, jac = self.map.get_X_and_Jac(y)
+        f_eval = self._eval(x).squeeze()
+        jf_vec = f_eval * jac
+        jf_vec2 = (jf_vec**2).detach()
+        if self.use_grid_improve:
+            self.map.accumulate_weight(y, jf_vec2)
+        self.strat.accumulate_weight(neval, jf_vec)
+        slot = self.it - 1
+        self.strat.update_DH(slot)  # also the per-iteration result and variance
+        if self.use_grid_improve:
+            self.map.update_map()
+        st = self._dev.stats[slot].cpu()
+        self.results[-1] = float(st[0])
+        self.sigma2[-1] = float(st[1])
+        acc = math.sqrt(self.sigma2[-1])
+        if self.results[-1] != 0.0:
+            acc = acc / abs(self.results[-1])
+        return acc
+
+    # ------------------------------------------------- shared host logic
+    def _check_abort_conditions(self):
+        """Every fifth iteration: stop on accuracy, adapt the evaluations per
+        iteration, stop on budget/iterations (vegas.py:161-209)."""
+        if self.it % 5 > 0:
+            return False
+        res_abs = abs(self._get_result())
+        err = self._get_error()
+        chi2 = self._get_chisq()
+        if (err <= self._eps_rel * res_abs or err <= self._eps_abs) and chi2 / 5.0 < 1.0:
+            return True
+        if chi2 / 5.0 < 1.0:
+            if res_abs == 0.0:
+                self._starting_N += self._N_increment
+            else:
+                acc = err / res_abs
+                self._starting_N = min(
+                    self._starting_N + self._N_increment,
+                    int(self._starting_N * math.sqrt(acc / (self._eps_rel + 1e-8))),
+                )
+        elif chi2 / 5.0 > 1.0:
+            self._starting_N += self._N_increment
+        if self._nr_of_fevals + self._starting_N * 5 > self.N:
+            return True
+        if self.it + 5 > self._max_iterations:
+            return True
+        self.results = []
+        self.sigma2 = []
+        return False
+
+    def _get_result(self):
+        """Inverse-variance weighted mean of the iteration results (EQ 30)."""
+        if any(s == 0.0 for s in self.sigma2):
+            return sum(self.results) / len(self.results)
+        num = sum(r / s for r, s in zip(self.results, self.sigma2))
+        den = sum(1.0 / s for s in self.sigma2)
+        return num / den
+
+    def _get_error(self):
+        """Error estimate from the variances (EQ 31)."""
+        res = sum(1.0 / s for s in self.sigma2 if s != 0.0)
+        return self.sigma2[0] if res == 0 else 1.0 / math.sqrt(res)
+
+    def _get_chisq(self):
+        """Chi square of the iteration results (EQ 32)."""
+        I_final = self._get_result()
+        return sum(((r - I_final) ** 2 / s for r, s in zip(self.results, self.sigma2) if r != I_final), 0.0)
