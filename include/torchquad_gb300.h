@@ -186,12 +186,29 @@ typedef struct tq_vegas_state {
   int64_t* cube_start;  /* [n_cubes+1] exclusive prefix of neval; last = total */
   uint64_t* rng_offset; /* [1] Philox block offset; the sampling kernels
                          * advance it by the blocks their draws consumed       */
-  double* stats;        /* [n_slots][4]: result, sigma2, points, (unused)      */
+  double* stats;        /* [n_stat_slots][4]: result, sigma2, points, unused   */
+  int64_t n_stat_slots; /* rows of stats                                       */
   int32_t* flags;       /* [4]: [0] map updates skipped (all-zero weights),
-                         * [1] infinite edges repaired, [2] unrepairable edges */
+                         * [1] infinite edges repaired, [2] unrepairable edges,
+                         * [3] a finish found its slot >= n_stat_slots       */
   double* scalars;      /* [4]: [0] sum of the unnormalised dh              */
   const void* domain;   /* [d][2] dtype                                        */
+  int64_t* control;     /* [8] per-iteration inputs read by the kernels, so a
+                         * sequence of launches can be captured once and
+                         * replayed: [0] nevals_exp (VEGAS._starting_N),
+                         * [1] statistics slot of the next finish (advanced by
+                         * tq_vegas_finish_iteration), [2] 1 if dh awaits
+                         * normalisation (set by finish, cleared by get_nh),
+                         * [3] Philox seed, [4] Philox stream id           */
 } tq_vegas_state;
+
+enum {
+  TQ_VC_NEVALS = 1,
+  TQ_VC_SLOT = 2,
+  TQ_VC_NORMALIZE = 4,
+  TQ_VC_SEED = 8,
+  TQ_VC_STREAM = 16
+};
 
 /* Scratch bytes the VEGAS entry points need for this state. */
 size_t tq_vegas_workspace_size(const tq_vegas_state* st);
@@ -200,13 +217,18 @@ size_t tq_vegas_workspace_size(const tq_vegas_state* st);
  * initial VEGASStratification.dh (vegas_stratification.py:13-44). */
 int tq_vegas_init(const tq_vegas_state* st, void* stream);
 
+/* Writes the control fields selected by `mask` (TQ_VC_* bits) on the stream
+ * (a one-thread kernel, so it orders with the other launches). */
+int tq_vegas_set_control(const tq_vegas_state* st, int mask, int64_t nevals_exp, int64_t slot,
+                         int64_t normalize, uint64_t seed, uint64_t stream_id, void* stream);
+
 /* One warm-up iteration, fused (vegas.py:228-256 without the map update):
- * y = u * 0.999999 with u from the Philox stream (seed, stream_id,
- * *st->rng_offset), x = map(y), f = integrand(domain(x)) * volume,
- * accumulate (f*jac)^2 into the map.  Advances *st->rng_offset. */
+ * y = u * 0.999999 with u from the Philox stream (control seed and stream
+ * id, block offset *st->rng_offset), x = map(y), f = integrand(domain(x)) *
+ * volume, accumulate (f*jac)^2 into the map.  Advances *st->rng_offset. */
 int tq_vegas_warmup_fused(const tq_vegas_state* st, int family, const double* params,
-                          int64_t n_samples, uint64_t seed, uint64_t stream_id,
-                          void* workspace, size_t workspace_bytes, void* stream);
+                          int64_t n_samples, void* workspace, size_t workspace_bytes,
+                          void* stream);
 
 /* VEGASMap.update_map (vegas_map.py:185-261) incl. _smooth_map (:113-172);
  * resets weights and counts.  Sets flags[0] if a dimension's weights are all
@@ -222,12 +244,12 @@ int tq_vegas_smooth_weights(const tq_vegas_state* st, double alpha, void* smooth
                             void* workspace, size_t workspace_bytes, void* stream);
 
 /* VEGASStratification.get_NH (vegas_stratification.py:92-103):
- * neval = max(2, floor(dh * nevals_exp)), cube_start = exclusive prefix,
- * cube_start[n_cubes] = total; zeroes jf/jf2.  If `normalize` != 0 the dh
+ * neval = max(2, floor(dh * control[0])), cube_start = exclusive prefix,
+ * cube_start[n_cubes] = total; zeroes jf/jf2.  If control[2] != 0 the dh
  * left unnormalised by tq_vegas_finish_iteration is first divided by its sum
- * (vegas_stratification.py:88-90). */
-int tq_vegas_get_nh(const tq_vegas_state* st, int64_t nevals_exp, int normalize,
-                    void* workspace, size_t workspace_bytes, void* stream);
+ * (vegas_stratification.py:88-90) and control[2] is cleared. */
+int tq_vegas_get_nh(const tq_vegas_state* st, void* workspace, size_t workspace_bytes,
+                    void* stream);
 
 /* One stratified iteration, fused (vegas.py:274-291): for every point of
  * every cube (cube_start order), y = (cube position + u) / n_strat
@@ -235,19 +257,19 @@ int tq_vegas_get_nh(const tq_vegas_state* st, int64_t nevals_exp, int normalize,
  * (get_X/get_Jac, vegas_map.py:44-74), f = integrand(domain(x)) * volume;
  * accumulates the map weights/counts (if use_grid_improve) and the per-cube
  * sums jf/jf2 (accumulate_weight, vegas_stratification.py:46-70).
- * max_points bounds cube_start[n_cubes] for sizing the launch.
- * Advances *st->rng_offset. */
+ * max_points sizes the launch (an upper bound of cube_start[n_cubes] or 0
+ * for a grid that covers any count).  Advances *st->rng_offset. */
 int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, const double* params,
-                           uint64_t seed, uint64_t stream_id, int use_grid_improve,
-                           int64_t max_points, void* workspace, size_t workspace_bytes,
-                           void* stream);
+                           int use_grid_improve, int64_t max_points, void* workspace,
+                           size_t workspace_bytes, void* stream);
 
-/* Per-cube estimates -> stats[slot] = {sum ih, sum sig2/n, points}
+/* Per-cube estimates -> stats[control[1]] = {sum ih, sum sig2/n, points}
  * (vegas.py:293-303, fp64 compensated sums) and the unnormalised dampened
  * counts dh (update_DH, vegas_stratification.py:72-90; the division by the
- * sum happens in the next tq_vegas_get_nh). */
-int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, int64_t slot,
-                              void* workspace, size_t workspace_bytes, void* stream);
+ * sum happens in the next tq_vegas_get_nh).  Advances control[1] and sets
+ * control[2].  The caller keeps control[1] below the rows of stats. */
+int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, void* workspace,
+                              size_t workspace_bytes, void* stream);
 
 /* Materialised path (arbitrary torch integrands, injected uniforms). */
 

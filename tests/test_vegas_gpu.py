@@ -111,7 +111,8 @@ def test_fused_iteration_matches_reference_state(case, cuda):
         dev.get_nh(st["starting_N"], normalize=False)
         assert dev.neval.cpu().tolist() == st["neval"]  # bit-exact
         M = sum(st["neval"])
-        dev.iterate_fused(f.family, params, case["seed"], 0, True, M)
+        dev.set_control(L.TQ_VC_SEED | L.TQ_VC_STREAM, seed=case["seed"], sid=0)
+        dev.iterate_fused(f.family, params, True, M)
         w = dev.weights.clone()
         _check_step(case, st, dev, dtype, cuda, w)
         assert int(dev.rng_offset.item()) == st["rng_offset"] + tq.RNG.blocks_for(3 * M, dtype)
@@ -236,6 +237,23 @@ def test_peak_accuracy_reference_cases(cuda):
         return torch.exp(torch.sum(d2[:, 0] - x, dim=1)) + torch.exp(torch.sum(x - d2[:, 1], dim=1))
 
     ref2 = 2.0 - 4.0 * math.exp(-100.0) + 2.0 * math.exp(-200.0)
+    # Two peaks in opposite corners: whether the warm-up finds both depends on
+    # the draws.  With this package's Philox stream the reference algorithm
+    # itself (the oracle, same draws) finds one peak for two of the
+    # reference's five seeds; the GPU must reproduce the algorithm on every
+    # seed and be accurate where the algorithm is.
+    from oracle import philox as OP
+    from oracle import vegas as OV
+
+    d2n = d2.cpu().numpy()
+
+    def diag_np(x):
+        return np.exp(np.sum(d2n[:, 0] - x, axis=1)) + np.exp(np.sum(x - d2n[:, 1], axis=1))
+
+    good = 0
     for seed in [0, 1, 2, 3, 41317]:
-        r = tq.VEGAS().integrate(diag, 2, N=30000, integration_domain=d2, seed=seed)
-        assert abs(r.item() - ref2) < 0.03
+        r = tq.VEGAS().integrate(diag, 2, N=30000, integration_domain=d2, seed=seed).item()
+        o = OV.Vegas().integrate(diag_np, 2, 30000, d2n, OP.ReplayStream(seed), dt=np.float64)
+        assert abs(r - o) <= 1e-9 * abs(o)
+        good += abs(r - ref2) < 0.03
+    assert good >= 3

@@ -53,10 +53,15 @@ class VegasState(ctypes.Structure):
         ("cube_start", c_void_p),
         ("rng_offset", c_void_p),
         ("stats", c_void_p),
+        ("n_stat_slots", c_int64),
         ("flags", c_void_p),
         ("scalars", c_void_p),
         ("domain", c_void_p),
+        ("control", c_void_p),
     ]
+
+
+TQ_VC_NEVALS, TQ_VC_SLOT, TQ_VC_NORMALIZE, TQ_VC_SEED, TQ_VC_STREAM = 1, 2, 4, 8, 16
 
 
 _VS = POINTER(VegasState)
@@ -94,14 +99,13 @@ SIGNATURES = {
     "tq_mc_fused_workspace_size": (c_size_t, [c_int, c_int64]),
     "tq_vegas_workspace_size": (c_size_t, [_VS]),
     "tq_vegas_init": (c_int, [_VS, c_void_p]),
-    "tq_vegas_warmup_fused": (
-        c_int, [_VS, c_int, c_void_p, c_int64, c_uint64, c_uint64, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_set_control": (c_int, [_VS, c_int, c_int64, c_int64, c_int64, c_uint64, c_uint64, c_void_p]),
+    "tq_vegas_warmup_fused": (c_int, [_VS, c_int, c_void_p, c_int64, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_update_map": (c_int, [_VS, c_double, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_smooth_weights": (c_int, [_VS, c_double, c_void_p, c_void_p, c_size_t, c_void_p]),
-    "tq_vegas_get_nh": (c_int, [_VS, c_int64, c_int, c_void_p, c_size_t, c_void_p]),
-    "tq_vegas_iterate_fused": (
-        c_int, [_VS, c_int, c_void_p, c_uint64, c_uint64, c_int, c_int64, c_void_p, c_size_t, c_void_p]),
-    "tq_vegas_finish_iteration": (c_int, [_VS, c_double, c_int64, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_get_nh": (c_int, [_VS, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_iterate_fused": (c_int, [_VS, c_int, c_void_p, c_int, c_int64, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_finish_iteration": (c_int, [_VS, c_double, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_strat_points": (c_int, [_VS, c_void_p, c_int64, c_void_p, c_void_p]),
     "tq_vegas_map_points": (c_int, [_VS, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "tq_vegas_accumulate": (

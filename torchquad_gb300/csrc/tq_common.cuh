@@ -153,6 +153,30 @@ struct Uniform<double> {
   }
 };
 
+// --------------------------------------------- division by an invariant
+// Unsigned 32-bit division by a run-time constant d >= 1 with one multiply-
+// high, the round-up method of Granlund & Montgomery, "Division by invariant
+// integers using multiplication" (PLDI 1994), Fig. 4.1:
+//   l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+//   q = (t + ((n - t) >> min(l,1))) >> max(l-1,0), t = mulhi(m, n).
+struct FastDiv {
+  uint32_t d, m, s1, s2;
+};
+__host__ __device__ inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f;
+  uint32_t l = 0;
+  while (l < 32 && (uint64_t(1) << l) < d) ++l;
+  f.d = d;
+  f.m = (uint32_t)(((uint64_t(1) << 32) * ((uint64_t(1) << l) - d)) / d + 1);
+  f.s1 = l < 1 ? l : 1;
+  f.s2 = l > 1 ? l - 1 : 0;
+  return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+  const uint32_t t = __umulhi(f.m, n);
+  return (t + ((n - t) >> f.s1)) >> f.s2;
+}
+
 // ------------------------------------------------------------- grid nodes
 // torch's CPU linspace, which IntegrationGrid uses through
 // _linspace_with_grads (utils.py:24-58): step = (b-a)/(n-1) in the working

@@ -99,17 +99,29 @@ struct SampleArgs {
   int family;
   const double* params;
   int64_t n_samples;  // warm-up: points; iterations: read from cube_start
-  uint64_t seed, sid;
   int use_map;        // accumulate the map histogram
   int edges_smem, hist_smem;
+  int small_cubes;    // n_cubes < 2^32: cube digits with 32-bit division
+  FastDiv ns_div;     // division by n_strat
   unsigned* ticket;
+};
+
+// Histogram weight type in shared memory: fp32 atomics are native, so the
+// fp32 path privatises in fp32 and flushes once per CTA into fp64.
+template <typename T>
+struct HistT {
+  using type = double;
+};
+template <>
+struct HistT<float> {
+  using type = float;
 };
 
 template <typename T>
 struct Smem {
   T* xe;
   T* dxe;
-  double* hw;
+  typename HistT<T>::type* hw;
   unsigned* hc;
   double* sj;
   double* sj2;
@@ -129,10 +141,10 @@ __device__ Smem<T> carve(unsigned char* base, const SampleArgs& a) {
   s.cs = (int64_t*)(base + off);
   off += sizeof(int64_t) * (kCubeSlots + 1);
   if (a.hist_smem) {
-    s.hw = (double*)(base + off);
+    s.hw = (typename HistT<T>::type*)(base + off);
     off += sizeof(double) * d * B;
   } else {
-    s.hw = a.st.weights;
+    s.hw = nullptr;
   }
   if (a.edges_smem) {
     s.xe = (T*)(base + off);
@@ -186,7 +198,7 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
   }
   if (a.hist_smem) {
     for (int64_t i = threadIdx.x; i < d * B; i += blockDim.x) {
-      sm.hw[i] = 0.0;
+      sm.hw[i] = 0;
       sm.hc[i] = 0u;
     }
   }
@@ -194,6 +206,7 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
 
   const int64_t M = WARM ? a.n_samples : st.cube_start[st.n_cubes];
   const uint64_t offset = *st.rng_offset;
+  const uint64_t seed = (uint64_t)st.control[3], sid = (uint64_t)st.control[4];
   const int64_t ns = st.n_strat;
   constexpr int PB = Uniform<T>::per_block;
 
@@ -216,9 +229,10 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
       for (int i = threadIdx.x; i < nc; i += blockDim.x) sm.sj[i] = sm.sj2[i] = 0.0;
       __syncthreads();
     }
+    int slot = -1;
+    double jfd = 0.0, jf2 = 0.0;
     if (j < M) {
-      int64_t c = 0;
-      int slot = 0;
+      uint64_t c = 0;
       if (!WARM) {
         int l = 0, h = nc;  // largest l with cs[l] <= j
         while (h - l > 1) {
@@ -227,31 +241,43 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
           else h = mid;
         }
         slot = l;
-        c = tile_c0 + l;
+        c = (uint64_t)(tile_c0 + l);
       }
-      uint64_t cur = ~0ull;
+      // Philox block of this point's first draw; later draws follow
+      const uint64_t e0 = (uint64_t)j * (uint64_t)d;
+      const uint64_t blk0 = offset + e0 / PB;
+      const int lane0 = (int)(e0 % PB);
+      int cur = -1;
       uint4 r = make_uint4(0, 0, 0, 0);
       T jac = (T)1;
       T s = T(0);
       int ids[kMaxDim];
-      int64_t cc = c;
+      uint32_t c32 = (uint32_t)c;
 #pragma unroll
       for (int k = 0; k < kMaxDim; ++k) {
         if (k < d) {
-          const uint64_t e = (uint64_t)j * d + k;
-          const uint64_t blk = e / PB;
-          if (blk != cur) {
-            r = philox_block(a.seed, a.sid, offset + blk);
-            cur = blk;
+          const int le = lane0 + k;
+          const int bi = le / PB;
+          if (bi != cur) {
+            r = philox_block(seed, sid, blk0 + (uint64_t)bi);
+            cur = bi;
           }
-          const T u = Uniform<T>::from(r, (int)(e - blk * PB));
+          const T u = Uniform<T>::from(r, le - bi * PB);
           T y;
           if (WARM) {
             y = mul_rn(u, warm_scale<T>());
           } else {
-            const int64_t q = cc / ns;
-            y = strat_y<T>(cc - q * ns, u, ns);
-            cc = q;
+            int64_t pos;
+            if (a.small_cubes) {
+              const uint32_t q = fdiv(c32, a.ns_div);
+              pos = (int64_t)(c32 - q * a.ns_div.d);
+              c32 = q;
+            } else {
+              const uint64_t q = c / (uint64_t)ns;
+              pos = (int64_t)(c - q * (uint64_t)ns);
+              c = q;
+            }
+            y = strat_y<T>(pos, u, ns);
           }
           T x, jf_k;
           ids[k] = map_coord<T>(sm.xe + k * (B + 1), sm.dxe + k * B, B, y, x, jf_k);
@@ -264,13 +290,16 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
       }
       const T f = mul_rn(fam_outer<FAM, T>(fam, s), volume);
       const T jfv = mul_rn(f, jac);
-      const double jf2 = (double)jfv * (double)jfv;
+      jfd = (double)jfv;
+      jf2 = jfd * jfd;
       if (a.use_map) {
+        using H = typename HistT<T>::type;
+        const H hv = (H)jf2;
 #pragma unroll
         for (int k = 0; k < kMaxDim; ++k) {
           if (k < d) {
             if (a.hist_smem) {
-              atomicAdd(sm.hw + k * B + ids[k], jf2);
+              atomicAdd(sm.hw + k * B + ids[k], hv);
               atomicAdd(sm.hc + k * B + ids[k], 1u);
             } else {
               atomicAdd(st.weights + k * B + ids[k], jf2);
@@ -279,8 +308,24 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
           }
         }
       }
-      if (!WARM) {
-        atomicAdd(sm.sj + slot, (double)jfv);
+    }
+    if (!WARM) {
+      // Points are in cube order: segmented inclusive scan over the warp,
+      // then one shared-memory add per cube segment.
+      const int lane = threadIdx.x & 31;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double a1 = __shfl_up_sync(0xffffffffu, jfd, o);
+        const double a2 = __shfl_up_sync(0xffffffffu, jf2, o);
+        const int so = __shfl_up_sync(0xffffffffu, slot, o);
+        if (lane >= o && so == slot) {
+          jfd += a1;
+          jf2 += a2;
+        }
+      }
+      const int next = __shfl_down_sync(0xffffffffu, slot, 1);
+      if (slot >= 0 && (lane == 31 || next != slot)) {
+        atomicAdd(sm.sj + slot, jfd);
         atomicAdd(sm.sj2 + slot, jf2);
       }
     }
@@ -297,7 +342,7 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
     __syncthreads();
     for (int64_t i = threadIdx.x; i < d * B; i += blockDim.x) {
       if (sm.hc[i]) {
-        atomicAdd(st.weights + i, sm.hw[i]);
+        atomicAdd(st.weights + i, (double)sm.hw[i]);
         atomicAdd((unsigned long long*)(st.counts + i), (unsigned long long)sm.hc[i]);
       }
     }
@@ -313,8 +358,6 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
 // ----------------------------------------------------------- get_NH
 struct NhArgs {
   tq_vegas_state st;
-  int64_t nevals_exp;
-  int normalize;
   int64_t* block_tot;  // [blocks]
   unsigned* ticket;
 };
@@ -324,16 +367,18 @@ __global__ void __launch_bounds__(kBlock) vegas_nh_kernel(NhArgs a) {
   const tq_vegas_state& st = a.st;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t nh = 0;
+  const int64_t nevals_exp = st.control[0];
+  const int64_t normalize = st.control[2];
   if (c < st.n_cubes) {
     T dh = ((T*)st.dh)[c];
-    if (a.normalize) {
+    if (normalize) {
       const T sum = (T)st.scalars[0];
       if (sum != (T)0) {
         dh = div_rn(dh, sum);  // vegas_stratification.py:88-90
         ((T*)st.dh)[c] = dh;
       }
     }
-    T f = floor(mul_rn(dh, (T)a.nevals_exp));  // :102
+    T f = floor(mul_rn(dh, (T)nevals_exp));  // :102
     f = f < (T)2 ? (T)2 : f;                    // :103 clip(nh, 2, None)
     nh = (int64_t)f;
     st.neval[c] = nh;
@@ -373,6 +418,7 @@ __global__ void __launch_bounds__(kBlock) vegas_nh_kernel(NhArgs a) {
         run += t;
       }
       st.cube_start[st.n_cubes] = run;
+      st.control[2] = 0;
       *a.ticket = 0u;
     }
   }
@@ -388,7 +434,6 @@ __global__ void __launch_bounds__(kBlock) vegas_nh_fixup_kernel(tq_vegas_state s
 struct FinishArgs {
   tq_vegas_state st;
   double beta;
-  int64_t slot;
   Acc* partials;  // [blocks][3]
   unsigned* ticket;
 };
@@ -437,10 +482,17 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
     s = block_reduce<kBlock>(s);
     ds = block_reduce<kBlock>(ds);
     if (threadIdx.x == 0) {
-      double* out = st.stats + 4 * a.slot;
-      out[0] = r.s + r.c;
-      out[1] = s.s + s.c;
-      out[2] = (double)st.cube_start[st.n_cubes];
+      const int64_t slot = st.control[1];
+      if (slot >= 0 && slot < st.n_stat_slots) {
+        double* out = st.stats + 4 * slot;
+        out[0] = r.s + r.c;
+        out[1] = s.s + s.c;
+        out[2] = (double)st.cube_start[st.n_cubes];
+      } else {
+        st.flags[3] = 1;
+      }
+      st.control[1] = slot + 1;
+      st.control[2] = 1;
       // the sum the reference normalises with is taken in the state dtype
       st.scalars[0] = (double)(T)(ds.s + ds.c);
       *a.ticket = 0u;
@@ -644,6 +696,19 @@ __global__ void vegas_init_kernel(tq_vegas_state st) {
     st.flags[threadIdx.x] = 0;
     st.scalars[threadIdx.x] = 0.0;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st.control[1] = 0;
+    st.control[2] = 0;
+  }
+}
+
+__global__ void vegas_set_control_kernel(int64_t* control, int mask, int64_t nevals, int64_t slot,
+                                         int64_t normalize, uint64_t seed, uint64_t sid) {
+  if (mask & TQ_VC_NEVALS) control[0] = nevals;
+  if (mask & TQ_VC_SLOT) control[1] = slot;
+  if (mask & TQ_VC_NORMALIZE) control[2] = normalize;
+  if (mask & TQ_VC_SEED) control[3] = (int64_t)seed;
+  if (mask & TQ_VC_STREAM) control[4] = (int64_t)sid;
 }
 
 // ------------------------------------------------ materialised kernels
@@ -741,7 +806,7 @@ static int check_state(const tq_vegas_state* st) {
   if (nc != st->n_cubes) return TQ_ERR_ARG;
   if (!st->x_edges || !st->dx_edges || !st->weights || !st->counts || !st->dh || !st->jf ||
       !st->jf2 || !st->neval || !st->cube_start || !st->rng_offset || !st->stats || !st->flags ||
-      !st->scalars || !st->domain)
+      !st->scalars || !st->domain || !st->control || st->n_stat_slots < 1)
     return TQ_ERR_ARG;
   return TQ_OK;
 }
@@ -814,24 +879,24 @@ extern "C" int tq_vegas_init(const tq_vegas_state* st, void* stream) {
 }
 
 static int launch_sample(const tq_vegas_state* st, int family, const double* params,
-                         int64_t n_samples, uint64_t seed, uint64_t sid, int use_map,
-                         int64_t max_points, bool warm, unsigned* ticket, cudaStream_t s) {
+                         int64_t n_samples, int use_map, int64_t max_points, bool warm,
+                         unsigned* ticket, cudaStream_t s) {
   SampleArgs a;
   a.st = *st;
   a.family = family;
   a.params = params;
   a.n_samples = n_samples;
-  a.seed = seed;
-  a.sid = sid;
   a.use_map = use_map;
   a.ticket = ticket;
+  a.small_cubes = st->n_cubes < (int64_t(1) << 32) && st->n_strat < (int64_t(1) << 31);
+  a.ns_div = make_fastdiv((uint32_t)(a.small_cubes ? st->n_strat : 1));
   const size_t tsize = dtype_size(st->dtype);
   const size_t limit = 96 * 1024;
   a.hist_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, true, false) <= limit / 2;
   a.edges_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, true) <= limit;
   const size_t smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, a.edges_smem);
-  int64_t tiles = (max_points + kTile - 1) / kTile;
   const int64_t cap = (int64_t)sm_count() * 8;
+  int64_t tiles = max_points > 0 ? (max_points + kTile - 1) / kTile : cap;
   if (tiles > cap) tiles = cap;
   if (tiles < 1) tiles = 1;
   const dim3 grid((unsigned)tiles);
@@ -856,23 +921,32 @@ static int launch_sample(const tq_vegas_state* st, int family, const double* par
   return launch_status();
 }
 
+extern "C" int tq_vegas_set_control(const tq_vegas_state* st, int mask, int64_t nevals_exp,
+                                    int64_t slot, int64_t normalize, uint64_t seed,
+                                    uint64_t stream_id, void* stream) {
+  const int rc = check_state(st);
+  if (rc != TQ_OK) return rc;
+  if ((mask & TQ_VC_NEVALS) && nevals_exp < 0) return TQ_ERR_ARG;
+  vegas_set_control_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(st->control, mask, nevals_exp, slot,
+                                                              normalize, seed, stream_id);
+  return launch_status();
+}
+
 extern "C" int tq_vegas_warmup_fused(const tq_vegas_state* st, int family, const double* params,
-                                     int64_t n_samples, uint64_t seed, uint64_t stream_id,
-                                     void* workspace, size_t workspace_bytes, void* stream) {
+                                     int64_t n_samples, void* workspace, size_t workspace_bytes,
+                                     void* stream) {
   TQ_VEGAS_WS();
   if (!params || n_samples < 1) return TQ_ERR_ARG;
-  return launch_sample(st, family, params, n_samples, seed, stream_id, 1, n_samples, true,
-                       ws.t_sample, s);
+  return launch_sample(st, family, params, n_samples, 1, n_samples, true, ws.t_sample, s);
 }
 
 extern "C" int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, const double* params,
-                                      uint64_t seed, uint64_t stream_id, int use_grid_improve,
-                                      int64_t max_points, void* workspace, size_t workspace_bytes,
-                                      void* stream) {
+                                      int use_grid_improve, int64_t max_points, void* workspace,
+                                      size_t workspace_bytes, void* stream) {
   TQ_VEGAS_WS();
-  if (!params || max_points < 1) return TQ_ERR_ARG;
-  return launch_sample(st, family, params, 0, seed, stream_id, use_grid_improve ? 1 : 0,
-                       max_points, false, ws.t_sample, s);
+  if (!params || max_points < 0) return TQ_ERR_ARG;
+  return launch_sample(st, family, params, 0, use_grid_improve ? 1 : 0, max_points, false,
+                       ws.t_sample, s);
 }
 
 static int launch_update_map(const tq_vegas_state* st, double alpha, void* workspace,
@@ -896,14 +970,11 @@ extern "C" int tq_vegas_smooth_weights(const tq_vegas_state* st, double alpha, v
   return launch_update_map(st, alpha, workspace, workspace_bytes, smoothed, stream);
 }
 
-extern "C" int tq_vegas_get_nh(const tq_vegas_state* st, int64_t nevals_exp, int normalize,
-                               void* workspace, size_t workspace_bytes, void* stream) {
+extern "C" int tq_vegas_get_nh(const tq_vegas_state* st, void* workspace, size_t workspace_bytes,
+                               void* stream) {
   TQ_VEGAS_WS();
-  if (nevals_exp < 0) return TQ_ERR_ARG;
   NhArgs a;
   a.st = *st;
-  a.nevals_exp = nevals_exp;
-  a.normalize = normalize;
   a.block_tot = ws.block_tot;
   a.ticket = ws.t_nh;
   const unsigned g = (unsigned)nh_blocks(st);
@@ -917,14 +988,12 @@ extern "C" int tq_vegas_get_nh(const tq_vegas_state* st, int64_t nevals_exp, int
   return launch_status();
 }
 
-extern "C" int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, int64_t slot,
-                                         void* workspace, size_t workspace_bytes, void* stream) {
+extern "C" int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, void* workspace,
+                                         size_t workspace_bytes, void* stream) {
   TQ_VEGAS_WS();
-  if (slot < 0) return TQ_ERR_ARG;
   FinishArgs a;
   a.st = *st;
   a.beta = beta;
-  a.slot = slot;
   a.partials = ws.partials;
   a.ticket = ws.t_finish;
   const unsigned g = (unsigned)finish_blocks(st);

@@ -41,6 +41,8 @@ class VegasDevice:
         self.stats = torch.zeros((max(1, stats_slots), 4), dtype=torch.float64, device=device)
         self.flags = torch.zeros((4,), dtype=torch.int32, device=device)
         self.scalars = torch.zeros((4,), dtype=torch.float64, device=device)
+        self.control = torch.zeros((8,), dtype=torch.int64, device=device)
+        self.params = torch.zeros((2 + 2 * dim,), dtype=torch.float64, device=device)
         if domain is None:
             domain = torch.tensor([[0.0, 1.0]] * dim, **f)
         self.domain = domain.detach().to(device=device, dtype=dtype).contiguous()
@@ -62,8 +64,9 @@ class VegasDevice:
         s.n_strat = self.n_strat
         s.n_cubes = self.n_cubes
         for name in ("x_edges", "dx_edges", "weights", "counts", "dh", "jf", "jf2", "neval",
-                     "cube_start", "rng_offset", "stats", "flags", "scalars", "domain"):
+                     "cube_start", "rng_offset", "stats", "flags", "scalars", "domain", "control"):
             setattr(s, name, getattr(self, name).data_ptr())
+        s.n_stat_slots = self.stats.shape[0]
 
     def ensure_slots(self, n):
         if n > self.stats.shape[0]:
@@ -71,25 +74,36 @@ class VegasDevice:
             new[: self.stats.shape[0]] = self.stats
             self.stats = new
             self.struct.stats = self.stats.data_ptr()
+            self.struct.n_stat_slots = self.stats.shape[0]
 
     def set_domain(self, domain):
-        self.domain = domain.detach().to(device=self.device, dtype=self.dtype).contiguous()
-        self.struct.domain = self.domain.data_ptr()
+        """Copy a domain into the state's own buffer (its address stays)."""
+        self.domain.copy_(domain.detach().to(device=self.device, dtype=self.dtype))
+
+    def reinit(self):
+        L.check(L.lib().tq_vegas_init(self.ref, L.stream_handle()), "tq_vegas_init")
+        L.count_launches(1)
+
+    def set_control(self, mask, nevals=0, slot=0, normalize=0, seed=0, sid=0):
+        L.check(L.lib().tq_vegas_set_control(self.ref, int(mask), int(nevals), int(slot), int(normalize),
+                                             int(seed) & ((1 << 64) - 1), int(sid) & ((1 << 64) - 1),
+                                             L.stream_handle()), "tq_vegas_set_control")
+        L.count_launches(1)
 
     # ---- thin calls -------------------------------------------------------
     def _ws(self):
         return self.ws.data_ptr(), self.ws.numel()
 
-    def warmup_fused(self, family, params, n_samples, seed, sid):
+    def warmup_fused(self, family, params, n_samples):
         p, n = self._ws()
-        L.check(L.lib().tq_vegas_warmup_fused(self.ref, family, params.data_ptr(), n_samples, seed,
-                                              sid, p, n, L.stream_handle()), "tq_vegas_warmup_fused")
+        L.check(L.lib().tq_vegas_warmup_fused(self.ref, family, params.data_ptr(), n_samples, p, n,
+                                              L.stream_handle()), "tq_vegas_warmup_fused")
         L.count_launches(1)
 
-    def iterate_fused(self, family, params, seed, sid, use_grid_improve, max_points):
+    def iterate_fused(self, family, params, use_grid_improve, max_points=0):
         p, n = self._ws()
-        L.check(L.lib().tq_vegas_iterate_fused(self.ref, family, params.data_ptr(), seed, sid,
-                                               int(bool(use_grid_improve)), max_points, p, n,
+        L.check(L.lib().tq_vegas_iterate_fused(self.ref, family, params.data_ptr(),
+                                               int(bool(use_grid_improve)), int(max_points), p, n,
                                                L.stream_handle()), "tq_vegas_iterate_fused")
         L.count_launches(1)
 
@@ -107,17 +121,26 @@ class VegasDevice:
         L.count_launches(1)
         return out
 
-    def get_nh(self, nevals_exp, normalize):
+    def get_nh(self, nevals_exp=None, normalize=None):
+        """get_NH; nevals_exp / normalize, if given, are written to the
+        control block first (otherwise the device values are used)."""
+        mask = (L.TQ_VC_NEVALS if nevals_exp is not None else 0) | (
+            L.TQ_VC_NORMALIZE if normalize is not None else 0)
+        if mask:
+            self.set_control(mask, nevals=nevals_exp or 0, normalize=int(bool(normalize)))
         p, n = self._ws()
-        L.check(L.lib().tq_vegas_get_nh(self.ref, int(nevals_exp), int(bool(normalize)), p, n,
-                                        L.stream_handle()), "tq_vegas_get_nh")
+        L.check(L.lib().tq_vegas_get_nh(self.ref, p, n, L.stream_handle()), "tq_vegas_get_nh")
         L.count_launches(2)
 
-    def finish(self, beta, slot):
-        self.ensure_slots(slot + 1)
+    def finish(self, beta, slot=None):
+        """finish_iteration into statistics row `slot` (if given, written to
+        the control block first; otherwise the device's running slot)."""
+        if slot is not None:
+            self.ensure_slots(slot + 1)
+            self.set_control(L.TQ_VC_SLOT, slot=slot)
         p, n = self._ws()
-        L.check(L.lib().tq_vegas_finish_iteration(self.ref, float(beta), int(slot), p, n,
-                                                  L.stream_handle()), "tq_vegas_finish_iteration")
+        L.check(L.lib().tq_vegas_finish_iteration(self.ref, float(beta), p, n, L.stream_handle()),
+                "tq_vegas_finish_iteration")
         L.count_launches(1)
 
     def strat_points(self, u):

@@ -33,6 +33,88 @@ ALPHA = 0.5  # vegas.py:220
 BETA = 0.75  # vegas_stratification.py:13
 
 
+class _FusedPlan:
+    """Device state plus captured CUDA graphs for one fused VEGAS shape.
+
+    The warm-up (state reset + five warm-up sampling/map-update pairs) and a
+    block of five stratified iterations (get_NH, fused sampling, finish, map
+    update) read every changing input from the state's control block, so
+    they are captured once and replayed for every later block and call with
+    the same shape.  The first use runs the launches eagerly."""
+
+    _cache = {}
+    _MAX = 8
+
+    def __init__(self, dev, family, use_grid_improve, use_warmup, ns):
+        self.dev, self.family = dev, family
+        self.use_grid_improve, self.use_warmup, self.ns = use_grid_improve, use_warmup, ns
+        self.uses = 0
+        self.g_warm = None
+        self.g_block = None
+
+    @classmethod
+    def get(cls, make_dev, shape_key, family, use_grid_improve, use_warmup, ns, max_iterations):
+        key = (*shape_key, family, bool(use_grid_improve), bool(use_warmup), ns, max_iterations)
+        plan = cls._cache.get(key)
+        if plan is None:
+            plan = cls(make_dev(), family, use_grid_improve, use_warmup, ns)
+            if len(cls._cache) >= cls._MAX:
+                cls._cache.pop(next(iter(cls._cache)))
+            cls._cache[key] = plan
+        return plan
+
+    # launch sequences
+    def _warm_seq(self):
+        d = self.dev
+        d.reinit()
+        if self.use_warmup:
+            for _ in range(5):
+                if self.ns > 0:
+                    d.warmup_fused(self.family, d.params, self.ns)
+                d.update_map(ALPHA)
+
+    def _block_seq(self):
+        d = self.dev
+        for _ in range(5):
+            d.get_nh()
+            d.iterate_fused(self.family, d.params, self.use_grid_improve)
+            d.finish(BETA)
+            if self.use_grid_improve:
+                d.update_map(ALPHA)
+
+    def _capture(self, seq):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            seq()
+        return g
+
+    def run_warmup(self):
+        self.uses += 1
+        if self.g_warm is None and self.uses > 1 and _graphs_enabled():
+            torch.cuda.synchronize()
+            # capture records the launches without running them
+            self.g_warm = self._capture(self._warm_seq)
+            self.g_block = self._capture(self._block_seq)
+        if self.g_warm is not None:
+            self.g_warm.replay()
+            L.count_launches(1 + (5 * (2 if self.ns > 0 else 1) if self.use_warmup else 0))
+        else:
+            self._warm_seq()
+
+    def run_block(self):
+        if self.g_block is not None:
+            self.g_block.replay()
+            L.count_launches(5 * (4 + (1 if self.use_grid_improve else 0)))
+        else:
+            self._block_seq()
+
+
+def _graphs_enabled():
+    import os
+
+    return os.environ.get("TORCHQUAD_GB300_CUDA_GRAPHS", "1") != "0"
+
+
 class VEGAS(BaseIntegrator):
     """VEGAS Enhanced (arXiv:2009.05112) with adaptive map and stratification."""
 
@@ -80,11 +162,6 @@ class VEGAS(BaseIntegrator):
 
         N_intervals = n_intervals if n_intervals is not None else max(2, self._N_increment // 10)
         n_strat = n_strat_for(self._N_increment, dim)
-        self._dev = VegasDevice(dim, self.dtype, N_intervals, n_strat, domain.device, domain,
-                                stats_slots=max(8, max_iterations + 5))
-        self.map = VEGASMap(N_intervals, dim, None, self.dtype, _device_state=self._dev)
-        self.strat = VEGASStratification(self._N_increment, dim, rng, None, self.dtype,
-                                         _device_state=self._dev)
         self.results = []
         self.sigma2 = []
         self.it = 0
@@ -96,46 +173,50 @@ class VEGAS(BaseIntegrator):
             and not (torch.is_grad_enabled() and (domain.requires_grad or fn.requires_grad()))
         )
         if fused:
-            return self._integrate_fused(fn, domain, use_warmup)
+            ns = self._starting_N // 5 if use_warmup else 0
+            plan = _FusedPlan.get(
+                lambda: VegasDevice(dim, self.dtype, N_intervals, n_strat, domain.device, domain,
+                                    stats_slots=max_iterations + 10),
+                (str(domain.device), torch.cuda.current_stream().cuda_stream, dim, self.dtype,
+                 N_intervals, n_strat), fn.family,
+                use_grid_improve, use_warmup, ns, max_iterations)
+            self._dev = plan.dev
+        else:
+            plan = None
+            self._dev = VegasDevice(dim, self.dtype, N_intervals, n_strat, domain.device, domain,
+                                    stats_slots=max(8, max_iterations + 10))
+        self.map = VEGASMap(N_intervals, dim, None, self.dtype, _device_state=self._dev)
+        self.strat = VEGASStratification(self._N_increment, dim, rng, None, self.dtype,
+                                         _device_state=self._dev)
+        if fused:
+            return self._integrate_fused(plan, fn, domain, use_warmup)
         return self._integrate_materialised(domain, use_warmup)
 
     # ------------------------------------------------------------ fused
-    def _integrate_fused(self, fn, domain, use_warmup):
-        dev = self._dev
+    def _integrate_fused(self, plan, fn, domain, use_warmup):
         rng = self.rng
-        params = fn.device_params(domain.device)
+        ns = plan.ns
+        dev = plan.dev
+        dev.set_domain(domain)
+        dev.params.copy_(fn.device_params(domain.device))
         dev.rng_offset.fill_(rng.offset)
+        dev.set_control(L.TQ_VC_NEVALS | L.TQ_VC_SEED | L.TQ_VC_STREAM, nevals=self._starting_N,
+                        seed=rng.seed, sid=rng.stream_id)
         self.alpha = ALPHA
-        warm_evals = 0
-        if use_warmup:
-            ns = self._starting_N // 5
-            for _ in range(5):
-                if ns > 0:
-                    dev.warmup_fused(fn.family, params, ns, rng.seed, rng.stream_id)
-                dev.update_map(self.alpha)
-            warm_evals = 5 * ns
+        plan.run_warmup()
+        warm_evals = 5 * ns if use_warmup else 0
         self._nr_of_fevals = warm_evals
-        normalize = False
-        max_pts = lambda: self._starting_N + self._starting_N // 64 + 2 * dev.n_cubes + 1024  # noqa: E731
         while True:
-            self.it += 1
-            slot = self.it - 1
-            dev.ensure_slots(slot + 1)
-            dev.get_nh(self._starting_N, normalize)
-            dev.iterate_fused(fn.family, params, rng.seed, rng.stream_id, self.use_grid_improve, max_pts())
-            dev.finish(BETA, slot)
-            normalize = True
-            if self.use_grid_improve:
-                dev.update_map(self.alpha)
-            if self.it % 5 == 0:
-                stats = dev.stats[: self.it].cpu()  # one host sync per five iterations
-                self.map.check_flags()
-                first = self.it - 5
-                self.results = [float(v) for v in stats[first : self.it, 0]]
-                self.sigma2 = [float(v) for v in stats[first : self.it, 1]]
-                self._nr_of_fevals = warm_evals + int(stats[: self.it, 2].sum())
-                if self._check_abort_conditions():
-                    break
+            dev.set_control(L.TQ_VC_NEVALS, nevals=self._starting_N)
+            plan.run_block()
+            self.it += 5
+            stats = dev.stats[: self.it].cpu()  # one host sync per five iterations
+            self.map.check_flags()
+            self.results = [float(v) for v in stats[self.it - 5 : self.it, 0]]
+            self.sigma2 = [float(v) for v in stats[self.it - 5 : self.it, 1]]
+            self._nr_of_fevals = warm_evals + int(stats[: self.it, 2].sum())
+            if self._check_abort_conditions():
+                break
         rng.offset = int(dev.rng_offset.item())
         # leave dh normalised, as update_DH does
         s = dev.scalars[0].to(self.dtype)
