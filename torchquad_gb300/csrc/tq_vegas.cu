@@ -230,7 +230,8 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
       __syncthreads();
     }
     int slot = -1;
-    double jfd = 0.0, jf2 = 0.0;
+    using H = typename HistT<T>::type;  // fp32 on the fp32 path
+    H jfd = 0, jf2 = 0;
     if (j < M) {
       uint64_t c = 0;
       if (!WARM) {
@@ -290,11 +291,10 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
       }
       const T f = mul_rn(fam_outer<FAM, T>(fam, s), volume);
       const T jfv = mul_rn(f, jac);
-      jfd = (double)jfv;
+      jfd = (H)jfv;
       jf2 = jfd * jfd;
       if (a.use_map) {
-        using H = typename HistT<T>::type;
-        const H hv = (H)jf2;
+        const H hv = jf2;
 #pragma unroll
         for (int k = 0; k < kMaxDim; ++k) {
           if (k < d) {
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
               atomicAdd(sm.hw + k * B + ids[k], hv);
               atomicAdd(sm.hc + k * B + ids[k], 1u);
             } else {
-              atomicAdd(st.weights + k * B + ids[k], jf2);
+              atomicAdd(st.weights + k * B + ids[k], (double)jf2);
               atomicAdd((unsigned long long*)(st.counts + k * B + ids[k]), 1ull);
             }
           }
@@ -315,8 +315,8 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
       const int lane = threadIdx.x & 31;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const double a1 = __shfl_up_sync(0xffffffffu, jfd, o);
-        const double a2 = __shfl_up_sync(0xffffffffu, jf2, o);
+        const H a1 = __shfl_up_sync(0xffffffffu, jfd, o);
+        const H a2 = __shfl_up_sync(0xffffffffu, jf2, o);
         const int so = __shfl_up_sync(0xffffffffu, slot, o);
         if (lane >= o && so == slot) {
           jfd += a1;
@@ -325,8 +325,8 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
       }
       const int next = __shfl_down_sync(0xffffffffu, slot, 1);
       if (slot >= 0 && (lane == 31 || next != slot)) {
-        atomicAdd(sm.sj + slot, jfd);
-        atomicAdd(sm.sj2 + slot, jf2);
+        atomicAdd(sm.sj + slot, (double)jfd);
+        atomicAdd(sm.sj2 + slot, (double)jf2);
       }
     }
     if (!WARM) {
@@ -410,14 +410,36 @@ __global__ void __launch_bounds__(kBlock) vegas_nh_kernel(NhArgs a) {
   if (c < st.n_cubes) st.cube_start[c] = excl;
   if (threadIdx.x == 0) a.block_tot[blockIdx.x] = warp_tot[kBlock / 32 - 1];
   if (last_block_arrives(a.ticket)) {
-    if (threadIdx.x == 0) {
-      int64_t run = 0;
-      for (unsigned b = 0; b < gridDim.x; ++b) {
-        const int64_t t = a.block_tot[b];
-        a.block_tot[b] = run;
-        run += t;
+    // exclusive scan of the block totals, kBlock at a time
+    int64_t carry = 0;
+    for (unsigned base = 0; base < gridDim.x; base += kBlock) {
+      const unsigned b = base + threadIdx.x;
+      const int64_t t = b < gridDim.x ? a.block_tot[b] : 0;
+      int64_t x = t;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t v = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += v;
       }
-      st.cube_start[st.n_cubes] = run;
+      __syncthreads();
+      if (lane == 31) warp_tot[warp] = x;
+      __syncthreads();
+      if (warp == 0) {
+        int64_t w = lane < kBlock / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int64_t v = __shfl_up_sync(0xffffffffu, w, o);
+          if (lane >= o) w += v;
+        }
+        if (lane < kBlock / 32) warp_tot[lane] = w;
+      }
+      __syncthreads();
+      const int64_t ex = carry + x - t + (warp > 0 ? warp_tot[warp - 1] : 0);
+      if (b < gridDim.x) a.block_tot[b] = ex;
+      carry += warp_tot[kBlock / 32 - 1];
+    }
+    if (threadIdx.x == 0) {
+      st.cube_start[st.n_cubes] = carry;
       st.control[2] = 0;
       *a.ticket = 0u;
     }
@@ -434,6 +456,7 @@ __global__ void __launch_bounds__(kBlock) vegas_nh_fixup_kernel(tq_vegas_state s
 struct FinishArgs {
   tq_vegas_state st;
   double beta;
+  double V;       // V_cubes = (1/n_strat)^dim, computed on the host
   Acc* partials;  // [blocks][3]
   unsigned* ticket;
 };
@@ -442,7 +465,8 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
   const tq_vegas_state& st = a.st;
   const int d = st.dim;
-  const double V = pow(1.0 / (double)st.n_strat, (double)d);  // V_cubes (:29)
+  (void)d;
+  const double V = a.V;  // V_cubes (vegas_stratification.py:29)
   const T Vt = (T)V, V2t = (T)(V * V);
   Acc res{0, 0}, s2{0, 0}, dsum{0, 0};
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < st.n_cubes;
@@ -503,14 +527,25 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
 // --------------------------------------------------------- map update
 // One CTA updates every dimension: the "all weights zero" test of
 // vegas_map.py:151-155 spans the whole map.
+// Bytes of the map-update working arrays (placed in shared memory when they
+// fit, else in the workspace).
+__host__ __device__ inline size_t map_work_bytes(int d, int64_t B, size_t tsize) {
+  const size_t DB = (size_t)d * B, DB1 = (size_t)d * (B + 1);
+  size_t off = 2 * DB * tsize + 2 * DB;
+  off = (off + 15) & ~size_t(15);
+  return off + DB1 * (8 + 8 + tsize) + 16;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state st, double alpha,
-                                                                  double* scratch,
+                                                                  double* scratch, int in_smem,
                                                                   void* smooth_out) {
+  extern __shared__ __align__(16) unsigned char map_smem[];
   const int d = st.dim;
   const int64_t B = st.n_bins;
   const int64_t DB = d * B;
-  T* w = (T*)scratch;                 // [d][B] averaged weights, then smoothed
+  unsigned char* base = in_smem ? map_smem : (unsigned char*)scratch;
+  T* w = (T*)base;                    // [d][B] averaged weights, then smoothed
   T* wtmp = w + DB;                   // [d][B]
   unsigned char* z = (unsigned char*)(wtmp + DB);        // [d][B] zero-count flags
   unsigned char* ztmp = z + DB;                          // [d][B]
@@ -818,8 +853,7 @@ static int64_t finish_blocks(const tq_vegas_state* st) {
   return need < cap ? need : cap;
 }
 static size_t map_scratch_bytes(const tq_vegas_state* st) {
-  const size_t DB = (size_t)st->dim * st->n_bins, DB1 = (size_t)st->dim * (st->n_bins + 1);
-  return 2 * DB * 8 + 2 * DB + 16 + DB1 * (8 + 8 + 8);
+  return map_work_bytes(st->dim, st->n_bins, 8);
 }
 
 // Workspace: [0,256) tickets; then nh block totals, finish partials and the
@@ -952,10 +986,24 @@ extern "C" int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, cons
 static int launch_update_map(const tq_vegas_state* st, double alpha, void* workspace,
                              size_t workspace_bytes, void* smooth_out, void* stream) {
   TQ_VEGAS_WS();
+  const size_t bytes = map_work_bytes(st->dim, st->n_bins, dtype_size(st->dtype));
+  const int in_smem = bytes <= 160 * 1024;
+  const size_t smem = in_smem ? bytes : 0;
+#define TQ_MAP_LAUNCH(T)                                                                      \
+  {                                                                                           \
+    auto kfn = vegas_update_map_kernel<T>;                                                    \
+    if (smem > 48 * 1024) {                                                                   \
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                           (int)smem);                                        \
+      if (e != cudaSuccess) return set_cuda_error(e);                                         \
+    }                                                                                         \
+    kfn<<<1, kBlock, smem, s>>>(*st, alpha, ws.map_scratch, in_smem, smooth_out);             \
+  }
   if (st->dtype == TQ_F64)
-    vegas_update_map_kernel<double><<<1, kBlock, 0, s>>>(*st, alpha, ws.map_scratch, smooth_out);
+    TQ_MAP_LAUNCH(double)
   else
-    vegas_update_map_kernel<float><<<1, kBlock, 0, s>>>(*st, alpha, ws.map_scratch, smooth_out);
+    TQ_MAP_LAUNCH(float)
+#undef TQ_MAP_LAUNCH
   return launch_status();
 }
 
@@ -994,6 +1042,7 @@ extern "C" int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, 
   FinishArgs a;
   a.st = *st;
   a.beta = beta;
+  a.V = pow(1.0 / (double)st->n_strat, (double)st->dim);
   a.partials = ws.partials;
   a.ticket = ws.t_finish;
   const unsigned g = (unsigned)finish_blocks(st);

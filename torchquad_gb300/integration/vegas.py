@@ -95,18 +95,23 @@ class _FusedPlan:
             # capture records the launches without running them
             self.g_warm = self._capture(self._warm_seq)
             self.g_block = self._capture(self._block_seq)
-        if self.g_warm is not None:
+        if self.g_warm is not None and not FORCE_EAGER[0]:
             self.g_warm.replay()
             L.count_launches(1 + (5 * (2 if self.ns > 0 else 1) if self.use_warmup else 0))
         else:
             self._warm_seq()
 
     def run_block(self):
-        if self.g_block is not None:
+        if self.g_block is not None and not FORCE_EAGER[0]:
             self.g_block.replay()
             L.count_launches(5 * (4 + (1 if self.use_grid_improve else 0)))
         else:
             self._block_seq()
+
+
+# Set [True] to run the captured sequences as individual launches (for
+# per-kernel instrumentation); graphs stay captured.
+FORCE_EAGER = [False]
 
 
 def _graphs_enabled():
