@@ -6,12 +6,14 @@
 // map), vegas_stratification.py (stratified sampling).  The reference
 // materialises y, x, f and jac for every point and scatter-adds them into
 // the map and the cubes with global atomics (utils.py:61-76).  Here one
-// kernel does a whole iteration: points of a 256-point tile are generated
-// in registers, the map histogram is privatised in shared memory per CTA and
-// flushed once, and per-cube sums use the cube-contiguous point order
-// (repeat_interleave order of vegas_stratification.py:154): a tile spans at
-// most 130 cubes because every cube has >= 2 points, so they get shared
-// memory slots and one flush per tile.
+// kernel does a whole iteration: each warp takes 32 consecutive points,
+// generates them in registers, adds to a warp-private map histogram in
+// shared memory (lanes hitting the same interval are combined first, so the
+// adds are plain and their order fixed), and reduces the per-cube sums with
+// a segmented scan over the cube-contiguous point order (repeat_interleave
+// order of vegas_stratification.py:154; a warp spans at most 17 cubes
+// because every cube has >= 2 points) into one global add per cube segment.
+// The histograms are flushed once per CTA.
 //
 // The arithmetic that decides interval indices and points (y, ID, offset,
 // x, jac) is written with explicitly rounded operations in the state's
@@ -22,8 +24,7 @@
 
 namespace tq {
 
-constexpr int kTile = 256;                  // points per tile = threads per CTA
-constexpr int kCubeSlots = kTile / 2 + 2;   // cubes a tile can touch
+constexpr int kTile = 256;  // threads per CTA of the sampler
 
 // ---- explicitly rounded arithmetic (no FMA contraction)
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
@@ -117,16 +118,26 @@ struct HistT<float> {
   using type = float;
 };
 
+// Shared memory of the sampler: the map (edges) when it fits, and one
+// private histogram per warp (weights in HistT, counts in u32) when it fits.
 template <typename T>
 struct Smem {
   T* xe;
   T* dxe;
-  typename HistT<T>::type* hw;
-  unsigned* hc;
-  double* sj;
-  double* sj2;
-  int64_t* cs;
+  typename HistT<T>::type* hw;  // [warps][d*B]
+  unsigned* hc;                 // [warps][d*B]
 };
+
+constexpr int kWarps = kTile / 32;
+
+__host__ __device__ inline size_t sample_smem_bytes(int d, int64_t B, size_t tsize, bool hist,
+                                                    bool edges) {
+  size_t off = 0;
+  if (edges) off += tsize * (d * (B + 1) + d * B);
+  off = (off + 15) & ~size_t(15);
+  if (hist) off += (size_t)kWarps * d * B * (sizeof(double) + sizeof(unsigned));
+  return off;
+}
 
 template <typename T>
 __device__ Smem<T> carve(unsigned char* base, const SampleArgs& a) {
@@ -134,18 +145,6 @@ __device__ Smem<T> carve(unsigned char* base, const SampleArgs& a) {
   const int d = a.st.dim;
   const int64_t B = a.st.n_bins;
   size_t off = 0;
-  s.sj = (double*)(base + off);
-  off += sizeof(double) * kCubeSlots;
-  s.sj2 = (double*)(base + off);
-  off += sizeof(double) * kCubeSlots;
-  s.cs = (int64_t*)(base + off);
-  off += sizeof(int64_t) * (kCubeSlots + 1);
-  if (a.hist_smem) {
-    s.hw = (typename HistT<T>::type*)(base + off);
-    off += sizeof(double) * d * B;
-  } else {
-    s.hw = nullptr;
-  }
   if (a.edges_smem) {
     s.xe = (T*)(base + off);
     off += sizeof(T) * d * (B + 1);
@@ -155,31 +154,53 @@ __device__ Smem<T> carve(unsigned char* base, const SampleArgs& a) {
     s.xe = (T*)a.st.x_edges;
     s.dxe = (T*)a.st.dx_edges;
   }
-  off = (off + 7) & ~size_t(7);
-  s.hc = a.hist_smem ? (unsigned*)(base + off) : nullptr;
+  off = (off + 15) & ~size_t(15);
+  if (a.hist_smem) {
+    s.hw = (typename HistT<T>::type*)(base + off);
+    off += (size_t)kWarps * d * B * sizeof(double);
+    s.hc = (unsigned*)(base + off);
+  } else {
+    s.hw = nullptr;
+    s.hc = nullptr;
+  }
   return s;
 }
 
-__host__ __device__ inline size_t sample_smem_bytes(int d, int64_t B, size_t tsize, bool hist,
-                                                    bool edges) {
-  size_t off = sizeof(double) * 2 * kCubeSlots + sizeof(int64_t) * (kCubeSlots + 1);
-  if (hist) off += sizeof(double) * d * B;
-  if (edges) off += tsize * (d * (B + 1) + d * B);
-  off = (off + 7) & ~size_t(7);
-  if (hist) off += sizeof(unsigned) * d * B;
-  return off;
+// Warp-aggregated histogram update: lanes with the same key form a group;
+// every member sums the group's values in lane order and the lowest lane
+// adds the sum (and the group size) to the warp-private bins.
+template <typename H>
+__device__ __forceinline__ void warp_hist_add(H* hw, unsigned* hc, int key, bool valid, H v) {
+  const int lane = threadIdx.x & 31;
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  H sum = v;
+  unsigned rest = grp & ~(1u << lane);
+  while (__any_sync(0xffffffffu, rest != 0u)) {
+    const int src = rest ? __ffs(rest) - 1 : lane;
+    const H x = __shfl_sync(0xffffffffu, v, src);
+    if (rest) {
+      sum += x;
+      rest &= rest - 1u;
+    }
+  }
+  if (valid && lane == __ffs(grp) - 1) {
+    hw[key] += sum;
+    hc[key] += (unsigned)__popc(grp);
+  }
 }
 
 template <typename T, int FAM, bool WARM>
-__global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
+__global__ void __launch_bounds__(kTile, 3) vegas_sample_kernel(SampleArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Family<T> fam;
   __shared__ T lo[kMaxDim], wid[kMaxDim];
   __shared__ T volume;
-  __shared__ int64_t tile_c0, tile_c1;
+  using H = typename HistT<T>::type;  // fp32 on the fp32 path
   const tq_vegas_state& st = a.st;
   const int d = st.dim;
   const int64_t B = st.n_bins;
+  const int64_t DB = d * B;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   Smem<T> sm = carve<T>(smem_raw, a);
   if (threadIdx.x == 0) {
     load_family<T>(fam, a.family, d, a.params);
@@ -194,15 +215,17 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
   }
   if (a.edges_smem) {
     for (int64_t i = threadIdx.x; i < d * (B + 1); i += blockDim.x) sm.xe[i] = ((const T*)st.x_edges)[i];
-    for (int64_t i = threadIdx.x; i < d * B; i += blockDim.x) sm.dxe[i] = ((const T*)st.dx_edges)[i];
+    for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) sm.dxe[i] = ((const T*)st.dx_edges)[i];
   }
   if (a.hist_smem) {
-    for (int64_t i = threadIdx.x; i < d * B; i += blockDim.x) {
+    for (int64_t i = threadIdx.x; i < (int64_t)kWarps * DB; i += blockDim.x) {
       sm.hw[i] = 0;
       sm.hc[i] = 0u;
     }
   }
   __syncthreads();
+  H* whw = a.hist_smem ? sm.hw + warp * DB : nullptr;
+  unsigned* whc = a.hist_smem ? sm.hc + warp * DB : nullptr;
 
   const int64_t M = WARM ? a.n_samples : st.cube_start[st.n_cubes];
   const uint64_t offset = *st.rng_offset;
@@ -210,40 +233,33 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
   const int64_t ns = st.n_strat;
   constexpr int PB = Uniform<T>::per_block;
 
-  for (int64_t tile = blockIdx.x; tile * kTile < M; tile += gridDim.x) {
-    const int64_t j0 = tile * kTile;
-    const int64_t j = j0 + threadIdx.x;
-    int nc = 0;
-    if (!WARM) {
-      const int warp = threadIdx.x >> 5;
-      if (warp == 0) {
-        const int64_t c = warp_find_cube(st.cube_start, st.n_cubes, j0);
-        if ((threadIdx.x & 31) == 0) tile_c0 = c;
-      } else if (warp == 1) {
-        const int64_t c = warp_find_cube(st.cube_start, st.n_cubes, min(M, j0 + kTile) - 1);
-        if ((threadIdx.x & 31) == 0) tile_c1 = c;
-      }
-      __syncthreads();
-      nc = (int)(tile_c1 - tile_c0 + 1);
-      for (int i = threadIdx.x; i <= nc; i += blockDim.x) sm.cs[i] = st.cube_start[tile_c0 + i];
-      for (int i = threadIdx.x; i < nc; i += blockDim.x) sm.sj[i] = sm.sj2[i] = 0.0;
-      __syncthreads();
-    }
+  // Warp tiles of 32 consecutive points; every cube has >= 2 points, so a
+  // tile spans at most 17 cubes.
+  for (int64_t wt = (int64_t)blockIdx.x * kWarps + warp; wt * 32 < M;
+       wt += (int64_t)gridDim.x * kWarps) {
+    const int64_t j0 = wt * 32;
+    const int64_t j = j0 + lane;
+    const bool valid = j < M;
     int slot = -1;
-    using H = typename HistT<T>::type;  // fp32 on the fp32 path
-    H jfd = 0, jf2 = 0;
-    if (j < M) {
-      uint64_t c = 0;
-      if (!WARM) {
-        int l = 0, h = nc;  // largest l with cs[l] <= j
-        while (h - l > 1) {
-          const int mid = (l + h) >> 1;
-          if (sm.cs[mid] <= j) l = mid;
-          else h = mid;
-        }
-        slot = l;
-        c = (uint64_t)(tile_c0 + l);
+    int64_t c0 = 0;
+    if (!WARM) {
+      c0 = warp_find_cube(st.cube_start, st.n_cubes, j0);
+      const int64_t cl = c0 + lane;
+      const int64_t csl = cl <= st.n_cubes ? st.cube_start[cl] : INT64_MAX;
+      int l = 0;  // largest l with cube_start[c0 + l] <= j
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = l + step;
+        const int64_t v = __shfl_sync(0xffffffffu, csl, cand & 31);
+        if (cand < 32 && v <= j) l = cand;
       }
+      slot = valid ? l : -1;
+    }
+    H jfd = 0, jf2 = 0;
+    int ids[kMaxDim];
+    if (valid) {
+      uint32_t c32 = (uint32_t)(c0 + slot);
+      uint64_t c = (uint64_t)(c0 + slot);
       // Philox block of this point's first draw; later draws follow
       const uint64_t e0 = (uint64_t)j * (uint64_t)d;
       const uint64_t blk0 = offset + e0 / PB;
@@ -252,8 +268,6 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
       uint4 r = make_uint4(0, 0, 0, 0);
       T jac = (T)1;
       T s = T(0);
-      int ids[kMaxDim];
-      uint32_t c32 = (uint32_t)c;
 #pragma unroll
       for (int k = 0; k < kMaxDim; ++k) {
         if (k < d) {
@@ -293,26 +307,24 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
       const T jfv = mul_rn(f, jac);
       jfd = (H)jfv;
       jf2 = jfd * jfd;
-      if (a.use_map) {
-        const H hv = jf2;
+    }
+    if (a.use_map) {
 #pragma unroll
-        for (int k = 0; k < kMaxDim; ++k) {
-          if (k < d) {
-            if (a.hist_smem) {
-              atomicAdd(sm.hw + k * B + ids[k], hv);
-              atomicAdd(sm.hc + k * B + ids[k], 1u);
-            } else {
-              atomicAdd(st.weights + k * B + ids[k], (double)jf2);
-              atomicAdd((unsigned long long*)(st.counts + k * B + ids[k]), 1ull);
-            }
+      for (int k = 0; k < kMaxDim; ++k) {
+        if (k < d) {
+          if (a.hist_smem) {
+            const int key = valid ? (int)(k * B) + ids[k] : -1 - lane;
+            warp_hist_add<H>(whw, whc, key, valid, jf2);
+          } else if (valid) {
+            atomicAdd(st.weights + k * B + ids[k], (double)jf2);
+            atomicAdd((unsigned long long*)(st.counts + k * B + ids[k]), 1ull);
           }
         }
       }
     }
     if (!WARM) {
-      // Points are in cube order: segmented inclusive scan over the warp,
-      // then one shared-memory add per cube segment.
-      const int lane = threadIdx.x & 31;
+      // points are in cube order: segmented inclusive scan over the warp,
+      // then one global add per cube segment
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const H a1 = __shfl_up_sync(0xffffffffu, jfd, o);
@@ -325,25 +337,24 @@ __global__ void __launch_bounds__(kTile) vegas_sample_kernel(SampleArgs a) {
       }
       const int next = __shfl_down_sync(0xffffffffu, slot, 1);
       if (slot >= 0 && (lane == 31 || next != slot)) {
-        atomicAdd(sm.sj + slot, (double)jfd);
-        atomicAdd(sm.sj2 + slot, (double)jf2);
+        atomicAdd(st.jf + c0 + slot, (double)jfd);
+        atomicAdd(st.jf2 + c0 + slot, (double)jf2);
       }
-    }
-    if (!WARM) {
-      __syncthreads();
-      for (int i = threadIdx.x; i < nc; i += blockDim.x) {
-        atomicAdd(st.jf + tile_c0 + i, sm.sj[i]);
-        atomicAdd(st.jf2 + tile_c0 + i, sm.sj2[i]);
-      }
-      __syncthreads();
     }
   }
   if (a.hist_smem && a.use_map) {
     __syncthreads();
-    for (int64_t i = threadIdx.x; i < d * B; i += blockDim.x) {
-      if (sm.hc[i]) {
-        atomicAdd(st.weights + i, (double)sm.hw[i]);
-        atomicAdd((unsigned long long*)(st.counts + i), (unsigned long long)sm.hc[i]);
+    for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
+      unsigned cnt = 0;
+      double w = 0.0;
+#pragma unroll
+      for (int q = 0; q < kWarps; ++q) {
+        cnt += sm.hc[q * DB + i];
+        w += (double)sm.hw[q * DB + i];
+      }
+      if (cnt) {
+        atomicAdd(st.weights + i, w);
+        atomicAdd((unsigned long long*)(st.counts + i), (unsigned long long)cnt);
       }
     }
   }
@@ -461,56 +472,70 @@ struct FinishArgs {
   unsigned* ticket;
 };
 
+// Plain fp64 tree sum over the CTA (pairwise: error O(log n) ulp); the
+// compensated sum is taken across CTAs by the last one.
+__device__ __forceinline__ double block_sum_plain(double v, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  return t;  // valid in thread 0
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
+  __shared__ double sh[kBlock / 32];
   const tq_vegas_state& st = a.st;
-  const int d = st.dim;
-  (void)d;
   const double V = a.V;  // V_cubes (vegas_stratification.py:29)
   const T Vt = (T)V, V2t = (T)(V * V);
-  Acc res{0, 0}, s2{0, 0}, dsum{0, 0};
+  const T beta = (T)a.beta;
+  double res = 0.0, s2 = 0.0, dsum = 0.0;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < st.n_cubes;
        c += (int64_t)gridDim.x * blockDim.x) {
-    const double n = (double)st.neval[c];
+    const int64_t nn = st.neval[c];
     const double J = st.jf[c], J2 = st.jf2[c];
-    const double inv = 1.0 / n;
-    const double ih = J * (inv * V);                     // vegas.py:294
-    const double sig2 = fabs(J2 * inv * (V * V) - ih * ih);  // :297-301
-    acc_add(res, ih);
-    acc_add(s2, sig2 * inv);
+    const double inv = 1.0 / (double)nn;
+    const double ih = J * (inv * V);                           // vegas.py:294
+    res += ih;
+    s2 += fabs(J2 * inv * (V * V) - ih * ih) * inv;            // :297-303
     // update_DH (vegas_stratification.py:72-86) in the state's dtype
-    const T cnt = (T)n, jT = (T)J, j2T = (T)J2;
+    const T cnt = (T)nn, jT = (T)J, j2T = (T)J2;
     const T q = div_rn(mul_rn(Vt, jT), cnt);
     T dt = sub_rn(div_rn(mul_rn(V2t, j2T), cnt), mul_rn(q, q));
     if (dt < (T)0) dt = (T)0;
-    const T dh = pow(dt, (T)a.beta);
+    const T dh = (a.beta == 0.75) ? pow(dt, (T)0.75) : pow(dt, beta);
     ((T*)st.dh)[c] = dh;
-    acc_add(dsum, (double)dh);
+    dsum += (double)dh;
   }
-  res = block_reduce<kBlock>(res);
-  s2 = block_reduce<kBlock>(s2);
-  dsum = block_reduce<kBlock>(dsum);
+  res = block_sum_plain(res, sh);
+  s2 = block_sum_plain(s2, sh);
+  dsum = block_sum_plain(dsum, sh);
   if (threadIdx.x == 0) {
-    a.partials[3 * blockIdx.x] = res;
-    a.partials[3 * blockIdx.x + 1] = s2;
-    a.partials[3 * blockIdx.x + 2] = dsum;
+    a.partials[3 * blockIdx.x] = Acc{res, 0.0};
+    a.partials[3 * blockIdx.x + 1] = Acc{s2, 0.0};
+    a.partials[3 * blockIdx.x + 2] = Acc{dsum, 0.0};
   }
   if (last_block_arrives(a.ticket)) {
-    Acc r{0, 0}, s{0, 0}, ds{0, 0};
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-      acc_merge(r, a.partials[3 * i]);
-      acc_merge(s, a.partials[3 * i + 1]);
-      acc_merge(ds, a.partials[3 * i + 2]);
-    }
-    r = block_reduce<kBlock>(r);
-    s = block_reduce<kBlock>(s);
-    ds = block_reduce<kBlock>(ds);
     if (threadIdx.x == 0) {
+      Acc r{0, 0}, q{0, 0}, ds{0, 0};
+      for (unsigned i = 0; i < gridDim.x; ++i) {  // index order: deterministic
+        acc_add(r, a.partials[3 * i].s);
+        acc_add(q, a.partials[3 * i + 1].s);
+        acc_add(ds, a.partials[3 * i + 2].s);
+      }
       const int64_t slot = st.control[1];
       if (slot >= 0 && slot < st.n_stat_slots) {
         double* out = st.stats + 4 * slot;
         out[0] = r.s + r.c;
-        out[1] = s.s + s.c;
+        out[1] = q.s + q.c;
         out[2] = (double)st.cube_start[st.n_cubes];
       } else {
         st.flags[3] = 1;
@@ -587,29 +612,18 @@ __global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state
         break;
     }
   }
-  // row sums (:151)
-  if (threadIdx.x < d) {
-    double acc = 0.0;
-    for (int64_t b = 0; b < B; ++b) acc += (double)w[threadIdx.x * B + b];
-    sums[threadIdx.x] = (T)acc;
+  // row sums (:151): one warp per dimension
+  {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = warp; k < d; k += blockDim.x >> 5) {
+      double acc = 0.0;
+      for (int64_t b = lane; b < B; b += 32) acc += (double)w[k * B + b];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if (lane == 0) sums[k] = (T)acc;
+    }
   }
   __syncthreads();
-  int zero_row = 0;
-  for (int k = threadIdx.x; k < d; k += blockDim.x) zero_row |= sums[k] == (T)0;
-  if (__syncthreads_or(zero_row)) {
-    // The map cannot be updated (:152-155, :187-196): reset and flag.
-    if (smooth_out) {
-      if (threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
-      return;
-    }
-    for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
-      st.weights[i] = 0.0;
-      st.counts[i] = 0;
-    }
-    if (threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
-    return;
-  }
-
   // EQ 18: [1,6,1]/8 smoothing with repeated borders, normalised; EQ 19
   for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
     const int64_t k = i / B, b = i - k * B;
@@ -631,47 +645,83 @@ __global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state
   }
   __syncthreads();
   if (smooth_out) return;  // _smooth_map only: the map and its weights stay as they are
-  // EQ 20-22 per dimension, sequentially as the reference's cumsums run
-  if (threadIdx.x < d) {
+  // EQ 20-22.  The reference's cumulative sums run sequentially; here only
+  // the additions do (one thread per dimension), the divisions and the edge
+  // formula run in parallel.
+  double* cumd = newx;          // [d][B+1]: fp64 cumulative sums, later new edges
+  int32_t* mult = (int32_t*)w;  // [d][B]: delta multiples, later edge indices
+  {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = warp; k < d; k += blockDim.x >> 5) {  // :201 delta per dimension
+      double acc = 0.0;
+      for (int64_t b = lane; b < B; b += 32) acc += (double)wtmp[k * B + b];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if (lane == 0) deltas[k] = div_rn((T)acc, (T)B);
+    }
+  }
+  if (threadIdx.x < d) {  // :210-213 fp64 cumsum of sw[:-1]
+    const int k = threadIdx.x;
+    double cum = 0.0;
+    for (int64_t b = 0; b < B - 1; ++b) {
+      cum += (double)wtmp[k * B + b];
+      cumd[k * (B + 1) + b] = cum;
+    }
+  }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < d * (B - 1); i += blockDim.x) {
+    const int64_t k = i / (B - 1), b = i - k * (B - 1);
+    int64_t m = (int64_t)(cumd[k * (B + 1) + b] / (double)deltas[k]);
+    m = m < 0 ? 0 : (m > B ? B : m);
+    mult[k * B + b] = (int32_t)m;
+  }
+  __syncthreads();
+  if (threadIdx.x < d) {  // :214-233 counts/sums per multiple, then prefixes
     const int k = threadIdx.x;
     const T* sw = wtmp + k * B;
-    const T* xe = (const T*)st.x_edges + k * (B + 1);
-    const T* dxe = (const T*)st.dx_edges + k * B;
-    double tot = 0.0;
-    for (int64_t b = 0; b < B; ++b) tot += (double)sw[b];
-    const T delta = div_rn((T)tot, (T)B);  // :201
-    deltas[k] = delta;
+    const T delta = deltas[k];
     int64_t* num = idx + k * (B + 1);
     T* vv = val + k * (B + 1);
     for (int64_t m = 0; m <= B; ++m) {
       num[m] = 0;
       vv[m] = (T)0;
     }
-    // :210-226: multiples of delta in the fp64 cumulative sum
-    double cum = 0.0;
     for (int64_t b = 0; b < B - 1; ++b) {
-      cum += (double)sw[b];
-      int64_t m = (int64_t)(cum / (double)delta);
-      m = m < 0 ? 0 : (m > B ? B : m);
+      const int m = mult[k * B + b];
       num[m] += 1;
       vv[m] = add_rn(vv[m], sw[b]);
     }
-    // :230-239: new inner edges
     int64_t ind = 0;
     double daccu = 0.0;  // cumsum of (delta - val) accumulated in fp64, rounded per step
-    double* nx = newx + k * (B + 1);
-    nx[0] = (double)xe[0];
-    nx[B] = (double)xe[B];
     for (int64_t e = 0; e < B - 1; ++e) {
       ind += num[e];
       daccu += (double)sub_rn(delta, vv[e]);
-      const int64_t ii = ind < 0 ? 0 : (ind > B - 1 ? B - 1 : ind);
-      const T da = (T)daccu;
-      const T ne = add_rn(xe[ii], mul_rn(div_rn(da, sw[ii]), dxe[ii]));
-      nx[e + 1] = (double)ne;
+      mult[k * B + e] = (int32_t)(ind < 0 ? 0 : (ind > B - 1 ? B - 1 : ind));
+      vv[e] = (T)daccu;
     }
+  }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < d * (B + 1); i += blockDim.x) {  // EQ 22
+    const int64_t k = i / (B + 1), e1 = i - k * (B + 1);
+    const T* xe = (const T*)st.x_edges + k * (B + 1);
+    double nv;
+    if (e1 == 0 || e1 == B) {
+      nv = (double)xe[e1];
+    } else {
+      const int ii = mult[k * B + e1 - 1];
+      const T* sw = wtmp + k * B;
+      const T* dxe = (const T*)st.dx_edges + k * B;
+      nv = (double)add_rn(xe[ii], mul_rn(div_rn(val[k * (B + 1) + e1 - 1], sw[ii]), dxe[ii]));
+    }
+    newx[i] = nv;  // cumd is no longer needed
+  }
+  __syncthreads();
+  if (threadIdx.x < d) {
     // :240-257: replace infinite edges by the mean of their (unrepaired)
-    // neighbours; vv (no longer needed) holds the means
+    // neighbours; val (no longer needed) holds the means
+    const int k = threadIdx.x;
+    double* nx = newx + k * (B + 1);
+    T* vv = val + k * (B + 1);
     bool bad = false;
     for (int64_t e = 1; e < B; ++e) bad |= !isfinite(nx[e]);
     if (bad) {
@@ -849,7 +899,7 @@ static int check_state(const tq_vegas_state* st) {
 static int64_t nh_blocks(const tq_vegas_state* st) { return (st->n_cubes + kBlock - 1) / kBlock; }
 static int64_t finish_blocks(const tq_vegas_state* st) {
   const int64_t need = (st->n_cubes + kBlock - 1) / kBlock;
-  const int64_t cap = (int64_t)sm_count() * 4;
+  const int64_t cap = (int64_t)sm_count() * 2;
   return need < cap ? need : cap;
 }
 static size_t map_scratch_bytes(const tq_vegas_state* st) {
@@ -926,7 +976,8 @@ static int launch_sample(const tq_vegas_state* st, int family, const double* par
   a.ns_div = make_fastdiv((uint32_t)(a.small_cubes ? st->n_strat : 1));
   const size_t tsize = dtype_size(st->dtype);
   const size_t limit = 96 * 1024;
-  a.hist_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, true, false) <= limit / 2;
+  a.hist_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, true, false) <= limit / 2 &&
+                st->dim * st->n_bins < (int64_t(1) << 30);
   a.edges_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, true) <= limit;
   const size_t smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, a.edges_smem);
   const int64_t cap = (int64_t)sm_count() * 8;
