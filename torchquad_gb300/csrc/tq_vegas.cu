@@ -46,13 +46,12 @@ __device__ __forceinline__ T warm_scale() {
 // Jacobian factor B * dx_edges[ID] (:73).
 template <typename T>
 __device__ __forceinline__ int map_coord(const T* __restrict__ xe, const T* __restrict__ dxe,
-                                         int64_t B, T y, T& x, T& jac_factor) {
-  const T Bf = (T)B;
+                                         int B, T Bf, T y, T& x, T& jac_factor) {
   const T yB = mul_rn(y, Bf);
   const T fl = floor(yB);
   int id = (int)fl;
   // y < 1 keeps id <= B-1; the clamp only guards memory for pathological B
-  id = id < 0 ? 0 : (id >= (int)B ? (int)B - 1 : id);
+  id = id < 0 ? 0 : (id >= B ? B - 1 : id);
   const T off = sub_rn(yB, fl);
   x = add_rn(xe[id], mul_rn(dxe[id], off));
   jac_factor = mul_rn(Bf, dxe[id]);
@@ -67,9 +66,10 @@ __device__ __forceinline__ int64_t cube_digit(int64_t c, int64_t n_strat, int k)
 }
 
 // y = (pos + u) / n_strat, values >= 1 replaced by 0.999999 (:159-165).
+// pos < n_strat < 2^31: 32-bit conversion.
 template <typename T>
-__device__ __forceinline__ T strat_y(int64_t pos, T u, int64_t n_strat) {
-  T y = div_rn(add_rn((T)pos, u), (T)n_strat);
+__device__ __forceinline__ T strat_y(int pos, T u, T nsf) {
+  T y = div_rn(add_rn((T)pos, u), nsf);
   return y >= (T)1 ? warm_scale<T>() : y;
 }
 
@@ -231,6 +231,9 @@ __global__ void __launch_bounds__(kTile, 3) vegas_sample_kernel(SampleArgs a) {
   const uint64_t offset = *st.rng_offset;
   const uint64_t seed = (uint64_t)st.control[3], sid = (uint64_t)st.control[4];
   const int64_t ns = st.n_strat;
+  const T nsf = (T)ns;
+  const int Bi = (int)B;
+  const T Bf = (T)Bi;
   constexpr int PB = Uniform<T>::per_block;
 
   // Warp tiles of 32 consecutive points; every cube has >= 2 points, so a
@@ -282,20 +285,20 @@ __global__ void __launch_bounds__(kTile, 3) vegas_sample_kernel(SampleArgs a) {
           if (WARM) {
             y = mul_rn(u, warm_scale<T>());
           } else {
-            int64_t pos;
+            int pos;
             if (a.small_cubes) {
               const uint32_t q = fdiv(c32, a.ns_div);
-              pos = (int64_t)(c32 - q * a.ns_div.d);
+              pos = (int)(c32 - q * a.ns_div.d);
               c32 = q;
             } else {
               const uint64_t q = c / (uint64_t)ns;
-              pos = (int64_t)(c - q * (uint64_t)ns);
+              pos = (int)(c - q * (uint64_t)ns);
               c = q;
             }
-            y = strat_y<T>(pos, u, ns);
+            y = strat_y<T>(pos, u, nsf);
           }
           T x, jf_k;
-          ids[k] = map_coord<T>(sm.xe + k * (B + 1), sm.dxe + k * B, B, y, x, jf_k);
+          ids[k] = map_coord<T>(sm.xe + k * (Bi + 1), sm.dxe + k * Bi, Bi, Bf, y, x, jf_k);
           jac = mul_rn(jac, jf_k);
           // vegas.py:110: fn(x * domain_sizes + domain_starts) * domain_volume
           const T xt = add_rn(mul_rn(x, wid[k]), lo[k]);
@@ -346,14 +349,14 @@ __global__ void __launch_bounds__(kTile, 3) vegas_sample_kernel(SampleArgs a) {
     __syncthreads();
     for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
       unsigned cnt = 0;
-      double w = 0.0;
+      H w = 0;
 #pragma unroll
       for (int q = 0; q < kWarps; ++q) {
         cnt += sm.hc[q * DB + i];
-        w += (double)sm.hw[q * DB + i];
+        w += sm.hw[q * DB + i];
       }
       if (cnt) {
-        atomicAdd(st.weights + i, w);
+        atomicAdd(st.weights + i, (double)w);
         atomicAdd((unsigned long long*)(st.counts + i), (unsigned long long)cnt);
       }
     }
@@ -524,13 +527,17 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
     a.partials[3 * blockIdx.x + 2] = Acc{dsum, 0.0};
   }
   if (last_block_arrives(a.ticket)) {
+    // fixed assignment of partials to threads and fixed tree: deterministic
+    Acc r{0, 0}, q{0, 0}, ds{0, 0};
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+      acc_add(r, a.partials[3 * i].s);
+      acc_add(q, a.partials[3 * i + 1].s);
+      acc_add(ds, a.partials[3 * i + 2].s);
+    }
+    r = block_reduce<kBlock>(r);
+    q = block_reduce<kBlock>(q);
+    ds = block_reduce<kBlock>(ds);
     if (threadIdx.x == 0) {
-      Acc r{0, 0}, q{0, 0}, ds{0, 0};
-      for (unsigned i = 0; i < gridDim.x; ++i) {  // index order: deterministic
-        acc_add(r, a.partials[3 * i].s);
-        acc_add(q, a.partials[3 * i + 1].s);
-        acc_add(ds, a.partials[3 * i + 2].s);
-      }
       const int64_t slot = st.control[1];
       if (slot >= 0 && slot < st.n_stat_slots) {
         double* out = st.stats + 4 * slot;
@@ -624,6 +631,21 @@ __global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state
     }
   }
   __syncthreads();
+  int zero_row = 0;
+  for (int k = threadIdx.x; k < d; k += blockDim.x) zero_row |= sums[k] == (T)0;
+  if (__syncthreads_or(zero_row)) {
+    // The map cannot be updated (:152-155, :187-196): reset and flag.
+    if (smooth_out) {
+      if (threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
+      return;
+    }
+    for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
+      st.weights[i] = 0.0;
+      st.counts[i] = 0;
+    }
+    if (threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
+    return;
+  }
   // EQ 18: [1,6,1]/8 smoothing with repeated borders, normalised; EQ 19
   for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
     const int64_t k = i / B, b = i - k * B;
@@ -812,9 +834,10 @@ __global__ void __launch_bounds__(kTile) vegas_strat_points_kernel(tq_vegas_stat
       else h = m;
     }
     int64_t cc = l;
+    const T nsf = (T)ns;
     for (int k = 0; k < d; ++k) {
       const int64_t q = cc / ns;
-      y[j * d + k] = strat_y<T>(cc - q * ns, u[j * d + k], ns);
+      y[j * d + k] = strat_y<T>((int)(cc - q * ns), u[j * d + k], nsf);
       cc = q;
     }
   }
@@ -824,7 +847,8 @@ template <typename T>
 __global__ void __launch_bounds__(kTile) vegas_map_points_kernel(tq_vegas_state st, const T* y,
                                                                  int64_t M, T* x, T* jac) {
   const int d = st.dim;
-  const int64_t B = st.n_bins;
+  const int B = (int)st.n_bins;
+  const T Bf = (T)B;
   const T* xe = (const T*)st.x_edges;
   const T* dxe = (const T*)st.dx_edges;
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < M;
@@ -832,7 +856,7 @@ __global__ void __launch_bounds__(kTile) vegas_map_points_kernel(tq_vegas_state 
     T jc = (T)1;
     for (int k = 0; k < d; ++k) {
       T xv, jf;
-      map_coord<T>(xe + k * (B + 1), dxe + k * B, B, y[j * d + k], xv, jf);
+      map_coord<T>(xe + k * (B + 1), dxe + k * B, B, Bf, y[j * d + k], xv, jf);
       x[j * d + k] = xv;
       jc = mul_rn(jc, jf);
     }
@@ -980,7 +1004,7 @@ static int launch_sample(const tq_vegas_state* st, int family, const double* par
                 st->dim * st->n_bins < (int64_t(1) << 30);
   a.edges_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, true) <= limit;
   const size_t smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, a.edges_smem);
-  const int64_t cap = (int64_t)sm_count() * 8;
+  const int64_t cap = (int64_t)sm_count() * 3;  // resident CTAs (launch bounds)
   int64_t tiles = max_points > 0 ? (max_points + kTile - 1) / kTile : cap;
   if (tiles > cap) tiles = cap;
   if (tiles < 1) tiles = 1;
