@@ -38,7 +38,9 @@ enum {
   TQ_ERR_WORKSPACE = -6,   /* workspace smaller than *_workspace_size()    */
   TQ_ERR_CUDA = -7,        /* a CUDA runtime call failed (tq_last_cuda_error) */
   TQ_ERR_DTYPE = -8,       /* unknown dtype code                           */
-  TQ_ERR_TIMEOUT = -9      /* a bounded device-side wait gave up           */
+  TQ_ERR_TIMEOUT = -9,     /* a bounded device-side wait gave up           */
+  TQ_ERR_SCRATCH = -10     /* needs more than the static scratch of
+                            * tq_grid_fused_noalloc holds                  */
 };
 
 enum { TQ_F32 = 0, TQ_F64 = 1 };
@@ -99,6 +101,20 @@ int tq_grid_fused(int dtype, int rule, int dim, int64_t n_per_dim,
                   const double* gl_weights, int family, const double* params,
                   void* out, int out_dtype, double* out64,
                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* tq_grid_fused without a workspace argument, for callers that cannot
+ * allocate device memory when they call (no counterpart in the reference).
+ * Scratch is a static device array of 256 B + 4096 CTA partials (64 KiB),
+ * enough for grids of up to 8 CTAs per SM on GPUs of up to 512 SMs; a
+ * request needing more returns TQ_ERR_SCRATCH.  The first call on a device
+ * looks the array's address up (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  Every call shares the one array, so calls that
+ * overlap on the GPU (other streams, other host threads) race: serialise
+ * them.  Allocates nothing. */
+int tq_grid_fused_noalloc(int dtype, int rule, int dim, int64_t n_per_dim,
+                          const void* domain, const double* gl_nodes,
+                          const double* gl_weights, int family, const double* params,
+                          void* out, int out_dtype, double* out64, void* stream);
 
 /* ---- grid rules: materialised path for arbitrary integrands -------------- */
 

@@ -24,6 +24,7 @@ TQ_ERR_WORKSPACE = -6
 TQ_ERR_CUDA = -7
 TQ_ERR_DTYPE = -8
 TQ_ERR_TIMEOUT = -9
+TQ_ERR_SCRATCH = -10
 
 TQ_F32, TQ_F64 = 0, 1
 
@@ -76,6 +77,11 @@ SIGNATURES = {
         c_int,
         [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
          c_void_p, c_int, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
+    "tq_grid_fused_noalloc": (
+        c_int,
+        [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
+         c_void_p, c_int, c_void_p, c_void_p],
     ),
     "tq_grid_points": (
         c_int,

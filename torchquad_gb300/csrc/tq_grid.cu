@@ -665,3 +665,58 @@ extern "C" int tq_finalize_sum(int dtype, int rule, int dim, const void* domain,
                                                      acc, n_values, out, out_dtype);
   return launch_status();
 }
+
+// ------------------------------------------- allocation-free entry point
+// For callers that cannot allocate device memory at call time: a plugin
+// inside a host application that owns all device memory, code that must not
+// allocate once it runs (a fixed-latency loop), or a plain C caller that has
+// no allocator to hand.  The CTA partials and the ticket word of the fused
+// grid rule live in this file-scope device array instead of a caller-given
+// workspace.  Every GPU that loads the library holds it until exit.
+#include <mutex>
+
+namespace {
+
+constexpr int kNoAllocSlots = 4096;  // CTA partials the static scratch holds
+constexpr size_t kNoAllocBytes = 256 + (size_t)kNoAllocSlots * sizeof(tq::Acc);
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (host code only sees a host-side stand-in under the array's
+// name, which must never be handed to a kernel).
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return tq::set_cuda_error(e);
+  if (dev < 0 || dev >= 64) return TQ_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return tq::set_cuda_error(e == cudaSuccess ? cudaErrorInvalidSymbol : e);
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return TQ_OK;
+}
+
+}  // namespace
+
+extern "C" int tq_grid_fused_noalloc(int dtype, int rule, int dim, int64_t n_per_dim,
+                                     const void* domain, const double* gl_nodes,
+                                     const double* gl_weights, int family, const double* params,
+                                     void* out, int out_dtype, double* out64, void* stream) {
+  if (tq_grid_fused_workspace_size(rule, dim, n_per_dim) > kNoAllocBytes) return TQ_ERR_SCRATCH;
+  void* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc != TQ_OK) return rc;
+  // the ticket word must start at zero; the last CTA leaves it at zero
+  const cudaError_t e = cudaMemsetAsync(scratch, 0, 16, (cudaStream_t)stream);
+  if (e != cudaSuccess) return tq::set_cuda_error(e);
+  return tq_grid_fused(dtype, rule, dim, n_per_dim, domain, gl_nodes, gl_weights, family, params,
+                       out, out_dtype, out64, scratch, kNoAllocBytes, stream);
+}

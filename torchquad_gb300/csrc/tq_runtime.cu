@@ -54,6 +54,8 @@ extern "C" const char* tq_status_string(int status) {
       return "unknown dtype code";
     case TQ_ERR_TIMEOUT:
       return "a bounded device-side wait gave up";
+    case TQ_ERR_SCRATCH:
+      return "problem needs more scratch than the static buffer of the allocation-free entry point holds";
     default:
       return "unknown status";
   }
