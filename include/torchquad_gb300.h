@@ -116,6 +116,23 @@ int tq_grid_fused_noalloc(int dtype, int rule, int dim, int64_t n_per_dim,
                           const double* gl_weights, int family, const double* params,
                           void* out, int out_dtype, double* out64, void* stream);
 
+/* ---- grid rules: adjoint --------------------------------------------------- */
+
+size_t tq_grid_adjoint_workspace_size(int dim, int64_t total_points);
+
+/* Value and gradient of the fused tensor-product rule (dim <= 8):
+ * out_value[0] = I, out_grad_domain[k][0|1] = dI/da_k | dI/db_k,
+ * out_grad_params[i] = dI/dparams[i] (same layout as params: c, b, a_k, u_k).
+ * Replaces torch autograd through the reference's materialised grid
+ * (integration_grid.py:74-88, utils.py:36-52, gaussian.py:81-84,159-162);
+ * the domain gradient is that of nodes a + t (b - a) with weights
+ * proportional to prod (b - a), as in those code paths. */
+int tq_grid_adjoint(int dtype, int rule, int dim, int64_t n_per_dim, const void* domain,
+                    const double* gl_nodes, const double* gl_weights, int family,
+                    const double* params, double* out_value, double* out_grad_domain,
+                    double* out_grad_params, void* workspace, size_t workspace_bytes,
+                    void* stream);
+
 /* ---- grid rules: materialised path for arbitrary integrands -------------- */
 
 /* Writes points[count][dim] (dtype; fp64 for TQ_RULE_GAUSS) for the flat

@@ -305,6 +305,46 @@ def gen_vegas_special(tq):
     return out
 
 
+def gen_grads(tq):
+    """Reference torch autograd of the grid rules w.r.t. the domain and the
+    integrand's parameters (the differentiation configuration and more)."""
+    import torch
+    import torchquad_gb300.integrands as I
+
+    f64 = torch.float64
+
+    def t(v):
+        return torch.tensor(v, dtype=f64, requires_grad=True)
+
+    cases = [
+        ("C4-GaussLegendre-osc4-32", "GaussLegendre", 4, 32**4, "Oscillatory",
+         dict(a=[1.2, -2.1, 0.7, 2.6], b=0.37), ["b"], [[0.0, 1.0]] * 4, "float64"),
+        ("Simpson-gauss2", "Simpson", 2, 33**2, "GaussianPeak",
+         dict(a=[2.0, 3.0], u=[0.3, 0.6], c=1.5), ["a", "u", "c"], [[-1.0, 1.0], [0.0, 2.0]], "float64"),
+        ("Trapezoid-expsum3", "Trapezoid", 3, 21**3, "ExpSum",
+         dict(a=[0.5, -1.0, 2.0], b=0.25), ["a", "b"], [[0.0, 1.0], [-1.0, 0.5], [0.2, 0.4]], "float64"),
+        ("Boole-sumsin1", "Boole", 1, 101, "SumSin", dict(a=[2.0], c=0.7), ["a", "c"], [[0.0, 2.0]], "float64"),
+        ("GaussLegendre-gauss3-f32", "GaussLegendre", 3, 8**3, "GaussianPeak",
+         dict(a=[1.0, 2.0, 0.5], u=[0.2, 0.5, 0.9]), ["a", "u"], [[0.0, 1.0]] * 3, "float32"),
+    ]
+    out = []
+    for name, rule, dim, N, kind, kw, grad_params, dom, dtype in cases:
+        kw2 = {}
+        for k, v in kw.items():
+            kw2[k] = t(v) if k in grad_params else v
+        f = getattr(I, kind)(dim, **kw2)
+        domain = torch.tensor(dom, dtype=getattr(torch, dtype), requires_grad=True)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            val = getattr(tq, rule)().integrate(f, dim, N=N, integration_domain=domain)
+        val.backward()
+        grads = {k: hexarr(kw2[k].grad.numpy()) for k in grad_params}
+        out.append(dict(name=name, rule=rule, dim=dim, N=N, family=kind, params=kw, grad_params=grad_params,
+                        domain=dom, dtype=dtype, value=hexf(val.item()), grad_domain=hexarr(domain.grad.numpy()),
+                        grads=grads))
+    return out
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     tq = _import_reference(ref_root)
@@ -318,6 +358,7 @@ def main():
         "multidim": gen_multidim(tq),
         "linspace": gen_linspace(),
         "mc": gen_mc(tq),
+        "grads": gen_grads(tq),
     }
     with open(HERE / "grid_mc_golden.json", "w") as fh:
         json.dump(data, fh, indent=0)

@@ -83,6 +83,12 @@ SIGNATURES = {
         [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p,
          c_void_p, c_int, c_void_p, c_void_p],
     ),
+    "tq_grid_adjoint_workspace_size": (c_size_t, [c_int, c_int64]),
+    "tq_grid_adjoint": (
+        c_int,
+        [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
+         c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
     "tq_grid_points": (
         c_int,
         [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p],

@@ -152,3 +152,23 @@ def mc_fused(dim, n_points, domain, integrand, seed, stream_id, offset):
     )
     L.count_launches(1)
     return out
+
+
+def grid_adjoint(rule, dim, n, domain, gl_nodes, gl_weights, integrand):
+    """(value, d/d domain [dim, 2], d/d params [2+2dim]) in fp64."""
+    dev = domain.device
+    val = torch.empty((), dtype=torch.float64, device=dev)
+    gdom = torch.empty((dim, 2), dtype=torch.float64, device=dev)
+    gpar = torch.empty((2 + 2 * dim,), dtype=torch.float64, device=dev)
+    params = integrand.device_params(dev)
+    ws = L.workspace.get(L.lib().tq_grid_adjoint_workspace_size(dim, n**dim), "adjoint")
+    L.check(
+        L.lib().tq_grid_adjoint(
+            L.dtype_code(domain.dtype), rule, dim, n, domain.data_ptr(), L.ptr(gl_nodes),
+            L.ptr(gl_weights), integrand.family, params.data_ptr(), val.data_ptr(), gdom.data_ptr(),
+            gpar.data_ptr(), ws.data_ptr(), ws.numel(), L.stream_handle(),
+        ),
+        "tq_grid_adjoint",
+    )
+    L.count_launches(1)
+    return val, gdom, gpar

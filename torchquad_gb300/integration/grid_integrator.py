@@ -49,6 +49,33 @@ def _n_per_dim(N, dim):
     return int(N ** (1.0 / dim) + 1e-8)
 
 
+class _FusedGridFn(torch.autograd.Function):
+    """Fused rule with a hand-written adjoint: forward is tq_grid_fused,
+    backward is tq_grid_adjoint (value and all gradients in one pass)."""
+
+    @staticmethod
+    def forward(ctx, domain, c, b, a, u, integ, fn, dim, n):
+        ctx.integ, ctx.fn, ctx.dim, ctx.n = integ, fn, dim, n
+        ctx.save_for_backward(domain, c, b, a, u)
+        return integ._integrate_fused(fn, dim, n, domain.detach())
+
+    @staticmethod
+    def backward(ctx, gout):
+        domain, c, b, a, u = ctx.saved_tensors
+        integ, fn, dim, n = ctx.integ, ctx.fn, ctx.dim, ctx.n
+        gl_nodes, gl_w = integ._gl_tables(n, domain.device)
+        _, gdom, gpar = K.grid_adjoint(integ._rule, dim, n, domain.detach(), gl_nodes, gl_w, fn)
+        g = gout.detach().to(torch.float64)
+
+        def back(t, grad):
+            if t is None or not t.requires_grad:
+                return None
+            return (g * grad).reshape(t.shape).to(t.device, t.dtype)
+
+        return (back(domain, gdom), back(c, gpar[0]), back(b, gpar[1]), back(a, gpar[2 : 2 + dim]),
+                back(u, gpar[2 + dim : 2 + 2 * dim]), None, None, None, None)
+
+
 class GridIntegrator(BaseIntegrator):
     """Base of the tensor-product rules (Newton-Cotes and Gaussian)."""
 
@@ -70,6 +97,8 @@ class GridIntegrator(BaseIntegrator):
         self._nr_of_fevals = n**dim
         if self._can_fuse(fn, dim, domain):
             return self._integrate_fused(fn, dim, n, domain)
+        if self._can_fuse_adjoint(fn, dim):
+            return _FusedGridFn.apply(domain, fn.c, fn.b, fn.a, fn.u, self, fn, dim, n)
         return self._integrate_materialised(fn, dim, n, domain)
 
     def calculate_grid(self, N, integration_domain, disable_integration_domain_check=False):
@@ -151,6 +180,11 @@ class GridIntegrator(BaseIntegrator):
         if torch.is_grad_enabled() and (domain.requires_grad or fn.requires_grad()):
             return False
         return True
+
+    def _can_fuse_adjoint(self, fn, dim):
+        """Built-in integrand whose gradient the adjoint kernel computes."""
+        return (isinstance(fn, BuiltinIntegrand) and fn.dim == dim and dim <= 8
+                and getattr(self, "_rescales_nodes", True))
 
     def _integrate_fused(self, fn, dim, n, domain):
         gl_nodes, gl_w = self._gl_tables(n, domain.device)

@@ -239,7 +239,10 @@ class VEGAS(BaseIntegrator):
             self._run_iteration()
             if self._check_abort_conditions():
                 break
-        return torch.tensor(self._get_result(), dtype=self.dtype, device=domain.device)
+        res = self._get_result()
+        if isinstance(res, torch.Tensor):  # differentiable (see _run_iteration)
+            return res.to(self.dtype)
+        return torch.tensor(res, dtype=self.dtype, device=domain.device)
 
     def _warmup_grid(self, warmup_N_it=5, N_samples=1000):
         """Warm up the map: warmup_N_it rounds of N_samples uniform points
@@ -272,11 +275,19 @@ class VEGAS(BaseIntegrator):
         if self.use_grid_improve:
             self.map.update_map()
         st = self._dev.stats[slot].cpu()
-        self.results[-1] = float(st[0])
+        res = float(st[0])
+        if torch.is_grad_enabled() and jf_vec.requires_grad:
+            # The iteration estimate sum_c JF_c V / n_c = sum_i jf_i V / n_c(i)
+            # (vegas.py:293-302) as a torch expression for the gradient; its
+            # value stays the kernel's compensated fp64 sum.
+            w = torch.repeat_interleave(self.strat.V_cubes / neval.to(torch.float64), neval)
+            r_t = (jf_vec.to(torch.float64) * w).sum()
+            res = res + (r_t - r_t.detach())
+        self.results[-1] = res
         self.sigma2[-1] = float(st[1])
         acc = math.sqrt(self.sigma2[-1])
-        if self.results[-1] != 0.0:
-            acc = acc / abs(self.results[-1])
+        if float(self.results[-1]) != 0.0:
+            acc = acc / abs(float(self.results[-1]))
         return acc
 
     # ------------------------------------------------- shared host logic
@@ -285,7 +296,7 @@ class VEGAS(BaseIntegrator):
         iteration, stop on budget/iterations (vegas.py:161-209)."""
         if self.it % 5 > 0:
             return False
-        res_abs = abs(self._get_result())
+        res_abs = abs(float(self._get_result()))
         err = self._get_error()
         chi2 = self._get_chisq()
         if (err <= self._eps_rel * res_abs or err <= self._eps_abs) and chi2 / 5.0 < 1.0:
@@ -324,5 +335,6 @@ class VEGAS(BaseIntegrator):
 
     def _get_chisq(self):
         """Chi square of the iteration results (EQ 32)."""
-        I_final = self._get_result()
-        return sum(((r - I_final) ** 2 / s for r, s in zip(self.results, self.sigma2) if r != I_final), 0.0)
+        I_final = float(self._get_result())
+        res = [float(r) for r in self.results]
+        return sum(((r - I_final) ** 2 / s for r, s in zip(res, self.sigma2) if r != I_final), 0.0)
