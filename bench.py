@@ -58,6 +58,104 @@ def _dist_env():
     return ws, rank, local
 
 
+# ------------------------------------------------- batched workload (C3)
+def c3_workload(n=4096, seed=1):
+    """4096 independent Gaussian-peak integrals: dims U{1..4}, rule U{trapezoid,
+    simpson, boole, gausslegendre}, N log-uniform 1e3..1e6 (points per
+    dimension then made valid for the rule), f = exp(-sum a_i (x_i-u_i)^2),
+    a_i ~ U[0.5, 5], u_i ~ U[0, 1], domains [l, l+w], l ~ U[-1, 0],
+    w ~ U[0.5, 2]; returns (specs, analytic values)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    rules = ["trapezoid", "simpson", "boole", "gausslegendre"]
+    out, exact = [], []
+    for _ in range(n):
+        d = int(rng.integers(1, 5))
+        rule = rules[int(rng.integers(0, 4))]
+        N = int(10 ** rng.uniform(3, 6))
+        a = rng.uniform(0.5, 5.0, d)
+        u = rng.uniform(0.0, 1.0, d)
+        lo = rng.uniform(-1.0, 0.0, d)
+        w = rng.uniform(0.5, 2.0, d)
+        dom = np.stack([lo, lo + w], axis=1)
+        out.append((rule, d, N, dom, a, u))
+        v = 1.0
+        for k in range(d):
+            s = math.sqrt(a[k])
+            v *= math.sqrt(math.pi / a[k]) / 2.0 * (math.erf(s * (lo[k] + w[k] - u[k])) - math.erf(s * (lo[k] - u[k])))
+        exact.append(v)
+    return out, exact
+
+
+def measure_batched(tq, dev, reps=5):
+    """Batched (one persistent launch) vs plain per-call integration of the
+    4096-integral workload, fp32 and fp64; integrals/s and accuracy."""
+    import numpy as np
+    import torch
+    from torchquad_gb300 import batch as B
+
+    specs, exact = c3_workload()
+    exact = np.array(exact)
+    cls = {"trapezoid": tq.Trapezoid, "simpson": tq.Simpson, "boole": tq.Boole, "gausslegendre": tq.GaussLegendre}
+    out = {"workload": "4096 Gaussian-peak integrals, dims 1-4, trapezoid/simpson/boole/gausslegendre, "
+                       "N log-uniform 1e3-1e6, seed 1"}
+    for dtype in (torch.float32, torch.float64):
+        name = "fp32" if dtype == torch.float32 else "fp64"
+        fs = [tq.GaussianPeak(d, a=a.tolist(), u=u.tolist()) for (_, d, _, _, a, u) in specs]
+        rules = [sp[0] for sp in specs]
+        Ns = [sp[2] for sp in specs]
+        doms = [sp[3] for sp in specs]
+        bg = B.BatchedGrid(dtype=dtype, autotune=True)
+        plan = bg.plan(fs, rules, Ns, doms)
+        shape = bg.tuned_shape(plan)
+        plan = bg.retile(plan, shape[2])
+        vals = bg.run(plan, shape)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            vals = bg.run(plan, shape)
+        e1.record()
+        torch.cuda.synchronize()
+        t_batch = e0.elapsed_time(e1) / reps / 1000.0
+        t0 = time.perf_counter()
+        v_e2e = bg.integrate(fs, rules, Ns, doms).cpu()
+        t_e2e = time.perf_counter() - t0
+        vb = vals.double().cpu().numpy()
+        # plain per-call GPU form: one integrate() per integral, domains resident
+        dtens = [torch.tensor(dm, dtype=dtype, device=dev) for dm in doms]
+        import warnings
+
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            for i in range(64):  # warm-up
+                cls[rules[i]]().integrate(fs[i], fs[i].dim, N=Ns[i], integration_domain=dtens[i])
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            plain = [cls[r]().integrate(f, f.dim, N=N, integration_domain=dt)
+                     for r, f, N, dt in zip(rules, fs, Ns, dtens)]
+            torch.cuda.synchronize()
+            t_plain = time.perf_counter() - t0
+        vp = np.array([float(x) for x in plain])
+        rel = np.abs(vb - exact) / np.abs(exact)
+        out[name] = {
+            "batched_integrals_per_s": len(specs) / t_batch,
+            "batched_ms": t_batch * 1000.0,
+            "batched_e2e_integrals_per_s": len(specs) / t_e2e,
+            "plain_integrals_per_s": len(specs) / t_plain,
+            "speedup_batched_vs_plain": t_plain / t_batch,
+            "speedup_batched_e2e_vs_plain": t_plain / t_e2e,
+            "evals_per_s": plan.total_points / t_batch,
+            "total_points": plan.total_points,
+            "tuned_shape": {"block": shape[0], "strip": shape[1], "tile_points": shape[2], "ctas": shape[3]},
+            "frac_within_1e-4_of_analytic": float(np.mean(rel <= 1e-4)),
+            "max_rel_diff_batched_vs_plain": float(np.max(np.abs(vb - vp) / np.maximum(np.abs(vp), 1e-300))),
+            "max_rel_diff_e2e_vs_resident": float(np.max(np.abs(v_e2e.double().numpy() - vb) / np.abs(vb))),
+        }
+    return out
+
+
 # ----------------------------------------------------------- CPU (oracle)
 def _oracle_one(seed):
     import numpy as np
@@ -373,6 +471,8 @@ def run_gpu(args):
         "clocks": clocks.summary(),
         "evals_per_step": tot_evals / (args.steps * ws),
     }
+    if not args.no_batched:
+        line["batched"] = measure_batched(tq, dev)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
     print(json.dumps(line), flush=True)
@@ -390,6 +490,7 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batched", action="store_true", help="skip the batched-vs-plain measurement")
     p.add_argument("--cpu-seconds", type=float, default=20.0)
     args = p.parse_args()
     if args.warmup < 3 and args.impl == "ours":

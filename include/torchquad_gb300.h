@@ -116,6 +116,31 @@ int tq_grid_fused_noalloc(int dtype, int rule, int dim, int64_t n_per_dim,
                           const double* gl_weights, int family, const double* params,
                           void* out, int out_dtype, double* out64, void* stream);
 
+/* ---- batched grid rules ---------------------------------------------------- */
+
+/* Descriptor of one integral of a batch (48 bytes, int64-aligned). */
+typedef struct tq_batch_desc {
+  int32_t rule, dim;   /* TQ_RULE_TRAPEZOID..TQ_RULE_GAUSS, 1..TQ_MAX_DIM        */
+  int64_t n, total;    /* points per dimension, n^dim                          */
+  int64_t par_off;     /* offset of the integral's 2+2*dim parameters in params */
+  int64_t dom_off;     /* offset of its [dim][2] domain in domains (dtype)      */
+  int64_t gl_off;      /* offset of its n Gauss roots/weights (fp64)           */
+} tq_batch_desc;
+
+/* Many tensor-product integrals of one built-in family in one persistent
+ * launch (no counterpart in the reference, whose batch is a loop of
+ * GridIntegrator.integrate, grid_integrator.py:32-55).  Integral i is cut
+ * into ceil(total_i / tile_points) tiles; tile_start[n_integrals+1] is the
+ * exclusive prefix of the tile counts (tile_start[n_integrals] = n_tiles).
+ * block (128|256), strip (4|16 nodes per thread) and grid_blocks (0: 8 per
+ * SM) are the tunable launch shape.  out[i] (out_dtype) receives integral
+ * i; workspace >= n_tiles * 16 bytes. */
+int tq_batch_grid(int dtype, int64_t n_integrals, const void* descs, const int64_t* tile_start,
+                  int64_t n_tiles, int64_t tile_points, const double* params,
+                  const void* domains, const double* gl_nodes, const double* gl_weights,
+                  int family, int block, int strip, int grid_blocks, void* out, int out_dtype,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- grid rules: adjoint --------------------------------------------------- */
 
 size_t tq_grid_adjoint_workspace_size(int dim, int64_t total_points);

@@ -28,6 +28,7 @@ from .utils.set_precision import set_precision
 from .utils.set_up_backend import set_up_backend
 
 from . import integrands
+from . import batch
 from .integrands import ExpSum, GaussianPeak, Oscillatory, SumSin, BuiltinIntegrand
 
 __all__ = [
@@ -51,6 +52,7 @@ __all__ = [
     "set_up_backend",
     "set_materialise_budget",
     "integrands",
+    "batch",
     "ExpSum",
     "GaussianPeak",
     "Oscillatory",

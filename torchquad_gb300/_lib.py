@@ -89,6 +89,11 @@ SIGNATURES = {
         [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
          c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
     ),
+    "tq_batch_grid": (
+        c_int,
+        [c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_void_p,
+         c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_size_t, c_void_p],
+    ),
     "tq_grid_points": (
         c_int,
         [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p],

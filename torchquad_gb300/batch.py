@@ -1,0 +1,273 @@
+"""Batched tensor-product integration: many integrals of mixed rule,
+dimension, size and domain in one persistent launch (``tq_batch_grid``).
+
+The reference has no batched API; the equivalent is a loop of per-call
+``Trapezoid/Simpson/Boole/GaussLegendre().integrate`` (grid_integrator.py:
+32-55).  Each integral here gets exactly the rule, points per dimension
+(after the reference's N adjustment, simpson.py:53-83 / boole.py:55-84) and
+weights that the per-call form uses; only the summation order differs.
+
+    from torchquad_gb300 import batch
+    b = batch.BatchedGrid(dtype=torch.float64)
+    values = b.integrate(integrands, rules, Ns, domains)   # [n] tensor
+
+All integrands of one call are built-in instances of the same family
+(``torchquad_gb300.integrands``); mixed families are split by family.
+The launch shape (threads per CTA, nodes per thread, nodes per tile, CTAs)
+is chosen by a small autotuner that times candidates on the actual batch.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .integrands import BuiltinIntegrand
+
+RULES = {
+    "trapezoid": L.TQ_RULE_TRAPEZOID,
+    "simpson": L.TQ_RULE_SIMPSON,
+    "boole": L.TQ_RULE_BOOLE,
+    "gausslegendre": L.TQ_RULE_GAUSS,
+    "gauss": L.TQ_RULE_GAUSS,
+}
+
+DESC_DTYPE = np.dtype(
+    [("rule", "<i4"), ("dim", "<i4"), ("n", "<i8"), ("total", "<i8"), ("par_off", "<i8"),
+     ("dom_off", "<i8"), ("gl_off", "<i8")]
+)
+assert DESC_DTYPE.itemsize == 48
+
+
+def rule_id(r) -> int:
+    if isinstance(r, (int, np.integer)):
+        return int(r)
+    if isinstance(r, type):
+        r = r.__name__
+    return RULES[str(r).lower()]
+
+
+def points_per_dim(rule: int, dim: int, N: int) -> int:
+    """n after the reference's N adjustment (no warnings in a batch)."""
+    n = int(N ** (1.0 / dim) + 1e-8)
+    if rule == L.TQ_RULE_SIMPSON:
+        if n < 3:
+            n = 3
+        elif n % 2 != 1:
+            n -= 1
+    elif rule == L.TQ_RULE_BOOLE:
+        if n < 5:
+            n = 5
+        elif (n - 1) % 4 != 0:
+            n -= (n - 1) % 4
+    elif n < 2:
+        raise ValueError(f"N={N} gives fewer than 2 points per dimension in {dim} dimensions")
+    return n
+
+
+_GL_CACHE = {}
+
+
+def _gl(n):
+    t = _GL_CACHE.get(n)
+    if t is None:
+        t = np.polynomial.legendre.leggauss(n)
+        _GL_CACHE[n] = t
+    return t
+
+
+@dataclass
+class BatchPlan:
+    """Device-resident packed batch (reusable across calls)."""
+
+    dtype: torch.dtype
+    family: int
+    n_int: int
+    desc_np: np.ndarray
+    descs: torch.Tensor
+    tile_start: torch.Tensor
+    n_tiles: int
+    tile_pts: int
+    params: torch.Tensor
+    domains: torch.Tensor
+    gl_nodes: torch.Tensor
+    gl_weights: torch.Tensor
+    total_points: int
+    shape_key: tuple
+
+
+class Autotuner:
+    """Times candidate launch shapes on the real batch; caches the best per
+    batch signature (dtype, family, size buckets)."""
+
+    def __init__(self):
+        self.cache = {}
+
+    def candidates(self, sms):
+        out = []
+        for tile in (8192, 32768, 131072):
+            for block in (128, 256):
+                for strip in (4, 16):
+                    out.append((block, strip, tile, sms * 8))
+        return out
+
+    def pick(self, key, run, sms, reps=3):
+        if key in self.cache:
+            return self.cache[key]
+        best, best_t = None, float("inf")
+        for cand in self.candidates(sms):
+            try:
+                run(cand)  # warm-up / validity
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    run(cand)
+                e1.record()
+                torch.cuda.synchronize()
+                t = e0.elapsed_time(e1) / reps
+            except L.TorchquadGB300Error:
+                continue
+            if t < best_t:
+                best, best_t = cand, t
+        self.cache[key] = best
+        return best
+
+
+AUTOTUNER = Autotuner()
+
+
+class BatchedGrid:
+    def __init__(self, dtype=torch.float64, autotune=True, tile_points=32768, block=256, strip=16):
+        if dtype not in (torch.float32, torch.float64):
+            raise TypeError("dtype must be torch.float32 or torch.float64")
+        self.dtype = dtype
+        self.autotune = autotune
+        self.default_shape = (block, strip, tile_points, 0)
+        self.last_shape = None
+
+    # ------------------------------------------------------------ packing
+    def plan(self, integrands, rules, Ns, domains, tile_points=None):
+        """Pack a batch into device arrays.  integrands: list of built-in
+        integrands of one family; rules: names ("simpson", ...) or TQ ids;
+        Ns: total points as for integrate(N=...); domains: [dim][2] each."""
+        device = L.require_cuda()
+        m = len(integrands)
+        if not (len(rules) == len(Ns) == len(domains) == m) or m == 0:
+            raise ValueError("integrands, rules, Ns and domains must have the same non-zero length")
+        fams = {f.family for f in integrands}
+        if len(fams) != 1 or not all(isinstance(f, BuiltinIntegrand) for f in integrands):
+            raise ValueError("one batch takes built-in integrands of a single family")
+        family = fams.pop()
+        tile_pts = int(tile_points or self.default_shape[2])
+        desc = np.zeros(m, dtype=DESC_DTYPE)
+        par, dom, gln, glw = [], [], [], []
+        par_off = dom_off = gl_off = 0
+        gl_index = {}
+        for i, (f, r, N, d) in enumerate(zip(integrands, rules, Ns, domains)):
+            rid = rule_id(r)
+            dim = f.dim
+            if dim < 1 or dim > L.TQ_MAX_DIM:
+                raise ValueError(f"integral {i}: dim {dim} out of range")
+            d = np.asarray(d, dtype=np.float64).reshape(dim, 2)
+            if np.any(d[:, 1] < d[:, 0]):
+                raise ValueError(f"integral {i}: integration_domain has invalid boundary values")
+            n = points_per_dim(rid, dim, int(N))
+            total = n**dim
+            g = 0
+            if rid == L.TQ_RULE_GAUSS:
+                if n not in gl_index:
+                    rr, ww = _gl(n)
+                    gl_index[n] = gl_off
+                    gln.append(rr)
+                    glw.append(ww)
+                    gl_off += n
+                g = gl_index[n]
+            pv = f.params_vector().numpy()
+            desc[i] = (rid, dim, n, total, par_off, dom_off, g)
+            par.append(pv)
+            dom.append(d.ravel())
+            par_off += pv.size
+            dom_off += 2 * dim
+        tiles = (desc["total"] + tile_pts - 1) // tile_pts
+        ts = np.zeros(m + 1, dtype=np.int64)
+        np.cumsum(tiles, out=ts[1:])
+        npdt = np.float32 if self.dtype == torch.float32 else np.float64
+        glcat = (np.concatenate(gln), np.concatenate(glw)) if gln else (np.zeros(1), np.zeros(1))
+        total_points = int(desc["total"].sum())
+        key = (self.dtype, family, int(math.log2(m)), int(math.log2(max(1, total_points))))
+        return BatchPlan(
+            dtype=self.dtype,
+            family=family,
+            n_int=m,
+            desc_np=desc,
+            descs=torch.from_numpy(desc.view(np.uint8).copy()).to(device),
+            tile_start=torch.from_numpy(ts).to(device),
+            n_tiles=int(ts[-1]),
+            tile_pts=tile_pts,
+            params=torch.from_numpy(np.concatenate(par)).to(device),
+            domains=torch.from_numpy(np.concatenate(dom).astype(npdt)).to(device),
+            gl_nodes=torch.from_numpy(glcat[0]).to(device),
+            gl_weights=torch.from_numpy(glcat[1]).to(device),
+            total_points=total_points,
+            shape_key=key,
+        )
+
+    def retile(self, plan, tile_pts):
+        if tile_pts == plan.tile_pts:
+            return plan
+        desc = plan.desc_np
+        tiles = (desc["total"] + tile_pts - 1) // tile_pts
+        ts = np.zeros(plan.n_int + 1, dtype=np.int64)
+        np.cumsum(tiles, out=ts[1:])
+        return BatchPlan(**{**plan.__dict__, "tile_start": torch.from_numpy(ts).to(plan.descs.device),
+                            "n_tiles": int(ts[-1]), "tile_pts": tile_pts})
+
+    # ------------------------------------------------------------ running
+    def run(self, plan, shape=None, out=None):
+        block, strip, tile_pts, grid = shape or self.default_shape
+        if tile_pts != plan.tile_pts:
+            plan = self.retile(plan, tile_pts)
+        if out is None:
+            out = torch.empty((plan.n_int,), dtype=self.dtype, device=plan.descs.device)
+        ws = L.workspace.get(plan.n_tiles * 16, "batch")
+        L.check(
+            L.lib().tq_batch_grid(
+                L.dtype_code(self.dtype), plan.n_int, plan.descs.data_ptr(), plan.tile_start.data_ptr(),
+                plan.n_tiles, plan.tile_pts, plan.params.data_ptr(), plan.domains.data_ptr(),
+                plan.gl_nodes.data_ptr(), plan.gl_weights.data_ptr(), plan.family, block, strip, grid,
+                out.data_ptr(), L.dtype_code(self.dtype), ws.data_ptr(), ws.numel(), L.stream_handle(),
+            ),
+            "tq_batch_grid",
+        )
+        L.count_launches(2)
+        return out
+
+    def tuned_shape(self, plan):
+        if not self.autotune:
+            return self.default_shape
+        cache = {}
+
+        def run(cand):
+            p = cache.get(cand[2])
+            if p is None:
+                p = cache[cand[2]] = self.retile(plan, cand[2])
+            self.run(p, cand)
+
+        return AUTOTUNER.pick(plan.shape_key, run, L.lib().tq_device_sm_count())
+
+    def integrate(self, integrands, rules, Ns, domains):
+        """Values of all integrals, [n] tensor of the batch dtype."""
+        plan = self.plan(integrands, rules, Ns, domains)
+        shape = self.tuned_shape(plan)
+        self.last_shape = shape
+        return self.run(self.retile(plan, shape[2]), shape)
+
+
+def integrate_batch(integrands, rules, Ns, domains, dtype=torch.float64, autotune=True):
+    """Functional form of BatchedGrid(dtype).integrate(...)."""
+    return BatchedGrid(dtype=dtype, autotune=autotune).integrate(integrands, rules, Ns, domains)

@@ -58,7 +58,8 @@ __device__ __forceinline__ Acc block_reduce(Acc a) {
   if (lane == 0) warp_acc[warp] = a;
   __syncthreads();
   if (warp == 0) {
-    a = (lane < BLOCK / 32) ? warp_acc[lane] : Acc{0.0, 0.0};
+    const int nw = min(BLOCK / 32, (int)(blockDim.x >> 5));
+    a = (lane < nw) ? warp_acc[lane] : Acc{0.0, 0.0};
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) acc_merge(a, acc_shfl_down(a, off));
   }
