@@ -72,9 +72,16 @@ def points_per_dim(rule: int, dim: int, N: int) -> int:
 _GL_CACHE = {}
 
 
+MAX_GAUSS_NODES = 20000
+
+
 def _gl(n):
     t = _GL_CACHE.get(n)
     if t is None:
+        if n > MAX_GAUSS_NODES:
+            raise ValueError(
+                f"{n} Gauss-Legendre nodes per dimension: numpy.polynomial.legendre.leggauss builds an "
+                f"n x n matrix; use at most {MAX_GAUSS_NODES}")
         t = np.polynomial.legendre.leggauss(n)
         _GL_CACHE[n] = t
     return t

@@ -75,6 +75,10 @@ class Gaussian(GridIntegrator):
                 raise NotImplementedError(f"N {N} is not an int and lacks an `item` method")
         if root_args in self._cache:
             return self._cache[root_args]
+        if self._root_fn is numpy.polynomial.legendre.leggauss and root_args[0] > 20000:
+            raise ValueError(
+                f"{root_args[0]} Gauss-Legendre nodes per dimension: numpy.polynomial.legendre.leggauss "
+                "builds an n x n matrix; use at most 20000")
         self._cache[root_args] = self._root_fn(*root_args)
         return self._cache[root_args]
 
