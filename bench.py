@@ -160,6 +160,56 @@ def measure_batched(tq, dev, reps=5):
     return out
 
 
+def measure_serving(tq, dev, n=120, rates=(1e2, 1e3, 1e4, 1e5)):
+    """Poisson request streams (MC / VEGAS / Simpson, dims 1-10, N log-uniform
+    1e4..1e8, target relative error 1e-3..1e-5, seed 2) through the serving
+    loop: p50/p99 latency and integrals/s per arrival rate, and the same
+    requests through the plain per-call API one after the other."""
+    import warnings
+
+    import torch
+    from torchquad_gb300.serving import IntegrationRequest, IntegrationServer, poisson_stream
+
+    out = {"requests_per_rate": n}
+    for rate in rates:
+        stream = poisson_stream(n, rate, seed=2)
+        with IntegrationServer(max_active=64) as srv:
+            t0 = time.perf_counter()
+            futs = []
+            for t_arr, req in stream:
+                delay = t0 + t_arr - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                futs.append(srv.submit(req))
+            srv.drain(timeout=600)
+            st = srv.stats()
+        out[f"rate_{int(rate)}"] = {k: st[k] for k in ("p50_ms", "p99_ms", "integrals_per_s", "peak_active", "evals")}
+    # plain per-call path, same requests, back to back
+    stream = poisson_stream(n, rates[-1], seed=2)
+    cls = {"montecarlo": tq.MonteCarlo, "vegas": tq.VEGAS, "simpson": tq.Simpson}
+    lat = []
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _, r in stream:
+            t1 = time.perf_counter()
+            dom = torch.tensor(r.domain, dtype=r.dtype, device=dev)
+            kw = {"seed": r.seed} if r.method != "simpson" else {}
+            if r.method == "vegas":
+                kw["eps_rel"] = r.eps_rel
+            cls[r.method]().integrate(r.integrand, r.dim, N=r.N, integration_domain=dom, **kw).item()
+            lat.append(time.perf_counter() - t1)
+        t_plain = time.perf_counter() - t0
+    import numpy as np
+
+    out["plain_per_call"] = {"integrals_per_s": n / t_plain, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                             "p99_ms": float(np.percentile(lat, 99) * 1e3)}
+    best = max(v["integrals_per_s"] for k, v in out.items() if k.startswith("rate_"))
+    out["served_vs_plain_integrals_per_s"] = best / (n / t_plain)
+    return out
+
+
 # ----------------------------------------------------------- CPU (oracle)
 def _oracle_one(seed):
     import numpy as np
@@ -477,6 +527,8 @@ def run_gpu(args):
     }
     if not args.no_batched:
         line["batched"] = measure_batched(tq, dev)
+    if not args.no_serving:
+        line["serving"] = measure_serving(tq, dev)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.cpu_seconds)
     print(json.dumps(line), flush=True)
@@ -495,6 +547,7 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the batched-vs-plain measurement")
+    p.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     p.add_argument("--cpu-seconds", type=float, default=20.0)
     args = p.parse_args()
     if args.warmup < 3 and args.impl == "ours":

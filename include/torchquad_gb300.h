@@ -141,6 +141,26 @@ int tq_batch_grid(int dtype, int64_t n_integrals, const void* descs, const int64
                   int family, int block, int strip, int grid_blocks, void* out, int out_dtype,
                   void* workspace, size_t workspace_bytes, void* stream);
 
+/* Descriptor of one Monte Carlo chunk of a batch (56 bytes). */
+typedef struct tq_mc_desc {
+  int32_t dim, pad;
+  int64_t first, count;  /* point range [first, first+count) of the stream */
+  uint64_t seed, stream_id;
+  int64_t par_off, dom_off;
+} tq_mc_desc;
+
+/* One chunk of each of many Monte Carlo integrations of one built-in family
+ * (no counterpart in the reference; its MonteCarlo.integrate,
+ * monte_carlo.py:20-106, does one integral per call).  Request r evaluates
+ * points [first, first+count) of its Philox stream (point p uses elements
+ * p*dim .. p*dim+dim-1 of tq_uniform's layout at block offset 0) with
+ * x = u * (b - a) + a, and adds sum f, sum f^2 to acc[r][0..1] and
+ * acc[r][2..3] (compensated pairs).  tile_start[n_requests+1] is the prefix
+ * of ceil(count / tile_points); workspace >= n_tiles * 32 bytes. */
+int tq_batch_mc(int dtype, int64_t n_requests, const void* descs, const int64_t* tile_start,
+                int64_t n_tiles, int64_t tile_points, const double* params, const void* domains,
+                int family, double* acc, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- grid rules: adjoint --------------------------------------------------- */
 
 size_t tq_grid_adjoint_workspace_size(int dim, int64_t total_points);

@@ -29,6 +29,7 @@ from .utils.set_up_backend import set_up_backend
 
 from . import integrands
 from . import batch
+from . import serving
 from .integrands import ExpSum, GaussianPeak, Oscillatory, SumSin, BuiltinIntegrand
 
 __all__ = [
@@ -53,6 +54,7 @@ __all__ = [
     "set_materialise_budget",
     "integrands",
     "batch",
+    "serving",
     "ExpSum",
     "GaussianPeak",
     "Oscillatory",

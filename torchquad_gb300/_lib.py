@@ -94,6 +94,11 @@ SIGNATURES = {
         [c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_void_p,
          c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_size_t, c_void_p],
     ),
+    "tq_batch_mc": (
+        c_int,
+        [c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_int, c_void_p,
+         c_void_p, c_size_t, c_void_p],
+    ),
     "tq_grid_points": (
         c_int,
         [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p],

@@ -189,3 +189,157 @@ extern "C" int tq_batch_grid(int dtype, int64_t n_integrals, const void* descs,
                                            out_dtype);
   return launch_status();
 }
+
+// ------------------------------------------------------ batched Monte Carlo
+// One chunk of points for each of many Monte Carlo integrations: request r
+// evaluates its points [first_r, first_r + count_r) of its own Philox stream
+// (seed_r, stream_r; point p uses the elements p*dim .. p*dim+dim-1, the
+// layout of tq_uniform) and adds sum f and sum f^2 to its running
+// compensated accumulators acc[r][0..3].  Tiles of tile_pts points;
+// per-tile partials are reduced in tile order, so a request's sums do not
+// depend on the other requests of the launch.
+
+namespace tq {
+
+struct McDesc {
+  int32_t dim, pad;
+  int64_t first, count;  // point range of this chunk
+  uint64_t seed, sid;
+  int64_t par_off, dom_off;
+};
+
+struct BatchMcArgs {
+  const McDesc* desc;
+  const int64_t* tile_start;
+  int64_t n_req, n_tiles, tile_pts;
+  const double* params;
+  const void* domains;
+  int family;
+  Acc* partials;  // [n_tiles][2]
+};
+
+template <typename T, int FAM>
+__global__ void __launch_bounds__(256) batch_mc_kernel(BatchMcArgs a) {
+  __shared__ Family<T> fam;
+  __shared__ T lo[kMaxDim], wid[kMaxDim];
+  __shared__ McDesc d;
+  __shared__ int64_t tile0;
+  constexpr int PB = Uniform<T>::per_block;
+  for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+    if (threadIdx.x == 0) {
+      int64_t l = 0, h = a.n_req;
+      while (h - l > 1) {
+        const int64_t m = (l + h) >> 1;
+        if (a.tile_start[m] <= tile) l = m;
+        else h = m;
+      }
+      d = a.desc[l];
+      tile0 = a.tile_start[l];
+      load_family<T>(fam, a.family, d.dim, a.params + d.par_off);
+      const T* dom = (const T*)a.domains + d.dom_off;
+      for (int k = 0; k < d.dim; ++k) {
+        lo[k] = dom[2 * k];
+        wid[k] = dom[2 * k + 1] - dom[2 * k];
+      }
+    }
+    __syncthreads();
+    const int dim = d.dim;
+    const int64_t begin = (tile - tile0) * a.tile_pts;
+    const int64_t end = min(d.count, begin + a.tile_pts);
+    Acc s1{0.0, 0.0}, s2{0.0, 0.0};
+    for (int64_t q = begin + threadIdx.x; q < end; q += blockDim.x) {
+      const uint64_t p = (uint64_t)(d.first + q);
+      const uint64_t e0 = p * (uint64_t)dim;
+      const uint64_t blk0 = e0 / PB;
+      const int lane0 = (int)(e0 % PB);
+      int cur = -1;
+      uint4 r = make_uint4(0, 0, 0, 0);
+      T s = T(0);
+      for (int k = 0; k < dim; ++k) {
+        const int le = lane0 + k, bi = le / PB;
+        if (bi != cur) {
+          r = philox_block(d.seed, d.sid, blk0 + (uint64_t)bi);
+          cur = bi;
+        }
+        const T u = Uniform<T>::from(r, le - bi * PB);
+        const T x = u * wid[k] + lo[k];
+        const T g = fam_term<FAM, T>(fam, k, x);
+        s = (k == 0) ? g : s + g;
+      }
+      const double f = (double)fam_outer<FAM, T>(fam, s);
+      acc_add(s1, f);
+      acc_add(s2, f * f);
+    }
+    s1 = block_reduce<256>(s1);
+    s2 = block_reduce<256>(s2);
+    if (threadIdx.x == 0) {
+      a.partials[2 * tile] = s1;
+      a.partials[2 * tile + 1] = s2;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void batch_mc_finalize_kernel(const int64_t* tile_start, int64_t n_req, const Acc* partials,
+                                         double* acc) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= n_req) return;
+  Acc s1{0.0, 0.0}, s2{0.0, 0.0};
+  for (int64_t t = tile_start[w] + lane; t < tile_start[w + 1]; t += 32) {
+    acc_merge(s1, partials[2 * t]);
+    acc_merge(s2, partials[2 * t + 1]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    acc_merge(s1, acc_shfl_down(s1, o));
+    acc_merge(s2, acc_shfl_down(s2, o));
+  }
+  if (lane == 0) {
+    Acc r1{acc[4 * w], acc[4 * w + 1]}, r2{acc[4 * w + 2], acc[4 * w + 3]};
+    acc_merge(r1, s1);
+    acc_merge(r2, s2);
+    acc[4 * w] = r1.s;
+    acc[4 * w + 1] = r1.c;
+    acc[4 * w + 2] = r2.s;
+    acc[4 * w + 3] = r2.c;
+  }
+}
+
+}  // namespace tq
+
+extern "C" int tq_batch_mc(int dtype, int64_t n_requests, const void* descs,
+                           const int64_t* tile_start, int64_t n_tiles, int64_t tile_points,
+                           const double* params, const void* domains, int family, double* acc,
+                           void* workspace, size_t workspace_bytes, void* stream) {
+  using namespace tq;
+  if (!valid_dtype(dtype)) return TQ_ERR_DTYPE;
+  if (n_requests < 1 || n_tiles < 1 || tile_points < 1 || !descs || !tile_start || !params ||
+      !domains || !acc || !workspace)
+    return TQ_ERR_ARG;
+  if (workspace_bytes < (size_t)n_tiles * 2 * sizeof(Acc)) return TQ_ERR_WORKSPACE;
+  BatchMcArgs a;
+  a.desc = (const McDesc*)descs;
+  a.tile_start = tile_start;
+  a.n_req = n_requests;
+  a.n_tiles = n_tiles;
+  a.tile_pts = tile_points;
+  a.params = params;
+  a.domains = domains;
+  a.family = family;
+  a.partials = (Acc*)workspace;
+  int64_t grid = (int64_t)sm_count() * 8;
+  if (grid > n_tiles) grid = n_tiles;
+  cudaStream_t s = (cudaStream_t)stream;
+  TQ_DISPATCH_FAMILY(family, FAM, {
+    if (dtype == TQ_F64)
+      batch_mc_kernel<double, FAM><<<(unsigned)grid, 256, 0, s>>>(a);
+    else
+      batch_mc_kernel<float, FAM><<<(unsigned)grid, 256, 0, s>>>(a);
+  });
+  int e = launch_status();
+  if (e != TQ_OK) return e;
+  batch_mc_finalize_kernel<<<(unsigned)((n_requests * 32 + 255) / 256), 256, 0, s>>>(
+      tile_start, n_requests, (const Acc*)workspace, acc);
+  return launch_status();
+}
