@@ -257,3 +257,38 @@ def test_peak_accuracy_reference_cases(cuda):
         assert abs(r - o) <= 1e-9 * abs(o)
         good += abs(r - ref2) < 0.03
     assert good >= 3
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_large_map_update_matches_oracle(dtype, cuda):
+    """Maps with more than 1024 intervals per dimension use block-wide scans."""
+    from oracle import vegas as OV
+
+    B, d = 5000, 2
+    rng = np.random.default_rng(4)
+    counts = rng.integers(1, 50, size=(d, B)).astype(np.int64)
+    weights = rng.uniform(0.1, 3.0, size=(d, B)) * counts
+    nd = np.float32 if dtype == torch.float32 else np.float64
+    m = OV.Map(B, d, nd)
+    m.weights = weights.astype(nd)
+    m.counts = counts.copy()
+    m.update_map()
+    dev = VegasDevice(d, dtype, B, 1, cuda)
+    dev.weights.copy_(torch.tensor(weights.astype(nd).astype(np.float64), device=cuda))
+    dev.counts.copy_(torch.tensor(counts, device=cuda))
+    dev.update_map(0.5)
+    got = dev.x_edges.double().cpu().numpy()
+    tol = 2e-5 if dtype == torch.float32 else 1e-10
+    assert np.max(np.abs(got - m.x_edges.astype(np.float64))) <= tol
+    assert int(dev.counts.abs().sum()) == 0  # reset after the update
+
+
+def test_default_interval_count_vegas(cuda):
+    """The reference's default map size (N_increment // 10 intervals) at a
+    size that takes the large-map path."""
+    f = tq.GaussianPeak.normal(3, 0.5, 0.1)
+    dom = torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float64, device=cuda)
+    v = tq.VEGAS()
+    r = v.integrate(f, 3, N=2_000_000, integration_domain=dom, seed=3)
+    assert v.map.N_intervals == 2_000_000 // 25 // 10
+    assert abs(r.item() - 1.0) < 5 * v._get_error() + 1e-3

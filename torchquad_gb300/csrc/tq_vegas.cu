@@ -559,6 +559,67 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
 // --------------------------------------------------------- map update
 // One CTA updates every dimension: the "all weights zero" test of
 // vegas_map.py:151-155 spans the whole map.
+// Block-wide inclusive prefix sum of a[0..n) in place: contiguous chunks per
+// thread, then a scan of the chunk totals.  (The large-map path only; the
+// small-map path sums sequentially like the reference.)
+__device__ void block_scan_inclusive(double* a, int64_t n, double* sh) {
+  const int nt = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int64_t per = (n + nt - 1) / nt;
+  const int64_t b0 = (int64_t)t * per, b1 = min(n, b0 + per);
+  double s = 0.0;
+  for (int64_t i = b0; i < b1; ++i) {
+    s += a[i];
+    a[i] = s;
+  }
+  double x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double v = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += v;
+  }
+  __syncthreads();
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    double y = lane < (nt >> 5) ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double v = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += v;
+    }
+    sh[lane] = y;
+  }
+  __syncthreads();
+  const double off = x - s + (warp > 0 ? sh[warp - 1] : 0.0);
+  for (int64_t i = b0; i < b1; ++i) a[i] += off;
+  __syncthreads();
+}
+
+// Block-wide sum (fp64), result in every thread.
+__device__ double block_sum_all(double v, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[i];
+  __syncthreads();
+  return t;
+}
+
+// First index in m[0..n) with m[i] >= key (m nondecreasing).
+__device__ __forceinline__ int64_t lower_bound_i32(const int32_t* m, int64_t n, int key) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (m[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
 // Bytes of the map-update working arrays (placed in shared memory when they
 // fit, else in the workspace).
 __host__ __device__ inline size_t map_work_bytes(int d, int64_t B, size_t tsize) {
@@ -568,8 +629,10 @@ __host__ __device__ inline size_t map_work_bytes(int d, int64_t B, size_t tsize)
   return off + DB1 * (8 + 8 + tsize) + 16;
 }
 
+constexpr int kSmallMap = 1024;  // intervals per dimension handled sequentially
+
 template <typename T>
-__global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state st, double alpha,
+__global__ void __launch_bounds__(1024) vegas_update_map_kernel(tq_vegas_state st, double alpha,
                                                                   double* scratch, int in_smem,
                                                                   void* smooth_out) {
   extern __shared__ __align__(16) unsigned char map_smem[];
@@ -619,8 +682,9 @@ __global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state
         break;
     }
   }
-  // row sums (:151): one warp per dimension
-  {
+  // row sums (:151): one warp per dimension, or the whole CTA for large maps
+  __shared__ double red[32];
+  if (B <= kSmallMap) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int k = warp; k < d; k += blockDim.x >> 5) {
       double acc = 0.0;
@@ -628,6 +692,13 @@ __global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
       if (lane == 0) sums[k] = (T)acc;
+    }
+  } else {
+    for (int k = 0; k < d; ++k) {
+      double acc = 0.0;
+      for (int64_t b = threadIdx.x; b < B; b += blockDim.x) acc += (double)w[k * B + b];
+      acc = block_sum_all(acc, red);
+      if (threadIdx.x == 0) sums[k] = (T)acc;
     }
   }
   __syncthreads();
@@ -672,6 +743,58 @@ __global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state
   // formula run in parallel.
   double* cumd = newx;          // [d][B+1]: fp64 cumulative sums, later new edges
   int32_t* mult = (int32_t*)w;  // [d][B]: delta multiples, later edge indices
+  if (B > kSmallMap) {
+    // Large maps: the same steps with block-wide scans; the per-multiple
+    // counts and the index prefix come from binary searches in the sorted
+    // multiples (ind[e] = #{b : mult[b] <= e}).
+    for (int k = 0; k < d; ++k) {
+      const T* sw = wtmp + k * B;
+      double tot = 0.0;
+      for (int64_t b = threadIdx.x; b < B; b += blockDim.x) tot += (double)sw[b];
+      tot = block_sum_all(tot, red);
+      const T delta = div_rn((T)tot, (T)B);  // :201
+      double* cd = cumd + k * (B + 1);
+      int32_t* mk = mult + k * B;
+      for (int64_t b = threadIdx.x; b < B - 1; b += blockDim.x) cd[b] = (double)sw[b];
+      __syncthreads();
+      block_scan_inclusive(cd, B - 1, red);  // :210-213
+      for (int64_t b = threadIdx.x; b < B - 1; b += blockDim.x) {
+        int64_t m = (int64_t)(cd[b] / (double)delta);
+        mk[b] = (int32_t)(m < 0 ? 0 : (m > B ? B : m));
+      }
+      __syncthreads();
+      T* vv = val + k * (B + 1);
+      int64_t* ind = idx + k * (B + 1);
+      for (int64_t m = threadIdx.x; m <= B; m += blockDim.x) {  // :214-230
+        const int64_t lo = lower_bound_i32(mk, B - 1, (int)m);
+        const int64_t hi = lower_bound_i32(mk, B - 1, (int)m + 1);
+        T acc = (T)0;
+        for (int64_t b = lo; b < hi; ++b) acc = add_rn(acc, sw[b]);
+        vv[m] = acc;
+        ind[m] = hi;
+      }
+      __syncthreads();
+      for (int64_t e = threadIdx.x; e < B - 1; e += blockDim.x) cd[e] = (double)sub_rn(delta, vv[e]);
+      __syncthreads();
+      block_scan_inclusive(cd, B - 1, red);  // :233
+      for (int64_t e = threadIdx.x; e < B - 1; e += blockDim.x) vv[e] = (T)cd[e];
+      __syncthreads();
+      const T* xe = (const T*)st.x_edges + k * (B + 1);
+      const T* dxe = (const T*)st.dx_edges + k * B;
+      for (int64_t e1 = threadIdx.x; e1 <= B; e1 += blockDim.x) {  // EQ 22
+        double nv;
+        if (e1 == 0 || e1 == B) {
+          nv = (double)xe[e1];
+        } else {
+          int64_t ii = ind[e1 - 1];
+          ii = ii < 0 ? 0 : (ii > B - 1 ? B - 1 : ii);
+          nv = (double)add_rn(xe[ii], mul_rn(div_rn(vv[e1 - 1], sw[ii]), dxe[ii]));
+        }
+        cd[e1] = nv;  // cumd row k becomes the new edges of row k
+      }
+      __syncthreads();
+    }
+  } else {
   {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int k = warp; k < d; k += blockDim.x >> 5) {  // :201 delta per dimension
@@ -737,10 +860,14 @@ __global__ void __launch_bounds__(kBlock) vegas_update_map_kernel(tq_vegas_state
     }
     newx[i] = nv;  // cumd is no longer needed
   }
+  }
   __syncthreads();
-  if (threadIdx.x < d) {
-    // :240-257: replace infinite edges by the mean of their (unrepaired)
-    // neighbours; val (no longer needed) holds the means
+  // :240-257: replace infinite edges by the mean of their (unrepaired)
+  // neighbours; val (no longer needed) holds the means.  The check is
+  // block-wide; the repair (rare) runs per dimension.
+  int any_bad = 0;
+  for (int64_t i = threadIdx.x; i < d * (B + 1); i += blockDim.x) any_bad |= !isfinite(newx[i]);
+  if (__syncthreads_or(any_bad) && threadIdx.x < d) {
     const int k = threadIdx.x;
     double* nx = newx + k * (B + 1);
     T* vv = val + k * (B + 1);
@@ -1072,7 +1199,8 @@ static int launch_update_map(const tq_vegas_state* st, double alpha, void* works
                                            (int)smem);                                        \
       if (e != cudaSuccess) return set_cuda_error(e);                                         \
     }                                                                                         \
-    kfn<<<1, kBlock, smem, s>>>(*st, alpha, ws.map_scratch, in_smem, smooth_out);             \
+    kfn<<<1, st->n_bins > kSmallMap ? 1024 : kBlock, smem, s>>>(*st, alpha, ws.map_scratch,   \
+                                                                in_smem, smooth_out);            \
   }
   if (st->dtype == TQ_F64)
     TQ_MAP_LAUNCH(double)
