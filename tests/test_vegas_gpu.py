@@ -261,26 +261,77 @@ def test_peak_accuracy_reference_cases(cuda):
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_large_map_update_matches_oracle(dtype, cuda):
-    """Maps with more than 1024 intervals per dimension use block-wide scans."""
+    """Maps with more than 1024 intervals per dimension use the tiled passes."""
     from oracle import vegas as OV
 
     B, d = 5000, 2
     rng = np.random.default_rng(4)
     counts = rng.integers(1, 50, size=(d, B)).astype(np.int64)
     weights = rng.uniform(0.1, 3.0, size=(d, B)) * counts
+    _check_large_map(OV, dtype, cuda, weights, counts)
+
+
+def _check_large_map(OV, dtype, cuda, weights, counts, tol32=2e-5):
+    d, B = counts.shape
     nd = np.float32 if dtype == torch.float32 else np.float64
     m = OV.Map(B, d, nd)
     m.weights = weights.astype(nd)
     m.counts = counts.copy()
-    m.update_map()
+    sw_ref = OV.Map.smooth_map(m.weights, m.counts, 0.5)
+    updated = m.update_map()
     dev = VegasDevice(d, dtype, B, 1, cuda)
     dev.weights.copy_(torch.tensor(weights.astype(nd).astype(np.float64), device=cuda))
     dev.counts.copy_(torch.tensor(counts, device=cuda))
+    x0 = dev.x_edges.double().cpu().numpy().copy()
+    sw = dev.smooth(0.5)
+    if sw_ref is not None:
+        tol_sw = 1e-5 if dtype == torch.float32 else 1e-12
+        assert np.max(np.abs(sw.double().cpu().numpy() - sw_ref) / np.abs(sw_ref).max()) <= tol_sw
+    f0 = int(dev.flags[0].item())
     dev.update_map(0.5)
     got = dev.x_edges.double().cpu().numpy()
-    tol = 2e-5 if dtype == torch.float32 else 1e-10
-    assert np.max(np.abs(got - m.x_edges.astype(np.float64))) <= tol
+    if updated:
+        tol = tol32 if dtype == torch.float32 else 1e-10
+        assert np.max(np.abs(got - m.x_edges.astype(np.float64))) <= tol
+        assert np.all(np.diff(got, axis=1) > 0)
+        dx = dev.dx_edges.double().cpu().numpy()
+        assert np.max(np.abs(dx - np.diff(got, axis=1))) <= (1e-6 if dtype == torch.float32 else 1e-14)
+    else:
+        assert np.array_equal(got, x0)  # the map cannot be updated: edges stay
+        assert int(dev.flags[0].item()) == f0 + 1
     assert int(dev.counts.abs().sum()) == 0  # reset after the update
+    assert float(dev.weights.abs().sum()) == 0.0
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("case", ["zeros", "peaked", "zero_row"])
+def test_large_map_cases_match_oracle(case, dtype, cuda):
+    """Tiled map update: empty intervals filled across tile boundaries and
+    beyond ten neighbours, concentrated weights (long runs of equal delta
+    multiples, multiples that skip), and a row without weight (map reset)."""
+    from oracle import vegas as OV
+
+    rng = np.random.default_rng({"zeros": 5, "peaked": 6, "zero_row": 7}[case])
+    d, B = (5, 40000) if case != "zero_row" else (3, 3000)
+    counts = rng.integers(1, 20, size=(d, B)).astype(np.int64)
+    weights = rng.uniform(0.1, 3.0, size=(d, B)) * counts
+    if case == "zeros":
+        z = rng.random((d, B)) < 0.3
+        z[:, 2040:2065] = True  # a run of 25 across the first tile boundary
+        z[:, :12] = True
+        z[:, -13:] = True
+        z[0, 10000:10003] = True
+        counts[z] = 0
+        weights[z] = 0.0
+    elif case == "peaked":
+        x = (np.arange(B) + 0.5) / B
+        for k in range(d):
+            peak = np.exp(-(((x - rng.uniform(0.2, 0.8)) / 0.01) ** 2)) + 1e-7
+            weights[k] = peak * counts[k]
+    else:
+        counts[1] = 0
+        weights[1] = 0.0
+    _check_large_map(OV, dtype, cuda, weights, counts, tol32=5e-5)
 
 
 def test_default_interval_count_vegas(cuda):

@@ -609,17 +609,6 @@ __device__ double block_sum_all(double v, double* sh) {
   return t;
 }
 
-// First index in m[0..n) with m[i] >= key (m nondecreasing).
-__device__ __forceinline__ int64_t lower_bound_i32(const int32_t* m, int64_t n, int key) {
-  int64_t lo = 0, hi = n;
-  while (lo < hi) {
-    const int64_t mid = (lo + hi) >> 1;
-    if (m[mid] < key) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
 // Bytes of the map-update working arrays (placed in shared memory when they
 // fit, else in the workspace).
 __host__ __device__ inline size_t map_work_bytes(int d, int64_t B, size_t tsize) {
@@ -682,9 +671,8 @@ __global__ void __launch_bounds__(1024) vegas_update_map_kernel(tq_vegas_state s
         break;
     }
   }
-  // row sums (:151): one warp per dimension, or the whole CTA for large maps
-  __shared__ double red[32];
-  if (B <= kSmallMap) {
+  // row sums (:151): one warp per dimension
+  {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int k = warp; k < d; k += blockDim.x >> 5) {
       double acc = 0.0;
@@ -692,13 +680,6 @@ __global__ void __launch_bounds__(1024) vegas_update_map_kernel(tq_vegas_state s
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
       if (lane == 0) sums[k] = (T)acc;
-    }
-  } else {
-    for (int k = 0; k < d; ++k) {
-      double acc = 0.0;
-      for (int64_t b = threadIdx.x; b < B; b += blockDim.x) acc += (double)w[k * B + b];
-      acc = block_sum_all(acc, red);
-      if (threadIdx.x == 0) sums[k] = (T)acc;
     }
   }
   __syncthreads();
@@ -743,58 +724,6 @@ __global__ void __launch_bounds__(1024) vegas_update_map_kernel(tq_vegas_state s
   // formula run in parallel.
   double* cumd = newx;          // [d][B+1]: fp64 cumulative sums, later new edges
   int32_t* mult = (int32_t*)w;  // [d][B]: delta multiples, later edge indices
-  if (B > kSmallMap) {
-    // Large maps: the same steps with block-wide scans; the per-multiple
-    // counts and the index prefix come from binary searches in the sorted
-    // multiples (ind[e] = #{b : mult[b] <= e}).
-    for (int k = 0; k < d; ++k) {
-      const T* sw = wtmp + k * B;
-      double tot = 0.0;
-      for (int64_t b = threadIdx.x; b < B; b += blockDim.x) tot += (double)sw[b];
-      tot = block_sum_all(tot, red);
-      const T delta = div_rn((T)tot, (T)B);  // :201
-      double* cd = cumd + k * (B + 1);
-      int32_t* mk = mult + k * B;
-      for (int64_t b = threadIdx.x; b < B - 1; b += blockDim.x) cd[b] = (double)sw[b];
-      __syncthreads();
-      block_scan_inclusive(cd, B - 1, red);  // :210-213
-      for (int64_t b = threadIdx.x; b < B - 1; b += blockDim.x) {
-        int64_t m = (int64_t)(cd[b] / (double)delta);
-        mk[b] = (int32_t)(m < 0 ? 0 : (m > B ? B : m));
-      }
-      __syncthreads();
-      T* vv = val + k * (B + 1);
-      int64_t* ind = idx + k * (B + 1);
-      for (int64_t m = threadIdx.x; m <= B; m += blockDim.x) {  // :214-230
-        const int64_t lo = lower_bound_i32(mk, B - 1, (int)m);
-        const int64_t hi = lower_bound_i32(mk, B - 1, (int)m + 1);
-        T acc = (T)0;
-        for (int64_t b = lo; b < hi; ++b) acc = add_rn(acc, sw[b]);
-        vv[m] = acc;
-        ind[m] = hi;
-      }
-      __syncthreads();
-      for (int64_t e = threadIdx.x; e < B - 1; e += blockDim.x) cd[e] = (double)sub_rn(delta, vv[e]);
-      __syncthreads();
-      block_scan_inclusive(cd, B - 1, red);  // :233
-      for (int64_t e = threadIdx.x; e < B - 1; e += blockDim.x) vv[e] = (T)cd[e];
-      __syncthreads();
-      const T* xe = (const T*)st.x_edges + k * (B + 1);
-      const T* dxe = (const T*)st.dx_edges + k * B;
-      for (int64_t e1 = threadIdx.x; e1 <= B; e1 += blockDim.x) {  // EQ 22
-        double nv;
-        if (e1 == 0 || e1 == B) {
-          nv = (double)xe[e1];
-        } else {
-          int64_t ii = ind[e1 - 1];
-          ii = ii < 0 ? 0 : (ii > B - 1 ? B - 1 : ii);
-          nv = (double)add_rn(xe[ii], mul_rn(div_rn(vv[e1 - 1], sw[ii]), dxe[ii]));
-        }
-        cd[e1] = nv;  // cumd row k becomes the new edges of row k
-      }
-      __syncthreads();
-    }
-  } else {
   {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int k = warp; k < d; k += blockDim.x >> 5) {  // :201 delta per dimension
@@ -860,7 +789,6 @@ __global__ void __launch_bounds__(1024) vegas_update_map_kernel(tq_vegas_state s
     }
     newx[i] = nv;  // cumd is no longer needed
   }
-  }
   __syncthreads();
   // :240-257: replace infinite edges by the mean of their (unrepaired)
   // neighbours; val (no longer needed) holds the means.  The check is
@@ -896,6 +824,418 @@ __global__ void __launch_bounds__(1024) vegas_update_map_kernel(tq_vegas_state s
     ((T*)st.dx_edges)[i] = sub_rn(xe[b + 1], xe[b]);  // :259
     st.weights[i] = 0.0;
     st.counts[i] = 0;
+  }
+}
+
+// ------------------------------------------------ map update, large maps
+// Maps of more than kSmallMap intervals per dimension (the reference's
+// default N_increment // 10 intervals at large N): the update of
+// vegas_map.py:114-260 as seven grid-wide passes over tiles of kMapTile
+// intervals, grid (tiles, dimensions), so every SM takes part.  Stream order
+// is the only grid-wide synchronisation.  Tile sums and tile prefixes are
+// combined by the last CTA of a pass (ticket) in tile order, so results do
+// not depend on CTA scheduling, and no CTA waits for another.
+constexpr int kMapThreads = 256;
+constexpr int kMapPer = 8;                       // consecutive intervals per thread
+constexpr int kMapTile = kMapThreads * kMapPer;  // intervals per CTA
+constexpr int kFillHalo = 16;  // 10 fill sweeps move values at most 10 intervals
+
+inline int64_t map_tiles(int64_t B) { return (B + kMapTile - 1) / kMapTile; }
+
+struct MapTiles {
+  void* wf;       // [d][B]   T: averaged and filled weights (EQ 17)
+  void* sw;       // [d][B]   T: smoothed weights (EQ 18-19)
+  int32_t* mk;    // [d][B]   delta multiples of the fp64 cumulative sums
+  int32_t* ind;   // [d][B+1] old interval index per new inner edge
+  void* vv;       // [d][B+1] T: smoothed-weight sums per multiple
+  void* newx;     // [d][B+1] T: new edges before the infinite-edge repair
+  double* part;   // [d][nt]  tile sums
+  double* pre;    // [d][nt]  exclusive tile prefixes
+  double* row;    // [2][kMaxDim] row sums, deltas (T values)
+  int* zero;      // some row of weights sums to zero: the map is reset
+  size_t total;
+};
+
+static MapTiles map_tile_layout(const tq_vegas_state* st, void* base) {
+  MapTiles m;
+  const int64_t d = st->dim, B = st->n_bins, nt = map_tiles(B);
+  const size_t ts = dtype_size(st->dtype);
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  char* p = (char*)base;
+  size_t off = 0;
+  m.wf = p + off;   off += al(d * B * ts);
+  m.sw = p + off;   off += al(d * B * ts);
+  m.mk = (int32_t*)(p + off);  off += al(d * B * 4);
+  m.ind = (int32_t*)(p + off); off += al(d * (B + 1) * 4);
+  m.vv = p + off;   off += al(d * (B + 1) * ts);
+  m.newx = p + off; off += al(d * (B + 1) * ts);
+  m.part = (double*)(p + off); off += al(d * nt * 8);
+  m.pre = (double*)(p + off);  off += al(d * nt * 8);
+  m.row = (double*)(p + off);  off += al(2 * kMaxDim * 8);
+  m.zero = (int*)(p + off);    off += 256;
+  m.total = off;
+  return m;
+}
+
+// Exclusive scan of one value per thread across the CTA (fixed order).
+__device__ __forceinline__ double cta_exclusive_scan(double x, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double xi = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double v = __shfl_up_sync(0xffffffffu, xi, o);
+    if (lane >= o) xi += v;
+  }
+  double ex = __shfl_up_sync(0xffffffffu, xi, 1);
+  if (lane == 0) ex = 0.0;
+  __syncthreads();
+  if (lane == 31) sh[warp] = xi;
+  __syncthreads();
+  if (warp == 0) {
+    double y = lane < nw ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double v = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += v;
+    }
+    double yx = __shfl_up_sync(0xffffffffu, y, 1);
+    if (lane == 0) yx = 0.0;
+    sh[lane] = yx;  // exclusive warp offsets
+  }
+  __syncthreads();
+  const double r = sh[warp] + ex;
+  __syncthreads();
+  return r;
+}
+
+// Last CTA of a pass: per dimension, exclusive prefixes of the tile sums in
+// tile order (one warp per dimension) and the row total.
+__device__ void tile_prefixes(double* part, double* pre, double* total, int d, int64_t nt) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = warp; k < d; k += nw) {
+    double carry = 0.0;
+    for (int64_t c0 = 0; c0 < nt; c0 += 32) {
+      const double v = c0 + lane < nt ? __ldcg(part + k * nt + c0 + lane) : 0.0;
+      double xi = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double u = __shfl_up_sync(0xffffffffu, xi, o);
+        if (lane >= o) xi += u;
+      }
+      double ex = __shfl_up_sync(0xffffffffu, xi, 1);
+      if (lane == 0) ex = 0.0;
+      if (pre && c0 + lane < nt) pre[k * nt + c0 + lane] = carry + ex;
+      carry += __shfl_sync(0xffffffffu, xi, 31);
+    }
+    if (lane == 0) total[k] = carry;
+  }
+}
+
+// Pass 1 (EQ 17, :118-145): averages, filling of empty intervals from their
+// neighbours (10 sweeps on the tile plus a halo; once no empty interval is
+// left a sweep changes nothing, so the reference's early exit needs no
+// grid-wide test), tile sums; the last CTA forms the row sums and the
+// zero-row test of :151-155.
+template <typename T>
+__global__ void __launch_bounds__(kMapThreads) map_fill_kernel(tq_vegas_state st, MapTiles m,
+                                                                unsigned* ticket) {
+  constexpr int E = kMapTile + 2 * kFillHalo;
+  __shared__ T w_s[E], wt_s[E];
+  __shared__ unsigned char z_s[E], zt_s[E];
+  __shared__ double red[32];
+  const int k = blockIdx.y;
+  const int64_t B = st.n_bins, nt = gridDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * kMapTile, e0 = t0 - kFillHalo;
+  int anyz = 0;
+  for (int i = threadIdx.x; i < E; i += blockDim.x) {
+    const int64_t b = e0 + i;
+    T wv = (T)0;
+    unsigned char zv = 0;
+    if (b >= 0 && b < B) {
+      const int64_t c = st.counts[k * B + b];
+      const T wi = (T)st.weights[k * B + b];
+      zv = c == 0;
+      wv = c == 0 ? wi : div_rn(wi, (T)c);
+    }
+    w_s[i] = wv;
+    z_s[i] = zv;
+    anyz |= zv;
+  }
+  if (__syncthreads_or(anyz)) {
+    for (int sweep = 0; sweep < 10; ++sweep) {
+      for (int i = threadIdx.x; i < E; i += blockDim.x) {
+        const bool right = e0 + i < B - 1 && i + 1 < E;
+        wt_s[i] = (right && z_s[i]) ? w_s[i + 1] : w_s[i];
+        zt_s[i] = right ? (z_s[i] && z_s[i + 1]) : z_s[i];
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < E; i += blockDim.x) {
+        const bool left = e0 + i > 0 && i > 0;
+        w_s[i] = (left && zt_s[i]) ? wt_s[i - 1] : wt_s[i];
+        z_s[i] = left ? (zt_s[i] && zt_s[i - 1]) : zt_s[i];
+      }
+      __syncthreads();
+    }
+  }
+  T* wf = (T*)m.wf + k * B;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < kMapTile; i += blockDim.x) {
+    const int64_t b = t0 + i;
+    if (b < B) {
+      const T v = w_s[kFillHalo + i];
+      wf[b] = v;
+      acc += (double)v;
+    }
+  }
+  acc = block_sum_all(acc, red);
+  if (threadIdx.x == 0) m.part[k * nt + blockIdx.x] = acc;
+  if (last_block_arrives(ticket)) {
+    __threadfence();
+    tile_prefixes(m.part, nullptr, m.row, st.dim, nt);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int z = 0;
+      for (int kk = 0; kk < st.dim; ++kk) {
+        const T s = (T)m.row[kk];
+        m.row[kk] = (double)s;
+        z |= s == (T)0;
+      }
+      *m.zero = z;
+      *ticket = 0u;
+    }
+  }
+}
+
+// Pass 2 (EQ 18-19): smoothing and range compression; tile sums of the
+// smoothed weights without the last interval (the fp64 cumulative sum of
+// :210-213 runs over sw[:-1]); the last CTA forms the tile prefixes and
+// delta = sum(sw) / B (:201).  smooth_only: _smooth_map alone (the result
+// goes to sw, which then is the caller's buffer).
+template <typename T>
+__global__ void __launch_bounds__(kMapThreads) map_smooth_kernel(tq_vegas_state st, MapTiles m, double alpha,
+                                                                  int smooth_only, unsigned* ticket) {
+  __shared__ double red[32];
+  if (*m.zero) {
+    if (smooth_only && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
+    return;
+  }
+  const int k = blockIdx.y;
+  const int64_t B = st.n_bins, nt = gridDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * kMapTile;
+  const T* r = (const T*)m.wf + k * B;
+  T* sw = (T*)m.sw + k * B;
+  const T sum = (T)m.row[k];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < kMapTile; i += blockDim.x) {
+    const int64_t b = t0 + i;
+    if (b >= B) break;
+    T v;
+    if (b == 0)
+      v = add_rn(mul_rn((T)7, r[0]), r[1]);
+    else if (b == B - 1)
+      v = add_rn(r[B - 2], mul_rn((T)7, r[B - 1]));
+    else
+      v = add_rn(add_rn(r[b - 1], mul_rn((T)6, r[b])), r[b + 1]);
+    v = div_rn(v, mul_rn((T)8, sum));
+    if (v != (T)0) {
+      const T t = div_rn(sub_rn(v, (T)1), log(v));
+      v = alpha == 0.5 ? sqrt(t) : pow(t, (T)alpha);
+    }
+    sw[b] = v;
+    if (b < B - 1) acc += (double)v;
+  }
+  if (smooth_only) return;
+  acc = block_sum_all(acc, red);
+  if (threadIdx.x == 0) m.part[k * nt + blockIdx.x] = acc;
+  if (last_block_arrives(ticket)) {
+    __threadfence();
+    tile_prefixes(m.part, m.pre, m.row + kMaxDim, st.dim, nt);
+    __syncthreads();
+    if (threadIdx.x < st.dim) {
+      const int kk = threadIdx.x;
+      const double tot = m.row[kMaxDim + kk] + (double)__ldcg((const T*)m.sw + kk * B + B - 1);
+      m.row[kMaxDim + kk] = (double)div_rn((T)tot, (T)B);
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+  }
+}
+
+// Pass 3 (:210-213): fp64 cumulative sums of sw[:-1] (tile prefix + scan in
+// the tile) divided by delta: the multiples; clears the per-multiple arrays.
+template <typename T>
+__global__ void __launch_bounds__(kMapThreads) map_multiples_kernel(tq_vegas_state st, MapTiles m) {
+  __shared__ double red[32];
+  if (*m.zero) return;
+  const int k = blockIdx.y;
+  const int64_t B = st.n_bins, nt = gridDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * kMapTile;
+  const T* sw = (const T*)m.sw + k * B;
+  const double delta = m.row[kMaxDim + k];
+  const int64_t b0 = t0 + (int64_t)threadIdx.x * kMapPer;
+  T v[kMapPer];
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < kMapPer; ++j) {
+    v[j] = b0 + j < B - 1 ? sw[b0 + j] : (T)0;
+    s += (double)v[j];
+  }
+  double cum = m.pre[k * nt + blockIdx.x] + cta_exclusive_scan(s, red);
+  int32_t* mk = m.mk + k * B;
+#pragma unroll
+  for (int j = 0; j < kMapPer; ++j) {
+    if (b0 + j < B - 1) {
+      cum += (double)v[j];
+      const int64_t q = (int64_t)(cum / delta);
+      mk[b0 + j] = (int32_t)(q < 0 ? 0 : (q > B ? B : q));
+    }
+  }
+  T* vv = (T*)m.vv + k * (B + 1);
+  int32_t* ind = m.ind + k * (B + 1);
+  for (int i = threadIdx.x; i < kMapTile; i += blockDim.x) {
+    const int64_t e = t0 + i;
+    if (e < B) {
+      vv[e] = (T)0;
+      ind[e] = 0;
+    }
+  }
+  if (blockIdx.x == nt - 1 && threadIdx.x == 0) {
+    vv[B] = (T)0;
+    ind[B] = 0;
+  }
+}
+
+// Pass 4 (:214-230) from the runs of equal multiples (mk nondecreasing):
+// ind[e] = #{b : mk[b] <= e}, which is b for e in [mk[b-1], mk[b]), and
+// vv[q] = the sequential sum (in T, as the reference's scatter-add) of sw
+// over the run of multiple q.
+template <typename T>
+__global__ void __launch_bounds__(kMapThreads) map_runs_kernel(tq_vegas_state st, MapTiles m) {
+  if (*m.zero) return;
+  const int k = blockIdx.y;
+  const int64_t B = st.n_bins;
+  const int64_t t0 = (int64_t)blockIdx.x * kMapTile;
+  const int32_t* mk = m.mk + k * B;
+  const T* sw = (const T*)m.sw + k * B;
+  T* vv = (T*)m.vv + k * (B + 1);
+  int32_t* ind = m.ind + k * (B + 1);
+  for (int i = threadIdx.x; i < kMapTile; i += blockDim.x) {
+    const int64_t b = t0 + i;
+    if (b >= B) break;
+    const int64_t from = b == 0 ? 0 : mk[b - 1];
+    const int64_t to = b == B - 1 ? B + 1 : mk[b];
+    for (int64_t e = from; e < to; ++e) ind[e] = (int32_t)b;
+    if (b < B - 1 && (b == 0 || mk[b] != mk[b - 1])) {
+      const int32_t q = mk[b];
+      T a = (T)0;
+      for (int64_t e = b; e < B - 1 && mk[e] == q; ++e) a = add_rn(a, sw[e]);
+      vv[q] = a;
+    }
+  }
+}
+
+// Pass 5 (:233): tile sums of delta - vv[e] over e < B - 1; the last CTA
+// forms the tile prefixes of the fp64 cumulative sum.
+template <typename T>
+__global__ void __launch_bounds__(kMapThreads) map_accu_sums_kernel(tq_vegas_state st, MapTiles m,
+                                                                     unsigned* ticket) {
+  __shared__ double red[32];
+  if (*m.zero) return;
+  const int k = blockIdx.y;
+  const int64_t B = st.n_bins, nt = gridDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * kMapTile;
+  const T delta = (T)m.row[kMaxDim + k];
+  const T* vv = (const T*)m.vv + k * (B + 1);
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < kMapTile; i += blockDim.x) {
+    const int64_t e = t0 + i;
+    if (e < B - 1) acc += (double)sub_rn(delta, vv[e]);
+  }
+  acc = block_sum_all(acc, red);
+  if (threadIdx.x == 0) m.part[k * nt + blockIdx.x] = acc;
+  if (last_block_arrives(ticket)) {
+    __threadfence();
+    tile_prefixes(m.part, m.pre, m.row, st.dim, nt);  // row sums are no longer needed
+    __syncthreads();
+    if (threadIdx.x == 0) *ticket = 0u;
+  }
+}
+
+// Pass 6 (:233-238, EQ 22): d_accu (fp64 cumulative sum rounded to T per
+// element, as torch's CPU cumsum) and the new inner edges.
+template <typename T>
+__global__ void __launch_bounds__(kMapThreads) map_edges_kernel(tq_vegas_state st, MapTiles m) {
+  __shared__ double red[32];
+  if (*m.zero) return;
+  const int k = blockIdx.y;
+  const int64_t B = st.n_bins, nt = gridDim.x;
+  const int64_t t0 = (int64_t)blockIdx.x * kMapTile;
+  const T delta = (T)m.row[kMaxDim + k];
+  const T* vv = (const T*)m.vv + k * (B + 1);
+  const T* sw = (const T*)m.sw + k * B;
+  const int32_t* ind = m.ind + k * (B + 1);
+  const T* xe = (const T*)st.x_edges + k * (B + 1);
+  const T* dxe = (const T*)st.dx_edges + k * B;
+  T* nx = (T*)m.newx + k * (B + 1);
+  const int64_t e0 = t0 + (int64_t)threadIdx.x * kMapPer;
+  double x[kMapPer];
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < kMapPer; ++j) {
+    x[j] = e0 + j < B - 1 ? (double)sub_rn(delta, vv[e0 + j]) : 0.0;
+    s += x[j];
+  }
+  double cum = m.pre[k * nt + blockIdx.x] + cta_exclusive_scan(s, red);
+#pragma unroll
+  for (int j = 0; j < kMapPer; ++j) {
+    const int64_t e = e0 + j;
+    if (e < B - 1) {
+      cum += x[j];
+      const T da = (T)cum;
+      int64_t ii = ind[e];
+      ii = ii < 0 ? 0 : (ii > B - 1 ? B - 1 : ii);
+      nx[e + 1] = add_rn(xe[ii], mul_rn(div_rn(da, sw[ii]), dxe[ii]));
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    nx[0] = xe[0];
+    nx[B] = xe[B];
+  }
+}
+
+// Pass 7 (:239-262): infinite edges replaced by the mean of their two
+// (unrepaired) neighbours, new edges and widths stored, weights and counts
+// reset; or, for a map that cannot be updated, only the reset.
+template <typename T>
+__global__ void __launch_bounds__(kMapThreads) map_commit_kernel(tq_vegas_state st, MapTiles m) {
+  const int k = blockIdx.y;
+  const int64_t B = st.n_bins;
+  const int64_t t0 = (int64_t)blockIdx.x * kMapTile;
+  const bool reset_only = *m.zero != 0;
+  if (reset_only && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
+  const T* nx = (const T*)m.newx + k * (B + 1);
+  T* xe = (T*)st.x_edges + k * (B + 1);
+  T* dxe = (T*)st.dx_edges + k * B;
+  auto fixed = [&](int64_t e, bool count) -> T {
+    T v = nx[e];
+    if (!isfinite((double)v)) {
+      if (count) atomicAdd(st.flags + 1, 1);
+      if (e > 0 && e < B) v = mul_rn((T)0.5, add_rn(nx[e - 1], nx[e + 1]));
+      if (count && !isfinite((double)v)) atomicAdd(st.flags + 2, 1);
+    }
+    return v;
+  };
+  for (int i = threadIdx.x; i < kMapTile; i += blockDim.x) {
+    const int64_t b = t0 + i;
+    if (b >= B) break;
+    if (!reset_only) {
+      const T lo = fixed(b, true);
+      const T hi = fixed(b + 1, b == B - 1);
+      xe[b] = lo;
+      if (b == B - 1) xe[B] = hi;
+      dxe[b] = sub_rn(hi, lo);
+    }
+    st.weights[k * B + b] = 0.0;
+    st.counts[k * B + b] = 0;
   }
 }
 
@@ -1054,6 +1394,7 @@ static int64_t finish_blocks(const tq_vegas_state* st) {
   return need < cap ? need : cap;
 }
 static size_t map_scratch_bytes(const tq_vegas_state* st) {
+  if (st->n_bins > kSmallMap) return map_tile_layout(st, nullptr).total;
   return map_work_bytes(st->dim, st->n_bins, 8);
 }
 
@@ -1063,6 +1404,7 @@ struct VegasWs {
   unsigned* t_sample;
   unsigned* t_nh;
   unsigned* t_finish;
+  unsigned* t_map;
   int64_t* block_tot;
   Acc* partials;
   double* map_scratch;
@@ -1075,6 +1417,7 @@ static VegasWs vegas_ws(const tq_vegas_state* st, void* base) {
   w.t_sample = (unsigned*)(p + 0);
   w.t_nh = (unsigned*)(p + 16);
   w.t_finish = (unsigned*)(p + 32);
+  w.t_map = (unsigned*)(p + 64);  // three tickets, 16 bytes apart
   size_t off = 256;
   w.block_tot = (int64_t*)(p + off);
   off += al(sizeof(int64_t) * (size_t)nh_blocks(st));
@@ -1188,6 +1531,30 @@ extern "C" int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, cons
 static int launch_update_map(const tq_vegas_state* st, double alpha, void* workspace,
                              size_t workspace_bytes, void* smooth_out, void* stream) {
   TQ_VEGAS_WS();
+  if (st->n_bins > kSmallMap) {
+    MapTiles m = map_tile_layout(st, ws.map_scratch);
+    if (smooth_out) m.sw = smooth_out;
+    const dim3 g((unsigned)map_tiles(st->n_bins), (unsigned)st->dim);
+    const int sm_only = smooth_out ? 1 : 0;
+#define TQ_TILED_MAP(T)                                                                 \
+  {                                                                                     \
+    map_fill_kernel<T><<<g, kMapThreads, 0, s>>>(*st, m, ws.t_map);                     \
+    map_smooth_kernel<T><<<g, kMapThreads, 0, s>>>(*st, m, alpha, sm_only, ws.t_map + 4); \
+    if (!sm_only) {                                                                     \
+      map_multiples_kernel<T><<<g, kMapThreads, 0, s>>>(*st, m);                        \
+      map_runs_kernel<T><<<g, kMapThreads, 0, s>>>(*st, m);                             \
+      map_accu_sums_kernel<T><<<g, kMapThreads, 0, s>>>(*st, m, ws.t_map + 8);          \
+      map_edges_kernel<T><<<g, kMapThreads, 0, s>>>(*st, m);                            \
+      map_commit_kernel<T><<<g, kMapThreads, 0, s>>>(*st, m);                           \
+    }                                                                                   \
+  }
+    if (st->dtype == TQ_F64)
+      TQ_TILED_MAP(double)
+    else
+      TQ_TILED_MAP(float)
+#undef TQ_TILED_MAP
+    return launch_status();
+  }
   const size_t bytes = map_work_bytes(st->dim, st->n_bins, dtype_size(st->dtype));
   const int in_smem = bytes <= 160 * 1024;
   const size_t smem = in_smem ? bytes : 0;
@@ -1199,7 +1566,7 @@ static int launch_update_map(const tq_vegas_state* st, double alpha, void* works
                                            (int)smem);                                        \
       if (e != cudaSuccess) return set_cuda_error(e);                                         \
     }                                                                                         \
-    kfn<<<1, st->n_bins > kSmallMap ? 1024 : kBlock, smem, s>>>(*st, alpha, ws.map_scratch,   \
+    kfn<<<1, kBlock, smem, s>>>(*st, alpha, ws.map_scratch,                                   \
                                                                 in_smem, smooth_out);            \
   }
   if (st->dtype == TQ_F64)

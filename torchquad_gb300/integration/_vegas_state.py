@@ -111,14 +111,19 @@ class VegasDevice:
         p, n = self._ws()
         L.check(L.lib().tq_vegas_update_map(self.ref, float(alpha), p, n, L.stream_handle()),
                 "tq_vegas_update_map")
-        L.count_launches(1)
+        L.count_launches(self.update_map_launches)
+
+    @property
+    def update_map_launches(self):
+        # maps of more than 1024 intervals per dimension: seven tiled passes
+        return 7 if self.n_bins > 1024 else 1
 
     def smooth(self, alpha):
         out = torch.empty((self.dim, self.n_bins), dtype=self.dtype, device=self.device)
         p, n = self._ws()
         L.check(L.lib().tq_vegas_smooth_weights(self.ref, float(alpha), out.data_ptr(), p, n,
                                                 L.stream_handle()), "tq_vegas_smooth_weights")
-        L.count_launches(1)
+        L.count_launches(2 if self.n_bins > 1024 else 1)
         return out
 
     def get_nh(self, nevals_exp=None, normalize=None):

@@ -97,14 +97,15 @@ class _FusedPlan:
             self.g_block = self._capture(self._block_seq)
         if self.g_warm is not None and not FORCE_EAGER[0]:
             self.g_warm.replay()
-            L.count_launches(1 + (5 * (2 if self.ns > 0 else 1) if self.use_warmup else 0))
+            L.count_launches(1 + (5 * ((1 if self.ns > 0 else 0) + self.dev.update_map_launches)
+                                  if self.use_warmup else 0))
         else:
             self._warm_seq()
 
     def run_block(self):
         if self.g_block is not None and not FORCE_EAGER[0]:
             self.g_block.replay()
-            L.count_launches(5 * (4 + (1 if self.use_grid_improve else 0)))
+            L.count_launches(5 * (4 + (self.dev.update_map_launches if self.use_grid_improve else 0)))
         else:
             self._block_seq()
 

@@ -40,7 +40,7 @@ from . import _lib as L
 from .batch import BatchedGrid
 from .integrands import BuiltinIntegrand
 from .integration._vegas_state import VegasDevice, n_strat_for
-from .integration.vegas import ALPHA, BETA, VEGAS
+from .integration.vegas import ALPHA, BETA, VEGAS, _graphs_enabled
 
 MC_DESC = np.dtype([("dim", "<i4"), ("pad", "<i4"), ("first", "<i8"), ("count", "<i8"), ("seed", "<u8"),
                     ("sid", "<u8"), ("par_off", "<i8"), ("dom_off", "<i8")])
@@ -124,6 +124,7 @@ class _VegasSession:
             self.dev.set_control(L.TQ_VC_NEVALS | L.TQ_VC_SEED | L.TQ_VC_STREAM, nevals=v._starting_N,
                                  seed=req.seed, sid=0)
         self.host = torch.empty((32 * 4 + 8,), dtype=torch.float64, pin_memory=True)
+        self.graph = None
         self.event = None
         self.warm_evals = 5 * (v._starting_N // 5)
         self.started = False
@@ -140,15 +141,35 @@ class _VegasSession:
                 self.started = True
             else:
                 d.set_control(L.TQ_VC_NEVALS, nevals=v._starting_N)
-            for _ in range(5):
-                d.get_nh()
-                d.iterate_fused(self.req.integrand.family, self.params, True)
-                d.finish(BETA)
-                d.update_map(ALPHA)
+            # The block reads its evaluation count, statistics slot and RNG
+            # offset from the control block, so the session captures it once
+            # (on its own stream, without a device synchronisation) and
+            # replays the graph for every block.
+            if self.graph is None and _graphs_enabled():
+                g = torch.cuda.CUDAGraph()
+                g.capture_begin(capture_error_mode="thread_local")
+                try:
+                    self._block()
+                finally:
+                    g.capture_end()
+                self.graph = g
+            if self.graph is not None:
+                self.graph.replay()
+                L.count_launches(5 * (4 + d.update_map_launches))
+            else:
+                self._block()
             v.it += 5
             self.host[: 32 * 4].copy_(d.stats.reshape(-1)[: 32 * 4], non_blocking=True)
             self.event = torch.cuda.Event()
             self.event.record(self.stream)
+
+    def _block(self):
+        d = self.dev
+        for _ in range(5):
+            d.get_nh()
+            d.iterate_fused(self.req.integrand.family, self.params, True)
+            d.finish(BETA)
+            d.update_map(ALPHA)
 
     def done(self):
         """After the block's event: True if the request is finished."""
@@ -195,6 +216,7 @@ class IntegrationServer:
         self._stream_rr = itertools.cycle(self._vegas_streams)
         self._thread = None
         self._active = 0
+        self.host_launch_s = 0.0  # scheduler time spent issuing device work
 
     # ---------------------------------------------------------------- API
     def start(self):
@@ -260,6 +282,7 @@ class IntegrationServer:
             "integrals_per_s": float(lat.size / span) if span > 0 else float("inf"),
             "evals": int(sum(r.evals for r in self.completed)),
             "peak_active": self.peak_active,
+            "host_launch_ms": self.host_launch_s * 1e3,
         }
 
     # ---------------------------------------------------------- scheduler
@@ -332,6 +355,13 @@ class IntegrationServer:
             self._grid_inflight.append((ev, host, rs))
 
     def _launch(self):
+        t0 = time.perf_counter()
+        try:
+            return self._launch_all()
+        finally:
+            self.host_launch_s += time.perf_counter() - t0
+
+    def _launch_all(self):
         launched = False
         for s in self._vegas:
             if s.event is None:
