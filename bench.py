@@ -400,7 +400,9 @@ def run_gpu(args):
     # run as individual launches, CUDA events around every fused sampling
     # launch on the launching (current) stream
     sampler_events, sampler_points = [], []
+    other_events = {"update_map": [], "finish": [], "get_nh": [], "warmup_fused": []}
     orig_iter = V.VegasDevice.iterate_fused
+    originals = {name: getattr(V.VegasDevice, name) for name in other_events}
 
     def timed_iterate(self, *a, **k):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -409,7 +411,22 @@ def run_gpu(args):
         e1.record()
         sampler_events.append((e0, e1))
 
+    def timed(name):
+        fn = originals[name]
+
+        def wrapper(self, *a, **k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = fn(self, *a, **k)
+            e1.record()
+            other_events[name].append((e0, e1))
+            return out
+
+        return wrapper
+
     V.VegasDevice.iterate_fused = timed_iterate
+    for name in other_events:
+        setattr(V.VegasDevice, name, timed(name))
     V.FORCE_EAGER[0] = True
     try:
         for k in range(args.steps):
@@ -421,8 +438,16 @@ def run_gpu(args):
             sampler_points += [float(stats[j]) for j in range(len(sampler_events) - n0)]
     finally:
         V.VegasDevice.iterate_fused = orig_iter
+        for name, fn in originals.items():
+            setattr(V.VegasDevice, name, fn)
         V.FORCE_EAGER[0] = False
     sampler_ms = [a.elapsed_time(b) for a, b in sampler_events]
+    # mean duration per call of each step of an iteration (eager launches,
+    # CUDA events on the launching stream)
+    step_us = {"iterate_fused": 1e3 * sum(sampler_ms) / max(1, len(sampler_ms))}
+    for name, evs in other_events.items():
+        if evs:
+            step_us[name] = 1e3 * sum(a.elapsed_time(b) for a, b in evs) / len(evs)
 
     # ---- end to end through the public API with host inputs
     e2e_ms, e2e_evals = [], 0
@@ -521,6 +546,7 @@ def run_gpu(args):
             "avg_launch_us": avg_ms * 1000.0,
             "flops_per_point": flops_per_point,
         },
+        "iteration_steps_us": step_us,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "evals_per_step": tot_evals / (args.steps * ws),

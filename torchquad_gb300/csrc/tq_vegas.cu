@@ -475,27 +475,40 @@ struct FinishArgs {
   unsigned* ticket;
 };
 
-// Plain fp64 tree sum over the CTA (pairwise: error O(log n) ulp); the
+// Three plain fp64 tree sums over the CTA at once (pairwise: error O(log n)
+// ulp; the three chains interleave); results valid in thread 0.  The
 // compensated sum is taken across CTAs by the last one.
-__device__ __forceinline__ double block_sum_plain(double v, double* sh) {
+__device__ __forceinline__ void block_sum3(double& x, double& y, double& z, double* sh) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if (lane == 0) sh[warp] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (warp == 0) {
-    t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    x += __shfl_down_sync(0xffffffffu, x, o);
+    y += __shfl_down_sync(0xffffffffu, y, o);
+    z += __shfl_down_sync(0xffffffffu, z, o);
   }
-  return t;  // valid in thread 0
+  if (lane == 0) {
+    sh[warp] = x;
+    sh[32 + warp] = y;
+    sh[64 + warp] = z;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    x = lane < nw ? sh[lane] : 0.0;
+    y = lane < nw ? sh[32 + lane] : 0.0;
+    z = lane < nw ? sh[64 + lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      x += __shfl_down_sync(0xffffffffu, x, o);
+      y += __shfl_down_sync(0xffffffffu, y, o);
+      z += __shfl_down_sync(0xffffffffu, z, o);
+    }
+  }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
-  __shared__ double sh[kBlock / 32];
+  __shared__ double sh[96];
   const tq_vegas_state& st = a.st;
   const double V = a.V;  // V_cubes (vegas_stratification.py:29)
   const T Vt = (T)V, V2t = (T)(V * V);
@@ -518,26 +531,30 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
     ((T*)st.dh)[c] = dh;
     dsum += (double)dh;
   }
-  res = block_sum_plain(res, sh);
-  s2 = block_sum_plain(s2, sh);
-  dsum = block_sum_plain(dsum, sh);
+  block_sum3(res, s2, dsum, sh);
   if (threadIdx.x == 0) {
     a.partials[3 * blockIdx.x] = Acc{res, 0.0};
     a.partials[3 * blockIdx.x + 1] = Acc{s2, 0.0};
     a.partials[3 * blockIdx.x + 2] = Acc{dsum, 0.0};
   }
-  if (last_block_arrives(a.ticket)) {
-    // fixed assignment of partials to threads and fixed tree: deterministic
+  if (last_block_arrives(a.ticket) && threadIdx.x < 32) {
+    // one warp, fixed assignment of partials to lanes and a fixed tree:
+    // deterministic; the three compensated chains interleave
+    const int lane = threadIdx.x;
     Acc r{0, 0}, q{0, 0}, ds{0, 0};
-    for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
-      acc_add(r, a.partials[3 * i].s);
-      acc_add(q, a.partials[3 * i + 1].s);
-      acc_add(ds, a.partials[3 * i + 2].s);
+    for (unsigned i = lane; i < gridDim.x; i += 32) {
+      acc_add(r, __ldcg(&a.partials[3 * i].s));
+      acc_add(q, __ldcg(&a.partials[3 * i + 1].s));
+      acc_add(ds, __ldcg(&a.partials[3 * i + 2].s));
     }
-    r = block_reduce<kBlock>(r);
-    q = block_reduce<kBlock>(q);
-    ds = block_reduce<kBlock>(ds);
-    if (threadIdx.x == 0) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const Acc r2 = acc_shfl_down(r, off), q2 = acc_shfl_down(q, off), d2 = acc_shfl_down(ds, off);
+      acc_merge(r, r2);
+      acc_merge(q, q2);
+      acc_merge(ds, d2);
+    }
+    if (lane == 0) {
       const int64_t slot = st.control[1];
       if (slot >= 0 && slot < st.n_stat_slots) {
         double* out = st.stats + 4 * slot;
@@ -557,44 +574,6 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
 }
 
 // --------------------------------------------------------- map update
-// One CTA updates every dimension: the "all weights zero" test of
-// vegas_map.py:151-155 spans the whole map.
-// Block-wide inclusive prefix sum of a[0..n) in place: contiguous chunks per
-// thread, then a scan of the chunk totals.  (The large-map path only; the
-// small-map path sums sequentially like the reference.)
-__device__ void block_scan_inclusive(double* a, int64_t n, double* sh) {
-  const int nt = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const int64_t per = (n + nt - 1) / nt;
-  const int64_t b0 = (int64_t)t * per, b1 = min(n, b0 + per);
-  double s = 0.0;
-  for (int64_t i = b0; i < b1; ++i) {
-    s += a[i];
-    a[i] = s;
-  }
-  double x = s;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const double v = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += v;
-  }
-  __syncthreads();
-  if (lane == 31) sh[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    double y = lane < (nt >> 5) ? sh[lane] : 0.0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const double v = __shfl_up_sync(0xffffffffu, y, o);
-      if (lane >= o) y += v;
-    }
-    sh[lane] = y;
-  }
-  __syncthreads();
-  const double off = x - s + (warp > 0 ? sh[warp - 1] : 0.0);
-  for (int64_t i = b0; i < b1; ++i) a[i] += off;
-  __syncthreads();
-}
-
 // Block-wide sum (fp64), result in every thread.
 __device__ double block_sum_all(double v, double* sh) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -609,223 +588,7 @@ __device__ double block_sum_all(double v, double* sh) {
   return t;
 }
 
-// Bytes of the map-update working arrays (placed in shared memory when they
-// fit, else in the workspace).
-__host__ __device__ inline size_t map_work_bytes(int d, int64_t B, size_t tsize) {
-  const size_t DB = (size_t)d * B, DB1 = (size_t)d * (B + 1);
-  size_t off = 2 * DB * tsize + 2 * DB;
-  off = (off + 15) & ~size_t(15);
-  return off + DB1 * (8 + 8 + tsize) + 16;
-}
-
-constexpr int kSmallMap = 1024;  // intervals per dimension handled sequentially
-
-template <typename T>
-__global__ void __launch_bounds__(1024) vegas_update_map_kernel(tq_vegas_state st, double alpha,
-                                                                  double* scratch, int in_smem,
-                                                                  void* smooth_out) {
-  extern __shared__ __align__(16) unsigned char map_smem[];
-  const int d = st.dim;
-  const int64_t B = st.n_bins;
-  const int64_t DB = d * B;
-  unsigned char* base = in_smem ? map_smem : (unsigned char*)scratch;
-  T* w = (T*)base;                    // [d][B] averaged weights, then smoothed
-  T* wtmp = w + DB;                   // [d][B]
-  unsigned char* z = (unsigned char*)(wtmp + DB);        // [d][B] zero-count flags
-  unsigned char* ztmp = z + DB;                          // [d][B]
-  double* newx = (double*)(((uintptr_t)(ztmp + DB) + 15) & ~uintptr_t(15));  // [d][B+1]
-  int64_t* idx = (int64_t*)(newx + d * (B + 1));         // [d][B+1]
-  T* val = (T*)(idx + d * (B + 1));                      // [d][B+1]
-  __shared__ T sums[kMaxDim];
-  __shared__ T deltas[kMaxDim];
-
-  // EQ 17: average weights per interval; remember empty intervals
-  int any_zero = 0;
-  for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
-    const int64_t c = st.counts[i];
-    const T wi = (T)st.weights[i];
-    z[i] = c == 0;
-    any_zero |= (c == 0);
-    w[i] = c == 0 ? wi : div_rn(wi, (T)c);
-  }
-  any_zero = __syncthreads_or(any_zero);
-  if (any_zero) {
-    // fill empty intervals from their neighbours, up to 10 sweeps (:131-142)
-    for (int sweep = 0; sweep < 10; ++sweep) {
-      for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
-        const int64_t col = i % B;
-        wtmp[i] = (col < B - 1 && z[i]) ? w[i + 1] : w[i];
-        ztmp[i] = (col < B - 1) ? (z[i] && z[i + 1]) : z[i];
-      }
-      __syncthreads();
-      for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
-        const int64_t col = i % B;
-        w[i] = (col > 0 && ztmp[i]) ? wtmp[i - 1] : wtmp[i];
-        z[i] = (col > 0) ? (ztmp[i] && ztmp[i - 1]) : ztmp[i];
-      }
-      if (!__syncthreads_or([&] {
-            int zz = 0;
-            for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) zz |= z[i];
-            return zz;
-          }()))
-        break;
-    }
-  }
-  // row sums (:151): one warp per dimension
-  {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int k = warp; k < d; k += blockDim.x >> 5) {
-      double acc = 0.0;
-      for (int64_t b = lane; b < B; b += 32) acc += (double)w[k * B + b];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-      if (lane == 0) sums[k] = (T)acc;
-    }
-  }
-  __syncthreads();
-  int zero_row = 0;
-  for (int k = threadIdx.x; k < d; k += blockDim.x) zero_row |= sums[k] == (T)0;
-  if (__syncthreads_or(zero_row)) {
-    // The map cannot be updated (:152-155, :187-196): reset and flag.
-    if (smooth_out) {
-      if (threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
-      return;
-    }
-    for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
-      st.weights[i] = 0.0;
-      st.counts[i] = 0;
-    }
-    if (threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
-    return;
-  }
-  // EQ 18: [1,6,1]/8 smoothing with repeated borders, normalised; EQ 19
-  for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
-    const int64_t k = i / B, b = i - k * B;
-    const T* r = w + k * B;
-    T v;
-    if (b == 0)
-      v = add_rn(mul_rn((T)7, r[0]), r[1]);
-    else if (b == B - 1)
-      v = add_rn(r[B - 2], mul_rn((T)7, r[B - 1]));
-    else
-      v = add_rn(add_rn(r[b - 1], mul_rn((T)6, r[b])), r[b + 1]);
-    v = div_rn(v, mul_rn((T)8, sums[k]));
-    if (v != (T)0) {
-      const T t = div_rn(sub_rn(v, (T)1), log(v));
-      v = alpha == 0.5 ? sqrt(t) : pow(t, (T)alpha);
-    }
-    wtmp[i] = v;
-    if (smooth_out) ((T*)smooth_out)[i] = v;
-  }
-  __syncthreads();
-  if (smooth_out) return;  // _smooth_map only: the map and its weights stay as they are
-  // EQ 20-22.  The reference's cumulative sums run sequentially; here only
-  // the additions do (one thread per dimension), the divisions and the edge
-  // formula run in parallel.
-  double* cumd = newx;          // [d][B+1]: fp64 cumulative sums, later new edges
-  int32_t* mult = (int32_t*)w;  // [d][B]: delta multiples, later edge indices
-  {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int k = warp; k < d; k += blockDim.x >> 5) {  // :201 delta per dimension
-      double acc = 0.0;
-      for (int64_t b = lane; b < B; b += 32) acc += (double)wtmp[k * B + b];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-      if (lane == 0) deltas[k] = div_rn((T)acc, (T)B);
-    }
-  }
-  if (threadIdx.x < d) {  // :210-213 fp64 cumsum of sw[:-1]
-    const int k = threadIdx.x;
-    double cum = 0.0;
-    for (int64_t b = 0; b < B - 1; ++b) {
-      cum += (double)wtmp[k * B + b];
-      cumd[k * (B + 1) + b] = cum;
-    }
-  }
-  __syncthreads();
-  for (int64_t i = threadIdx.x; i < d * (B - 1); i += blockDim.x) {
-    const int64_t k = i / (B - 1), b = i - k * (B - 1);
-    int64_t m = (int64_t)(cumd[k * (B + 1) + b] / (double)deltas[k]);
-    m = m < 0 ? 0 : (m > B ? B : m);
-    mult[k * B + b] = (int32_t)m;
-  }
-  __syncthreads();
-  if (threadIdx.x < d) {  // :214-233 counts/sums per multiple, then prefixes
-    const int k = threadIdx.x;
-    const T* sw = wtmp + k * B;
-    const T delta = deltas[k];
-    int64_t* num = idx + k * (B + 1);
-    T* vv = val + k * (B + 1);
-    for (int64_t m = 0; m <= B; ++m) {
-      num[m] = 0;
-      vv[m] = (T)0;
-    }
-    for (int64_t b = 0; b < B - 1; ++b) {
-      const int m = mult[k * B + b];
-      num[m] += 1;
-      vv[m] = add_rn(vv[m], sw[b]);
-    }
-    int64_t ind = 0;
-    double daccu = 0.0;  // cumsum of (delta - val) accumulated in fp64, rounded per step
-    for (int64_t e = 0; e < B - 1; ++e) {
-      ind += num[e];
-      daccu += (double)sub_rn(delta, vv[e]);
-      mult[k * B + e] = (int32_t)(ind < 0 ? 0 : (ind > B - 1 ? B - 1 : ind));
-      vv[e] = (T)daccu;
-    }
-  }
-  __syncthreads();
-  for (int64_t i = threadIdx.x; i < d * (B + 1); i += blockDim.x) {  // EQ 22
-    const int64_t k = i / (B + 1), e1 = i - k * (B + 1);
-    const T* xe = (const T*)st.x_edges + k * (B + 1);
-    double nv;
-    if (e1 == 0 || e1 == B) {
-      nv = (double)xe[e1];
-    } else {
-      const int ii = mult[k * B + e1 - 1];
-      const T* sw = wtmp + k * B;
-      const T* dxe = (const T*)st.dx_edges + k * B;
-      nv = (double)add_rn(xe[ii], mul_rn(div_rn(val[k * (B + 1) + e1 - 1], sw[ii]), dxe[ii]));
-    }
-    newx[i] = nv;  // cumd is no longer needed
-  }
-  __syncthreads();
-  // :240-257: replace infinite edges by the mean of their (unrepaired)
-  // neighbours; val (no longer needed) holds the means.  The check is
-  // block-wide; the repair (rare) runs per dimension.
-  int any_bad = 0;
-  for (int64_t i = threadIdx.x; i < d * (B + 1); i += blockDim.x) any_bad |= !isfinite(newx[i]);
-  if (__syncthreads_or(any_bad) && threadIdx.x < d) {
-    const int k = threadIdx.x;
-    double* nx = newx + k * (B + 1);
-    T* vv = val + k * (B + 1);
-    bool bad = false;
-    for (int64_t e = 1; e < B; ++e) bad |= !isfinite(nx[e]);
-    if (bad) {
-      atomicAdd(st.flags + 1, 1);
-      for (int64_t e = 1; e < B; ++e)
-        vv[e] = mul_rn((T)0.5, add_rn((T)nx[e - 1], (T)nx[e + 1]));
-      for (int64_t e = 1; e < B; ++e)
-        if (!isfinite(nx[e])) nx[e] = (double)vv[e];
-      for (int64_t e = 1; e < B; ++e)
-        if (!isfinite(nx[e])) {
-          atomicAdd(st.flags + 2, 1);
-          break;
-        }
-    }
-  }
-  __syncthreads();
-  for (int64_t i = threadIdx.x; i < d * (B + 1); i += blockDim.x)
-    ((T*)st.x_edges)[i] = (T)newx[i];
-  __syncthreads();
-  for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
-    const int64_t k = i / B, b = i - k * B;
-    const T* xe = (const T*)st.x_edges + k * (B + 1);
-    ((T*)st.dx_edges)[i] = sub_rn(xe[b + 1], xe[b]);  // :259
-    st.weights[i] = 0.0;
-    st.counts[i] = 0;
-  }
-}
+constexpr int kSmallMap = 1024;  // intervals per dimension for the one-CTA-per-row path
 
 // ------------------------------------------------ map update, large maps
 // Maps of more than kSmallMap intervals per dimension (the reference's
@@ -1239,6 +1002,209 @@ __global__ void __launch_bounds__(kMapThreads) map_commit_kernel(tq_vegas_state 
   }
 }
 
+// ------------------------------------------------ map update, small maps
+// Maps of at most kSmallMap intervals per dimension: one CTA per dimension
+// runs the whole update of vegas_map.py:114-260 for its row in shared
+// memory, the cumulative sums as block scans.  The map-wide "some row of
+// weights sums to zero" test (:151-155) is made by every CTA over the whole
+// map: the weights are sums of squares, so a row of averaged (and filled)
+// weights sums to zero exactly when each of its averages is zero.  Since
+// every CTA reads every row, the weights and counts are cleared by the last
+// CTA to finish (ticket), not by each CTA for its own row.
+constexpr int kRowThreads = 256;
+constexpr int kRowPer = kSmallMap / kRowThreads;  // consecutive intervals per thread in the scans
+
+inline size_t map_row_smem(int64_t B, size_t ts) {
+  return (((5 * B + 2) * ts + (2 * B + 1) * 4 + 2 * B) + 15) & ~size_t(15);
+}
+
+// The last CTA to arrive (all others have finished reading the weights)
+// resets the weights and counts of the whole map (_reset_weight).
+__device__ void clear_map_by_last(const tq_vegas_state& st, unsigned* ticket) {
+  if (last_block_arrives(ticket)) {
+    const int64_t n = (int64_t)st.dim * st.n_bins;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      st.weights[i] = 0.0;
+      st.counts[i] = 0;
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRowThreads) vegas_map_rows_kernel(tq_vegas_state st, double alpha,
+                                                                      void* smooth_out, unsigned* ticket) {
+  extern __shared__ __align__(16) unsigned char row_smem[];
+  __shared__ double red[32];
+  __shared__ int rownz[kMaxDim];
+  const int k = blockIdx.x, d = st.dim;
+  const int B = (int)st.n_bins;
+  T* w = (T*)row_smem;                                 // [B] averaged, filled weights
+  T* wt = w + B;                                       // [B]
+  T* sw = wt + B;                                      // [B] smoothed weights
+  T* vv = sw + B;                                      // [B+1] sums per delta multiple
+  T* nx = vv + (B + 1);                                // [B+1] new edges
+  int32_t* mk = (int32_t*)(nx + (B + 1));              // [B] delta multiples
+  int32_t* ind = mk + B;                               // [B+1] old interval per new edge
+  unsigned char* z = (unsigned char*)(ind + (B + 1));  // [B] empty intervals
+  unsigned char* zt = z + B;                           // [B]
+  // zero-row test over the whole map
+  if (threadIdx.x < d) rownz[threadIdx.x] = 0;
+  __syncthreads();
+  for (int kk = 0; kk < d; ++kk) {
+    int nz = 0;
+    for (int b = threadIdx.x; b < B; b += blockDim.x) {
+      const int64_t c = st.counts[(int64_t)kk * B + b];
+      const T wi = (T)st.weights[(int64_t)kk * B + b];
+      nz |= (c == 0 ? wi : div_rn(wi, (T)c)) != (T)0;
+    }
+    if (nz) rownz[kk] = 1;
+  }
+  __syncthreads();
+  int zero_row = 0;
+  for (int kk = 0; kk < d; ++kk) zero_row |= !rownz[kk];
+  if (zero_row) {  // the map cannot be updated (:187-196): only the reset
+    if (k == 0 && threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
+    if (!smooth_out) clear_map_by_last(st, ticket);
+    return;
+  }
+  // EQ 17 and the filling of empty intervals (:118-145).  A sweep over a row
+  // without empty intervals changes nothing, so stopping per row gives the
+  // reference's map-wide stopping rule.
+  int anyz = 0;
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {
+    const int64_t c = st.counts[(int64_t)k * B + b];
+    const T wi = (T)st.weights[(int64_t)k * B + b];
+    z[b] = c == 0;
+    anyz |= c == 0;
+    w[b] = c == 0 ? wi : div_rn(wi, (T)c);
+  }
+  if (__syncthreads_or(anyz)) {
+    for (int sweep = 0; sweep < 10; ++sweep) {
+      for (int b = threadIdx.x; b < B; b += blockDim.x) {
+        wt[b] = (b < B - 1 && z[b]) ? w[b + 1] : w[b];
+        zt[b] = (b < B - 1) ? (z[b] && z[b + 1]) : z[b];
+      }
+      __syncthreads();
+      int left = 0;
+      for (int b = threadIdx.x; b < B; b += blockDim.x) {
+        w[b] = (b > 0 && zt[b]) ? wt[b - 1] : wt[b];
+        z[b] = (b > 0) ? (zt[b] && zt[b - 1]) : zt[b];
+        left |= z[b];
+      }
+      if (!__syncthreads_or(left)) break;
+    }
+  }
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < B; b += blockDim.x) acc += (double)w[b];
+  const T sum = (T)block_sum_all(acc, red);  // :151
+  // EQ 18-19
+  acc = 0.0;
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {
+    T v;
+    if (b == 0)
+      v = add_rn(mul_rn((T)7, w[0]), w[1]);
+    else if (b == B - 1)
+      v = add_rn(w[B - 2], mul_rn((T)7, w[B - 1]));
+    else
+      v = add_rn(add_rn(w[b - 1], mul_rn((T)6, w[b])), w[b + 1]);
+    v = div_rn(v, mul_rn((T)8, sum));
+    if (v != (T)0) {
+      const T t = div_rn(sub_rn(v, (T)1), log(v));
+      v = alpha == 0.5 ? sqrt(t) : pow(t, (T)alpha);
+    }
+    sw[b] = v;
+    acc += (double)v;
+    if (smooth_out) ((T*)smooth_out)[(int64_t)k * B + b] = v;
+  }
+  if (smooth_out) return;  // _smooth_map only: the map and its weights stay
+  const T delta = div_rn((T)block_sum_all(acc, red), (T)B);  // :201 (the barrier publishes sw)
+  // :210-213: fp64 cumulative sums of sw[:-1] divided by delta
+  const int b0 = threadIdx.x * kRowPer;
+  double x[kRowPer];
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < kRowPer; ++j) {
+    x[j] = b0 + j < B - 1 ? (double)sw[b0 + j] : 0.0;
+    s += x[j];
+  }
+  double cum = cta_exclusive_scan(s, red);
+#pragma unroll
+  for (int j = 0; j < kRowPer; ++j) {
+    if (b0 + j < B - 1) {
+      cum += x[j];
+      const int64_t q = (int64_t)(cum / (double)delta);
+      mk[b0 + j] = (int32_t)(q < 0 ? 0 : (q > B ? B : q));
+    }
+  }
+  for (int e = threadIdx.x; e <= B; e += blockDim.x) {
+    vv[e] = (T)0;
+    ind[e] = 0;
+  }
+  __syncthreads();
+  // :214-230 from the runs of equal multiples: ind[e] = #{b : mk[b] <= e},
+  // vv[q] = the sequential sum of sw over the run of multiple q
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {
+    const int from = b == 0 ? 0 : mk[b - 1];
+    const int to = b == B - 1 ? B + 1 : mk[b];
+    for (int e = from; e < to; ++e) ind[e] = b;
+    if (b < B - 1 && (b == 0 || mk[b] != mk[b - 1])) {
+      const int q = mk[b];
+      T a = (T)0;
+      for (int e = b; e < B - 1 && mk[e] == q; ++e) a = add_rn(a, sw[e]);
+      vv[q] = a;
+    }
+  }
+  __syncthreads();
+  // :233 d_accu (fp64 cumulative sum rounded to T per element) and EQ 22
+  const T* xe = (const T*)st.x_edges + (int64_t)k * (B + 1);
+  const T* dxe = (const T*)st.dx_edges + (int64_t)k * B;
+  s = 0.0;
+#pragma unroll
+  for (int j = 0; j < kRowPer; ++j) {
+    x[j] = b0 + j < B - 1 ? (double)sub_rn(delta, vv[b0 + j]) : 0.0;
+    s += x[j];
+  }
+  cum = cta_exclusive_scan(s, red);
+#pragma unroll
+  for (int j = 0; j < kRowPer; ++j) {
+    const int e = b0 + j;
+    if (e < B - 1) {
+      cum += x[j];
+      int ii = ind[e];
+      ii = ii < 0 ? 0 : (ii > B - 1 ? B - 1 : ii);
+      nx[e + 1] = add_rn(xe[ii], mul_rn(div_rn((T)cum, sw[ii]), dxe[ii]));
+    }
+  }
+  if (threadIdx.x == 0) {
+    nx[0] = xe[0];
+    nx[B] = xe[B];
+  }
+  __syncthreads();
+  // :239-257: infinite edges replaced by the mean of their neighbours (rare)
+  int bad = 0;
+  for (int e = threadIdx.x; e <= B; e += blockDim.x) bad |= !isfinite((double)nx[e]);
+  if (__syncthreads_or(bad)) {
+    if (threadIdx.x == 0) {
+      atomicAdd(st.flags + 1, 1);
+      for (int e = 1; e < B; ++e) vv[e] = mul_rn((T)0.5, add_rn(nx[e - 1], nx[e + 1]));
+      for (int e = 1; e < B; ++e)
+        if (!isfinite((double)nx[e])) nx[e] = vv[e];
+      for (int e = 0; e <= B; ++e)
+        if (!isfinite((double)nx[e])) {
+          atomicAdd(st.flags + 2, 1);
+          break;
+        }
+    }
+    __syncthreads();
+  }
+  T* xo = (T*)st.x_edges + (int64_t)k * (B + 1);
+  T* dxo = (T*)st.dx_edges + (int64_t)k * B;
+  for (int e = threadIdx.x; e <= B; e += blockDim.x) xo[e] = nx[e];
+  for (int b = threadIdx.x; b < B; b += blockDim.x) dxo[b] = sub_rn(nx[b + 1], nx[b]);  // :259
+  clear_map_by_last(st, ticket);
+}
+
 // ----------------------------------------------------------- init
 template <typename T>
 __global__ void vegas_init_kernel(tq_vegas_state st) {
@@ -1395,7 +1361,7 @@ static int64_t finish_blocks(const tq_vegas_state* st) {
 }
 static size_t map_scratch_bytes(const tq_vegas_state* st) {
   if (st->n_bins > kSmallMap) return map_tile_layout(st, nullptr).total;
-  return map_work_bytes(st->dim, st->n_bins, 8);
+  return 256;
 }
 
 // Workspace: [0,256) tickets; then nh block totals, finish partials and the
@@ -1555,25 +1521,22 @@ static int launch_update_map(const tq_vegas_state* st, double alpha, void* works
 #undef TQ_TILED_MAP
     return launch_status();
   }
-  const size_t bytes = map_work_bytes(st->dim, st->n_bins, dtype_size(st->dtype));
-  const int in_smem = bytes <= 160 * 1024;
-  const size_t smem = in_smem ? bytes : 0;
-#define TQ_MAP_LAUNCH(T)                                                                      \
-  {                                                                                           \
-    auto kfn = vegas_update_map_kernel<T>;                                                    \
-    if (smem > 48 * 1024) {                                                                   \
-      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
-                                           (int)smem);                                        \
-      if (e != cudaSuccess) return set_cuda_error(e);                                         \
-    }                                                                                         \
-    kfn<<<1, kBlock, smem, s>>>(*st, alpha, ws.map_scratch,                                   \
-                                                                in_smem, smooth_out);            \
+  const size_t smem = map_row_smem(st->n_bins, dtype_size(st->dtype));
+#define TQ_ROWS_LAUNCH(T)                                                                      \
+  {                                                                                            \
+    auto kfn = vegas_map_rows_kernel<T>;                                                       \
+    if (smem > 48 * 1024) {                                                                    \
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                           (int)smem);                                         \
+      if (e != cudaSuccess) return set_cuda_error(e);                                          \
+    }                                                                                          \
+    kfn<<<st->dim, kRowThreads, smem, s>>>(*st, alpha, smooth_out, ws.t_map);                  \
   }
   if (st->dtype == TQ_F64)
-    TQ_MAP_LAUNCH(double)
+    TQ_ROWS_LAUNCH(double)
   else
-    TQ_MAP_LAUNCH(float)
-#undef TQ_MAP_LAUNCH
+    TQ_ROWS_LAUNCH(float)
+#undef TQ_ROWS_LAUNCH
   return launch_status();
 }
 
