@@ -424,6 +424,19 @@ def run_gpu(args):
 
         return wrapper
 
+    # a device-side sleep ahead of every block of launches lets the host
+    # enqueue the whole block first, so the events time the GPU alone
+    orig_block, orig_warm = V._FusedPlan._block_seq, V._FusedPlan._warm_seq
+
+    def slept(fn):
+        def wrapper(self):
+            if not torch.cuda.is_current_stream_capturing():
+                torch.cuda._sleep(4_000_000)
+            return fn(self)
+
+        return wrapper
+
+    V._FusedPlan._block_seq, V._FusedPlan._warm_seq = slept(orig_block), slept(orig_warm)
     V.VegasDevice.iterate_fused = timed_iterate
     for name in other_events:
         setattr(V.VegasDevice, name, timed(name))
@@ -437,6 +450,7 @@ def run_gpu(args):
             stats = v._dev.stats[: v.it, 2].cpu()
             sampler_points += [float(stats[j]) for j in range(len(sampler_events) - n0)]
     finally:
+        V._FusedPlan._block_seq, V._FusedPlan._warm_seq = orig_block, orig_warm
         V.VegasDevice.iterate_fused = orig_iter
         for name, fn in originals.items():
             setattr(V.VegasDevice, name, fn)

@@ -79,6 +79,41 @@ __device__ __forceinline__ void accf_add(AccF& a, float x) {
   a.s = t;
 }
 
+// Double-float (two-float) accumulation on the FP32 pipe: the unevaluated
+// sum hi + lo, |lo| <= ulp(hi) / 2, about 48 significant bits.  Additions
+// use Knuth's TwoSum and Dekker's Fast2Sum for the renormalisation (the
+// accurate variant: two TwoSums per addition, so cancellation between terms
+// of either sign keeps the bound).  On GB300 an FP64 warp instruction
+// occupies an SM sub-partition's FP64 unit for about 64 cycles; these
+// operations keep long reductions off that unit.
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return F2{s, e};
+}
+__device__ __forceinline__ F2 fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return F2{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  F2 s = two_sum(a.hi, b.hi);
+  const F2 t = two_sum(a.lo, b.lo);
+  s = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, t.lo));
+}
+__device__ __forceinline__ F2 f2_add(F2 a, float b) {
+  const F2 s = two_sum(a.hi, b);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+__device__ __forceinline__ F2 f2_shfl_down(F2 a, int off) {
+  return F2{__shfl_down_sync(0xffffffffu, a.hi, off), __shfl_down_sync(0xffffffffu, a.lo, off)};
+}
+__device__ __forceinline__ double f2_value(F2 a) { return (double)a.hi + (double)a.lo; }
+
 // "Last CTA finishes" pattern: every CTA writes its partial, fences, takes a
 // ticket; the CTA that draws the last ticket reduces all partials in index
 // order (deterministic) and resets the ticket for the next launch.  No CTA

@@ -25,6 +25,9 @@
 namespace tq {
 
 constexpr int kTile = 256;  // threads per CTA of the sampler
+#ifndef TQ_SAMPLE_MIN_BLOCKS
+#define TQ_SAMPLE_MIN_BLOCKS 4  // resident sampler CTAs per SM (64 registers)
+#endif
 
 // ---- explicitly rounded arithmetic (no FMA contraction)
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
@@ -190,7 +193,7 @@ __device__ __forceinline__ void warp_hist_add(H* hw, unsigned* hc, int key, bool
 }
 
 template <typename T, int FAM, bool WARM>
-__global__ void __launch_bounds__(kTile, 3) vegas_sample_kernel(SampleArgs a) {
+__global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kernel(SampleArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Family<T> fam;
   __shared__ T lo[kMaxDim], wid[kMaxDim];
@@ -361,11 +364,12 @@ __global__ void __launch_bounds__(kTile, 3) vegas_sample_kernel(SampleArgs a) {
       }
     }
   }
-  if (last_block_arrives(a.ticket)) {
-    if (threadIdx.x == 0) {
-      *st.rng_offset = offset + ((uint64_t)M * d + PB - 1) / PB;
-      *a.ticket = 0u;
-    }
+  // The last CTA advances the RNG offset.  It reads nothing the other CTAs
+  // wrote (each read the offset before taking its ticket), so no fence.
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(a.ticket, 1u) == gridDim.x - 1) {
+    *st.rng_offset = offset + ((uint64_t)M * d + PB - 1) / PB;
+    *a.ticket = 0u;
   }
 }
 
@@ -568,6 +572,96 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
       st.control[2] = 1;
       // the sum the reference normalises with is taken in the state dtype
       st.scalars[0] = (double)(T)(ds.s + ds.c);
+      *a.ticket = 0u;
+    }
+  }
+}
+
+// fp32 states: the per-cube terms in fp32 (the reference computes them in
+// the state's dtype), every sum as a double-float on the FP32 pipe: per
+// thread, over the CTA, and across CTAs in the last one.  The only FP64
+// instructions are the two conversions of the cube's fp64 sums per cube.
+__device__ __forceinline__ void f2_warp_sum3(F2& x, F2& y, F2& z) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const F2 x2 = f2_shfl_down(x, o), y2 = f2_shfl_down(y, o), z2 = f2_shfl_down(z, o);
+    x = f2_add(x, x2);
+    y = f2_add(y, y2);
+    z = f2_add(z, z2);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) vegas_finish_f32_kernel(FinishArgs a) {
+  __shared__ F2 sh[3][kBlock / 32];
+  const tq_vegas_state& st = a.st;
+  const float Vt = (float)a.V, V2t = (float)(a.V * a.V);
+  const float beta = (float)a.beta;
+  F2 res{0.f, 0.f}, s2{0.f, 0.f}, dsum{0.f, 0.f};
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < st.n_cubes;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t nn = st.neval[c];
+    const float cnt = (float)nn;  // the reference's JF / neval in the state dtype
+    const float jT = __double2float_rn(st.jf[c]), j2T = __double2float_rn(st.jf2[c]);
+    // vegas.py:294-303: ih = JF * V / n, sigma2 += |JF2 * V^2 / n - ih^2| / n
+    const float inv = __frcp_rn(cnt);
+    const float q = __fmul_rn(jT, inv);
+    const float var = fabsf(__fmaf_rn(-q, q, __fmul_rn(j2T, inv)));
+    res = f2_add(res, __fmul_rn(q, Vt));
+    s2 = f2_add(s2, __fmul_rn(__fmul_rn(var, V2t), inv));
+    // update_DH (vegas_stratification.py:72-86), reference operation order
+    const float qd = div_rn(mul_rn(Vt, jT), cnt);
+    float dt = sub_rn(div_rn(mul_rn(V2t, j2T), cnt), mul_rn(qd, qd));
+    if (dt < 0.f) dt = 0.f;
+    const float dh = (a.beta == 0.75) ? powf(dt, 0.75f) : powf(dt, beta);
+    ((float*)st.dh)[c] = dh;
+    dsum = f2_add(dsum, dh);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  f2_warp_sum3(res, s2, dsum);
+  if (lane == 0) {
+    sh[0][warp] = res;
+    sh[1][warp] = s2;
+    sh[2][warp] = dsum;
+  }
+  __syncthreads();
+  F2* part = (F2*)a.partials;  // [blocks][3] double-floats in the Acc slots
+  if (warp == 0) {
+    const F2 zero{0.f, 0.f};
+    res = lane < kBlock / 32 ? sh[0][lane] : zero;
+    s2 = lane < kBlock / 32 ? sh[1][lane] : zero;
+    dsum = lane < kBlock / 32 ? sh[2][lane] : zero;
+    f2_warp_sum3(res, s2, dsum);
+    if (lane == 0) {
+      part[6 * blockIdx.x] = res;
+      part[6 * blockIdx.x + 2] = s2;
+      part[6 * blockIdx.x + 4] = dsum;
+    }
+  }
+  if (last_block_arrives(a.ticket) && warp == 0) {
+    F2 r{0.f, 0.f}, q{0.f, 0.f}, ds{0.f, 0.f};
+    for (unsigned i = lane; i < gridDim.x; i += 32) {  // fixed assignment and tree: deterministic
+      const float2 pr = __ldcg((const float2*)&part[6 * i]);
+      const float2 pq = __ldcg((const float2*)&part[6 * i + 2]);
+      const float2 pd = __ldcg((const float2*)&part[6 * i + 4]);
+      r = f2_add(r, F2{pr.x, pr.y});
+      q = f2_add(q, F2{pq.x, pq.y});
+      ds = f2_add(ds, F2{pd.x, pd.y});
+    }
+    f2_warp_sum3(r, q, ds);
+    if (lane == 0) {
+      const int64_t slot = st.control[1];
+      if (slot >= 0 && slot < st.n_stat_slots) {
+        double* out = st.stats + 4 * slot;
+        out[0] = f2_value(r);
+        out[1] = f2_value(q);
+        out[2] = (double)st.cube_start[st.n_cubes];
+      } else {
+        st.flags[3] = 1;
+      }
+      st.control[1] = slot + 1;
+      st.control[2] = 1;
+      // the sum the reference normalises with is taken in the state dtype
+      st.scalars[0] = (double)__fadd_rn(ds.hi, ds.lo);
       *a.ticket = 0u;
     }
   }
@@ -1440,7 +1534,7 @@ static int launch_sample(const tq_vegas_state* st, int family, const double* par
                 st->dim * st->n_bins < (int64_t(1) << 30);
   a.edges_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, true) <= limit;
   const size_t smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, a.edges_smem);
-  const int64_t cap = (int64_t)sm_count() * 3;  // resident CTAs (launch bounds)
+  const int64_t cap = (int64_t)sm_count() * TQ_SAMPLE_MIN_BLOCKS;  // resident CTAs
   int64_t tiles = max_points > 0 ? (max_points + kTile - 1) / kTile : cap;
   if (tiles > cap) tiles = cap;
   if (tiles < 1) tiles = 1;
@@ -1582,7 +1676,7 @@ extern "C" int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, 
   if (st->dtype == TQ_F64)
     vegas_finish_kernel<double><<<g, kBlock, 0, s>>>(a);
   else
-    vegas_finish_kernel<float><<<g, kBlock, 0, s>>>(a);
+    vegas_finish_f32_kernel<<<g, kBlock, 0, s>>>(a);
   return launch_status();
 }
 
