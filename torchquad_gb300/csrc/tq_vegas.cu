@@ -169,26 +169,21 @@ __device__ Smem<T> carve(unsigned char* base, const SampleArgs& a) {
   return s;
 }
 
-// Warp-aggregated histogram update: lanes with the same key form a group;
-// every member sums the group's values in lane order and the lowest lane
-// adds the sum (and the group size) to the warp-private bins.
+// Warp-private histogram update without atomics: lanes with the same key
+// form a group (__match_any_sync); the members add their values to the bin
+// one per round in lane order (a lane's rank in its group is its round), so
+// no two lanes write one bin in the same round and the order is fixed.  The
+// lowest member adds the group's count.
 template <typename H>
 __device__ __forceinline__ void warp_hist_add(H* hw, unsigned* hc, int key, bool valid, H v) {
   const int lane = threadIdx.x & 31;
   const unsigned grp = __match_any_sync(0xffffffffu, key);
-  H sum = v;
-  unsigned rest = grp & ~(1u << lane);
-  while (__any_sync(0xffffffffu, rest != 0u)) {
-    const int src = rest ? __ffs(rest) - 1 : lane;
-    const H x = __shfl_sync(0xffffffffu, v, src);
-    if (rest) {
-      sum += x;
-      rest &= rest - 1u;
-    }
-  }
-  if (valid && lane == __ffs(grp) - 1) {
-    hw[key] += sum;
-    hc[key] += (unsigned)__popc(grp);
+  const unsigned rank = (unsigned)__popc(grp & ((1u << lane) - 1u));
+  const unsigned rounds = __reduce_max_sync(0xffffffffu, valid ? rank : 0u);
+  if (valid && rank == 0u) hc[key] += (unsigned)__popc(grp);
+  for (unsigned r = 0; r <= rounds; ++r) {
+    if (valid && rank == r) hw[key] += v;
+    __syncwarp();
   }
 }
 
@@ -240,18 +235,24 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
   constexpr int PB = Uniform<T>::per_block;
 
   // Warp tiles of 32 consecutive points; every cube has >= 2 points, so a
-  // tile spans at most 17 cubes.
-  for (int64_t wt = (int64_t)blockIdx.x * kWarps + warp; wt * 32 < M;
-       wt += (int64_t)gridDim.x * kWarps) {
+  // tile spans at most 17 cubes.  Each warp takes a contiguous range of
+  // tiles (balanced to one tile), finds the cube of its first point once and
+  // then walks the cube boundaries tile by tile.
+  const int64_t n_tiles = (M + 31) / 32;
+  const int64_t n_warps = (int64_t)gridDim.x * kWarps;
+  const int64_t gw = (int64_t)blockIdx.x * kWarps + warp;
+  const int64_t t_begin = gw * n_tiles / n_warps, t_end = (gw + 1) * n_tiles / n_warps;
+  int64_t c0 = 0;  // cube of the tile's first point
+  if (!WARM && t_begin < t_end) c0 = warp_find_cube(st.cube_start, st.n_cubes, t_begin * 32);
+  for (int64_t wt = t_begin; wt < t_end; ++wt) {
     const int64_t j0 = wt * 32;
     const int64_t j = j0 + lane;
     const bool valid = j < M;
     int slot = -1;
-    int64_t c0 = 0;
+    int64_t csl = 0;
     if (!WARM) {
-      c0 = warp_find_cube(st.cube_start, st.n_cubes, j0);
       const int64_t cl = c0 + lane;
-      const int64_t csl = cl <= st.n_cubes ? st.cube_start[cl] : INT64_MAX;
+      csl = cl <= st.n_cubes ? st.cube_start[cl] : INT64_MAX;
       int l = 0;  // largest l with cube_start[c0 + l] <= j
 #pragma unroll
       for (int step = 16; step > 0; step >>= 1) {
@@ -346,6 +347,9 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
         atomicAdd(st.jf + c0 + slot, (double)jfd);
         atomicAdd(st.jf2 + c0 + slot, (double)jf2);
       }
+      // cube of the next tile's first point (at most 17 cubes ahead)
+      const unsigned ahead = __ballot_sync(0xffffffffu, csl <= j0 + 32);
+      c0 += 31 - __clz(ahead);
     }
   }
   if (a.hist_smem && a.use_map) {
