@@ -1,0 +1,391 @@
+// VEGAS+ on GB300: fused stratified sampling (Philox -> stratified y ->
+// adaptive-map x, jac -> integrand -> map histogram and per-cube sums), the
+// map update and the stratification update.
+//
+// Reference (torchquad v0.5.0): vegas.py (driver), vegas_map.py (adaptive
+// map), vegas_stratification.py (stratified sampling).  The reference
+// materialises y, x, f and jac for every point and scatter-adds them into
+// the map and the cubes with global atomics (utils.py:61-76).  Here one
+// kernel does a whole iteration: each warp takes 32 consecutive points,
+// generates them in registers, adds to a warp-private map histogram in
+// shared memory (lanes hitting the same interval are combined first, so the
+// adds are plain and their order fixed), and reduces the per-cube sums with
+// a segmented scan over the cube-contiguous point order (repeat_interleave
+// order of vegas_stratification.py:154; a warp spans at most 17 cubes
+// because every cube has >= 2 points) into one global add per cube segment.
+// The histograms are flushed once per CTA.
+//
+// The arithmetic that decides interval indices and points (y, ID, offset,
+// x, jac) is written with explicitly rounded operations in the state's
+// dtype, in the reference's operation order, so that indices and counts
+// match the reference bit for bit given the same uniforms and map.
+
+#pragma once
+
+#include "tq_common.cuh"
+
+namespace tq {
+
+constexpr int kTile = 256;  // threads per CTA of the sampler
+#ifndef TQ_SAMPLE_MIN_BLOCKS
+#define TQ_SAMPLE_MIN_BLOCKS 4  // resident sampler CTAs per SM (64 registers)
+#endif
+
+// ---- explicitly rounded arithmetic (no FMA contraction)
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+
+template <typename T>
+__device__ __forceinline__ T warm_scale() {
+  return (T)0.999999;  // vegas.py:236 (and the clamp of vegas_stratification.py:165)
+}
+
+// Map one coordinate: interval ID = floor(y*B), offset = y*B - floor(y*B)
+// (vegas_map.py:76-97), x = x_edges[ID] + dx_edges[ID]*offset (:57),
+// Jacobian factor B * dx_edges[ID] (:73).
+template <typename T>
+__device__ __forceinline__ int map_coord(const T* __restrict__ xe, const T* __restrict__ dxe,
+                                         int B, T Bf, T y, T& x, T& jac_factor) {
+  const T yB = mul_rn(y, Bf);
+  const T fl = floor(yB);
+  int id = (int)fl;
+  // y < 1 keeps id <= B-1; the clamp only guards memory for pathological B
+  id = id < 0 ? 0 : (id >= B ? B - 1 : id);
+  const T off = sub_rn(yB, fl);
+  x = add_rn(xe[id], mul_rn(dxe[id], off));
+  jac_factor = mul_rn(Bf, dxe[id]);
+  return id;
+}
+
+// Coordinate k of the position of cube c: (c / n_strat^k) mod n_strat,
+// dimension 0 fastest (vegas_stratification.py:105-138).
+__device__ __forceinline__ int64_t cube_digit(int64_t c, int64_t n_strat, int k) {
+  for (int i = 0; i < k; ++i) c /= n_strat;
+  return c % n_strat;
+}
+
+// y = (pos + u) / n_strat, values >= 1 replaced by 0.999999 (:159-165).
+// pos < n_strat < 2^31: 32-bit conversion.
+template <typename T>
+__device__ __forceinline__ T strat_y(int pos, T u, T nsf) {
+  T y = div_rn(add_rn((T)pos, u), nsf);
+  return y >= (T)1 ? warm_scale<T>() : y;
+}
+
+// Largest c in [0, n) with cs[c] <= target; cs strictly increasing, cs[0] = 0.
+// One warp, 32-ary search with coalesced probes.
+__device__ __forceinline__ int64_t warp_find_cube(const int64_t* __restrict__ cs, int64_t n,
+                                                  int64_t target) {
+  const int lane = threadIdx.x & 31;
+  int64_t lo = 0, hi = n;
+  while (hi - lo > 32) {
+    const int64_t step = (hi - lo + 31) / 32;
+    const int64_t pos = lo + lane * step;
+    const bool ok = pos < hi && cs[pos] <= target;
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    const int last = 31 - __clz(m);
+    lo = lo + last * step;
+    hi = min(hi, lo + step);
+  }
+  const int64_t pos = lo + lane;
+  const bool ok = pos < hi && cs[pos] <= target;
+  const unsigned m = __ballot_sync(0xffffffffu, ok);
+  return lo + (31 - __clz(m));
+}
+
+// ------------------------------------------------------------ sampling
+struct SampleArgs {
+  tq_vegas_state st;
+  int family;
+  const double* params;
+  int64_t n_samples;  // warm-up: points; iterations: read from cube_start
+  int use_map;        // accumulate the map histogram
+  int edges_smem, hist_smem;
+  int small_cubes;    // n_cubes < 2^32: cube digits with 32-bit division
+  FastDiv ns_div;     // division by n_strat
+  unsigned* ticket;
+};
+
+// Histogram weight type in shared memory: fp32 atomics are native, so the
+// fp32 path privatises in fp32 and flushes once per CTA into fp64.
+template <typename T>
+struct HistT {
+  using type = double;
+};
+template <>
+struct HistT<float> {
+  using type = float;
+};
+
+// Shared memory of the sampler: the map (edges) when it fits, and one
+// private histogram per warp (weights in HistT, counts in u32) when it fits.
+template <typename T>
+struct Smem {
+  T* xe;
+  T* dxe;
+  typename HistT<T>::type* hw;  // [warps][d*B]
+  unsigned* hc;                 // [warps][d*B]
+};
+
+constexpr int kWarps = kTile / 32;
+
+__host__ __device__ inline size_t sample_smem_bytes(int d, int64_t B, size_t tsize, bool hist,
+                                                    bool edges) {
+  size_t off = 0;
+  if (edges) off += tsize * (d * (B + 1) + d * B);
+  off = (off + 15) & ~size_t(15);
+  if (hist) off += (size_t)kWarps * d * B * (sizeof(double) + sizeof(unsigned));
+  return off;
+}
+
+template <typename T>
+__device__ Smem<T> carve(unsigned char* base, const SampleArgs& a) {
+  Smem<T> s;
+  const int d = a.st.dim;
+  const int64_t B = a.st.n_bins;
+  size_t off = 0;
+  if (a.edges_smem) {
+    s.xe = (T*)(base + off);
+    off += sizeof(T) * d * (B + 1);
+    s.dxe = (T*)(base + off);
+    off += sizeof(T) * d * B;
+  } else {
+    s.xe = (T*)a.st.x_edges;
+    s.dxe = (T*)a.st.dx_edges;
+  }
+  off = (off + 15) & ~size_t(15);
+  if (a.hist_smem) {
+    s.hw = (typename HistT<T>::type*)(base + off);
+    off += (size_t)kWarps * d * B * sizeof(double);
+    s.hc = (unsigned*)(base + off);
+  } else {
+    s.hw = nullptr;
+    s.hc = nullptr;
+  }
+  return s;
+}
+
+// Warp-private histogram update without atomics: lanes with the same key
+// form a group (__match_any_sync); the members add their values to the bin
+// one per round in lane order (a lane's rank in its group is its round), so
+// no two lanes write one bin in the same round and the order is fixed.  The
+// lowest member adds the group's count.
+template <typename H>
+__device__ __forceinline__ void warp_hist_add(H* hw, unsigned* hc, int key, bool valid, H v) {
+  const int lane = threadIdx.x & 31;
+  const unsigned grp = __match_any_sync(0xffffffffu, key);
+  const unsigned rank = (unsigned)__popc(grp & ((1u << lane) - 1u));
+  const unsigned rounds = __reduce_max_sync(0xffffffffu, valid ? rank : 0u);
+  if (valid && rank == 0u) hc[key] += (unsigned)__popc(grp);
+  for (unsigned r = 0; r <= rounds; ++r) {
+    if (valid && rank == r) hw[key] += v;
+    __syncwarp();
+  }
+}
+
+// D > 0: the dimension is known at compile time (fully unrolled point
+// loops, D interval indices in registers); D = 0: any dimension up to
+// kMaxDim from the state.
+template <typename T, int FAM, bool WARM, int D>
+__global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kernel(SampleArgs a) {
+  constexpr int KD = D > 0 ? D : kMaxDim;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ Family<T> fam;
+  __shared__ T lo[kMaxDim], wid[kMaxDim];
+  __shared__ T volume;
+  using H = typename HistT<T>::type;  // fp32 on the fp32 path
+  const tq_vegas_state& st = a.st;
+  const int d = D > 0 ? D : st.dim;
+  const int64_t B = st.n_bins;
+  const int64_t DB = d * B;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  Smem<T> sm = carve<T>(smem_raw, a);
+  if (threadIdx.x == 0) {
+    load_family<T>(fam, a.family, d, a.params);
+    const T* dom = (const T*)st.domain;
+    T v = (T)1;
+    for (int k = 0; k < d; ++k) {
+      lo[k] = dom[2 * k];
+      wid[k] = sub_rn(dom[2 * k + 1], dom[2 * k]);
+      v = mul_rn(v, wid[k]);
+    }
+    volume = v;
+  }
+  if (a.edges_smem) {
+    for (int64_t i = threadIdx.x; i < d * (B + 1); i += blockDim.x) sm.xe[i] = ((const T*)st.x_edges)[i];
+    for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) sm.dxe[i] = ((const T*)st.dx_edges)[i];
+  }
+  if (a.hist_smem) {
+    for (int64_t i = threadIdx.x; i < (int64_t)kWarps * DB; i += blockDim.x) {
+      sm.hw[i] = 0;
+      sm.hc[i] = 0u;
+    }
+  }
+  __syncthreads();
+  H* whw = a.hist_smem ? sm.hw + warp * DB : nullptr;
+  unsigned* whc = a.hist_smem ? sm.hc + warp * DB : nullptr;
+
+  const int64_t M = WARM ? a.n_samples : st.cube_start[st.n_cubes];
+  const uint64_t offset = *st.rng_offset;
+  const uint64_t seed = (uint64_t)st.control[3], sid = (uint64_t)st.control[4];
+  const int64_t ns = st.n_strat;
+  const T nsf = (T)ns;
+  const int Bi = (int)B;
+  const T Bf = (T)Bi;
+  constexpr int PB = Uniform<T>::per_block;
+
+  // Warp tiles of 32 consecutive points; every cube has >= 2 points, so a
+  // tile spans at most 17 cubes.  Each warp takes a contiguous range of
+  // tiles (balanced to one tile), finds the cube of its first point once and
+  // then walks the cube boundaries tile by tile.
+  const int64_t n_tiles = (M + 31) / 32;
+  const int64_t n_warps = (int64_t)gridDim.x * kWarps;
+  const int64_t gw = (int64_t)blockIdx.x * kWarps + warp;
+  const int64_t t_begin = gw * n_tiles / n_warps, t_end = (gw + 1) * n_tiles / n_warps;
+  int64_t c0 = 0;  // cube of the tile's first point
+  if (!WARM && t_begin < t_end) c0 = warp_find_cube(st.cube_start, st.n_cubes, t_begin * 32);
+  for (int64_t wt = t_begin; wt < t_end; ++wt) {
+    const int64_t j0 = wt * 32;
+    const int64_t j = j0 + lane;
+    const bool valid = j < M;
+    int slot = -1;
+    int64_t csl = 0;
+    if (!WARM) {
+      const int64_t cl = c0 + lane;
+      csl = cl <= st.n_cubes ? st.cube_start[cl] : INT64_MAX;
+      int l = 0;  // largest l with cube_start[c0 + l] <= j
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = l + step;
+        const int64_t v = __shfl_sync(0xffffffffu, csl, cand & 31);
+        if (cand < 32 && v <= j) l = cand;
+      }
+      slot = valid ? l : -1;
+    }
+    H jfd = 0, jf2 = 0;
+    int ids[KD];
+    if (valid) {
+      uint32_t c32 = (uint32_t)(c0 + slot);
+      uint64_t c = (uint64_t)(c0 + slot);
+      // Philox block of this point's first draw; later draws follow
+      const uint64_t e0 = (uint64_t)j * (uint64_t)d;
+      const uint64_t blk0 = offset + e0 / PB;
+      const int lane0 = (int)(e0 % PB);
+      int cur = -1;
+      uint4 r = make_uint4(0, 0, 0, 0);
+      T jac = (T)1;
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < KD; ++k) {
+        if (k < d) {
+          const int le = lane0 + k;
+          const int bi = le / PB;
+          if (bi != cur) {
+            r = philox_block(seed, sid, blk0 + (uint64_t)bi);
+            cur = bi;
+          }
+          const T u = Uniform<T>::from(r, le - bi * PB);
+          T y;
+          if (WARM) {
+            y = mul_rn(u, warm_scale<T>());
+          } else {
+            int pos;
+            if (a.small_cubes) {
+              const uint32_t q = fdiv(c32, a.ns_div);
+              pos = (int)(c32 - q * a.ns_div.d);
+              c32 = q;
+            } else {
+              const uint64_t q = c / (uint64_t)ns;
+              pos = (int)(c - q * (uint64_t)ns);
+              c = q;
+            }
+            y = strat_y<T>(pos, u, nsf);
+          }
+          T x, jf_k;
+          ids[k] = map_coord<T>(sm.xe + k * (Bi + 1), sm.dxe + k * Bi, Bi, Bf, y, x, jf_k);
+          jac = mul_rn(jac, jf_k);
+          // vegas.py:110: fn(x * domain_sizes + domain_starts) * domain_volume
+          const T xt = add_rn(mul_rn(x, wid[k]), lo[k]);
+          const T g = fam_term<FAM, T>(fam, k, xt);
+          s = (k == 0) ? g : s + g;
+        }
+      }
+      const T f = mul_rn(fam_outer<FAM, T>(fam, s), volume);
+      const T jfv = mul_rn(f, jac);
+      jfd = (H)jfv;
+      jf2 = jfd * jfd;
+    }
+    if (a.use_map) {
+#pragma unroll
+      for (int k = 0; k < KD; ++k) {
+        if (k < d) {
+          if (a.hist_smem) {
+            const int key = valid ? (int)(k * B) + ids[k] : -1 - lane;
+            warp_hist_add<H>(whw, whc, key, valid, jf2);
+          } else if (valid) {
+            atomicAdd(st.weights + k * B + ids[k], (double)jf2);
+            atomicAdd((unsigned long long*)(st.counts + k * B + ids[k]), 1ull);
+          }
+        }
+      }
+    }
+    if (!WARM) {
+      // points are in cube order: segmented inclusive scan over the warp,
+      // then one global add per cube segment
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const H a1 = __shfl_up_sync(0xffffffffu, jfd, o);
+        const H a2 = __shfl_up_sync(0xffffffffu, jf2, o);
+        const int so = __shfl_up_sync(0xffffffffu, slot, o);
+        if (lane >= o && so == slot) {
+          jfd += a1;
+          jf2 += a2;
+        }
+      }
+      const int next = __shfl_down_sync(0xffffffffu, slot, 1);
+      if (slot >= 0 && (lane == 31 || next != slot)) {
+        atomicAdd(st.jf + c0 + slot, (double)jfd);
+        atomicAdd(st.jf2 + c0 + slot, (double)jf2);
+      }
+      // cube of the next tile's first point (at most 17 cubes ahead)
+      const unsigned ahead = __ballot_sync(0xffffffffu, csl <= j0 + 32);
+      c0 += 31 - __clz(ahead);
+    }
+  }
+  if (a.hist_smem && a.use_map) {
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < DB; i += blockDim.x) {
+      unsigned cnt = 0;
+      H w = 0;
+#pragma unroll
+      for (int q = 0; q < kWarps; ++q) {
+        cnt += sm.hc[q * DB + i];
+        w += sm.hw[q * DB + i];
+      }
+      if (cnt) {
+        atomicAdd(st.weights + i, (double)w);
+        atomicAdd((unsigned long long*)(st.counts + i), (unsigned long long)cnt);
+      }
+    }
+  }
+  // The last CTA advances the RNG offset.  It reads nothing the other CTAs
+  // wrote (each read the offset before taking its ticket), so no fence.
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(a.ticket, 1u) == gridDim.x - 1) {
+    *st.rng_offset = offset + ((uint64_t)M * d + PB - 1) / PB;
+    *a.ticket = 0u;
+  }
+}
+
+// fp32 iterations with 1 <= dim <= 8: the dimension-specialised sampler
+// (tq_vegas_sample_d.cu).
+int launch_sample_f32_dims(const SampleArgs& a, int family, int dim, unsigned grid, size_t smem,
+                           cudaStream_t s);
+
+}  // namespace tq
