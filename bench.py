@@ -160,6 +160,96 @@ def measure_batched(tq, dev, reps=5):
     return out
 
 
+def sampler_traffic_bytes():
+    """DRAM bytes (read + write) of one fused-sampler launch of this workload,
+    from the committed ncu summary (profiles/), or None without one."""
+    p = Path(__file__).resolve().parent / "profiles" / "vegas_iteration_kernels_d6_N1e7_ncu.md"
+    try:
+        for line in p.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch vegas_sample_kernel:"):
+                return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def measure_grid_cases(tq, dev, reps=20):
+    """The two grid-rule configurations: C1, plain Simpson, dim 3, 101 points
+    per dimension (N = 1,030,301), fp64, exp(x0+x1+x2) on [0,1]^3 against
+    (e-1)^3; C4, GaussLegendre, dim 4, 32 nodes per dimension, fp64,
+    cos(2 pi u + a.x) with u and the domain bounds requiring gradients:
+    forward and forward+backward times, gradients against central
+    differences (h = 1e-6).  Device-resident inputs, CUDA events."""
+    import numpy as np
+    import torch
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            r = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, r
+
+    out = {}
+    dom = torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float64, device=dev)
+    f1 = tq.ExpSum(3)
+    ms, v = timed(lambda: tq.Simpson().integrate(f1, 3, N=1_030_301, integration_domain=dom))
+    exact = (math.e - 1.0) ** 3
+    t0 = time.perf_counter()
+    v_e2e = tq.Simpson().integrate(f1, 3, N=1_030_301,
+                                   integration_domain=torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float64)).item()
+    t_e2e = time.perf_counter() - t0
+    out["c1_simpson_d3_fp64"] = {"ms": ms, "evals_per_s": 1_030_301 / (ms / 1000.0), "e2e_ms": t_e2e * 1000.0,
+                                 "rel_err_vs_analytic": abs(v.item() - exact) / exact,
+                                 "e2e_value_matches": v_e2e == v.item()}
+    a = [1.2, -2.1, 0.7, 2.6]
+    u0 = 0.37
+
+    def fwd(u, d):
+        return tq.GaussLegendre().integrate(tq.Oscillatory(4, a=a, b=u), 4, N=32**4, integration_domain=d)
+
+    u = torch.tensor(u0, dtype=torch.float64, device=dev, requires_grad=True)
+    d4 = torch.tensor([[0.0, 1.0]] * 4, dtype=torch.float64, device=dev, requires_grad=True)
+    with torch.no_grad():
+        ms_f, _ = timed(lambda: fwd(torch.tensor(u0, dtype=torch.float64, device=dev),
+                                    torch.tensor([[0.0, 1.0]] * 4, dtype=torch.float64, device=dev)))
+
+    def fb():
+        u.grad = None
+        d4.grad = None
+        val = fwd(u, d4)
+        val.backward()
+        return val
+
+    ms_fb, _ = timed(fb)
+    g = np.concatenate([[u.grad.item()], d4.grad.double().cpu().numpy().ravel()])
+    h = 1e-6
+    fd = []
+    with torch.no_grad():
+        for k in range(9):
+            up, dp = u0, np.array([[0.0, 1.0]] * 4)
+            um, dm = u0, dp.copy()
+            if k == 0:
+                up, um = u0 + h, u0 - h
+            else:
+                dp = dp.copy()
+                dp.ravel()[k - 1] += h
+                dm.ravel()[k - 1] -= h
+            fp = fwd(torch.tensor(up, dtype=torch.float64, device=dev), torch.tensor(dp, device=dev)).item()
+            fm = fwd(torch.tensor(um, dtype=torch.float64, device=dev), torch.tensor(dm, device=dev)).item()
+            fd.append((fp - fm) / (2 * h))
+    fd = np.array(fd)
+    out["c4_gausslegendre_d4_grad_fp64"] = {
+        "forward_ms": ms_f, "forward_backward_ms": ms_fb, "evals_per_s": 32**4 / (ms_f / 1000.0),
+        "max_abs_grad_diff_vs_central_differences": float(np.max(np.abs(g - fd))),
+        "max_abs_grad": float(np.max(np.abs(g)))}
+    return out
+
+
 def measure_serving(tq, dev, n=120, rates=(1e2, 1e3, 1e4, 1e5)):
     """Poisson request streams (MC / VEGAS / Simpson, dims 1-10, N log-uniform
     1e4..1e8, target relative error 1e-3..1e-5, seed 2) through the serving
@@ -382,6 +472,13 @@ def run_gpu(args):
     step_ms, evals = [], 0
     launches0 = L.launches[0]
     with clocks:
+        # keep the GPU under the same load for about a second first, so the
+        # 200 ms clock samples cover the load the timed steps run under
+        t_soak = time.perf_counter() + 1.0
+        k_soak = 0
+        while time.perf_counter() < t_soak:
+            one(20_000 + k_soak, domain_dev)
+            k_soak += 1
         barrier()
         for k in range(args.steps):
             flush.fill_(k & 0xFF)
@@ -554,7 +651,7 @@ def run_gpu(args):
             "peak": fp32_peak,
             "unit": "TFLOP/s",
             "frac": achieved / fp32_peak,
-            "traffic": None,
+            "traffic": sampler_traffic_bytes(),
             "peak_source": "FP32 FMA probe kernel measured in this run (MEASURED_PEAKS.json has HBM and bf16 only)",
             "points_per_launch": pts,
             "avg_launch_us": avg_ms * 1000.0,
@@ -566,6 +663,7 @@ def run_gpu(args):
         "evals_per_step": tot_evals / (args.steps * ws),
     }
     if not args.no_batched:
+        line["grid_cases"] = measure_grid_cases(tq, dev)
         line["batched"] = measure_batched(tq, dev)
     if not args.no_serving:
         line["serving"] = measure_serving(tq, dev)
