@@ -13,6 +13,8 @@
 // The reference has no batched form: a batch is a loop of per-call
 // GridIntegrator.integrate (grid_integrator.py:32-55).
 
+#include <type_traits>
+
 #include "tq_grid_common.cuh"
 
 namespace tq {
@@ -44,6 +46,11 @@ __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
   __shared__ uint64_t rstride[kMaxDim];
   __shared__ BatchDesc d;
   __shared__ int64_t tile0;
+  InnerTab* tab = nullptr;
+  if constexpr (std::is_same<T, double>::value) {
+    __shared__ InnerTab tab_s;
+    tab = &tab_s;
+  }
   for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
     if (threadIdx.x == 0) {
       int64_t lo = 0, hi = a.n_int;  // largest i with tile_start[i] <= tile
@@ -74,6 +81,13 @@ __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
     const double wlast = g.wscale[last];
     const T a_l = g.a[last], b_l = g.b[last], st_l = g.step[last];
     const int half = n32 / 2;
+    // fp64: last-dimension tables of this tile's integral (one
+    // outer-function evaluation per row)
+    bool use_tab = false;
+    if constexpr (std::is_same<T, double>::value) {
+      if (dim >= 2 && n <= kTabMax)
+        use_tab = build_inner_tab<FAM>(*tab, g, fam, last, n32, gl, rule, gln, glw);
+    }
     Acc acc{0.0, 0.0};
     for (int64_t base = begin + (int64_t)threadIdx.x * P; base < end;
          base += (int64_t)blockDim.x * P) {
@@ -93,7 +107,22 @@ __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
         }
         const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
         T sum = T(0), comp = T(0);
-        for (int j = jl; j < seg_end; ++j) {
+        bool tabbed = false;
+        if constexpr (std::is_same<T, double>::value) {
+          if (use_tab) {
+            const RowFactor rf = row_factor<FAM>(fam, s_outer);
+            if (rf.ok) {
+              for (int j = jl; j < seg_end; ++j) {
+                const double y = tab->w[j] * tab_value<FAM>(rf, tab->t1[j], tab->t2[j]) - comp;
+                const double tt = sum + y;
+                comp = (tt - sum) - y;
+                sum = tt;
+              }
+              tabbed = true;
+            }
+          }
+        }
+        for (int j = tabbed ? seg_end : jl; j < seg_end; ++j) {
           T x;
           if (gl)
             x = (T)__dadd_rn(__dmul_rn(g.half[last], __ldg(gln + j)), g.mid[last]);

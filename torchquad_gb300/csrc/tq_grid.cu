@@ -12,6 +12,8 @@
 // w_i * f(x_i) directly; the per-dimension collapse becomes the product of
 // 1-D weights, which is the same quadrature.
 
+#include <type_traits>
+
 #include "tq_grid_common.cuh"
 
 namespace tq {
@@ -121,6 +123,15 @@ __global__ void __launch_bounds__(kBlock, 2) grid_fused_kernel(FusedArgs args) {
   const double wlast = g.wscale[last];
   const T a_l = g.a[last], b_l = g.b[last], st_l = g.step[last];
   const int half = n32 / 2;
+  // fp64: last-dimension tables (one outer-function evaluation per row)
+  bool use_tab = false;
+  InnerTab* tab = nullptr;
+  if constexpr (std::is_same<T, double>::value) {
+    __shared__ InnerTab tab_s;
+    tab = &tab_s;
+    if (dim >= 2 && n <= kTabMax)
+      use_tab = build_inner_tab<FAM>(tab_s, g, fam, last, n32, GL, RULE, gl_nodes, gl_w);
+  }
 
   Acc acc{0.0, 0.0};
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
@@ -144,15 +155,27 @@ __global__ void __launch_bounds__(kBlock, 2) grid_fused_kernel(FusedArgs args) {
                                 w_outer);
       const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
       SegSum<T> seg;
-      for (int j = jl; j < seg_end; ++j) {
-        T x;
-        if (GL)
-          x = (T)__dadd_rn(__dmul_rn(g.half[last], __ldg(gl_nodes + j)), g.mid[last]);
-        else
-          x = (j < half) ? fma(st_l, (T)j, a_l) : fma(-st_l, (T)(n32 - 1 - j), b_l);
-        const T f = fam_outer<FAM, T>(fam, s_outer + fam_term<FAM, T>(fam, last, x));
-        const T wj = GL ? (T)__ldg(gl_w + j) : (T)nc_int_t<RULE>(j, n32);
-        seg.add(wj * f);
+      bool tabbed = false;
+      if constexpr (std::is_same<T, double>::value) {
+        if (use_tab) {
+          const RowFactor rf = row_factor<FAM>(fam, s_outer);
+          if (rf.ok) {
+            for (int j = jl; j < seg_end; ++j) seg.add(tab->w[j] * tab_value<FAM>(rf, tab->t1[j], tab->t2[j]));
+            tabbed = true;
+          }
+        }
+      }
+      if (!tabbed) {
+        for (int j = jl; j < seg_end; ++j) {
+          T x;
+          if (GL)
+            x = (T)__dadd_rn(__dmul_rn(g.half[last], __ldg(gl_nodes + j)), g.mid[last]);
+          else
+            x = (j < half) ? fma(st_l, (T)j, a_l) : fma(-st_l, (T)(n32 - 1 - j), b_l);
+          const T f = fam_outer<FAM, T>(fam, s_outer + fam_term<FAM, T>(fam, last, x));
+          const T wj = GL ? (T)__ldg(gl_w + j) : (T)nc_int_t<RULE>(j, n32);
+          seg.add(wj * f);
+        }
       }
       acc_add(acc, seg.value() * (w_outer * wlast));
       left -= seg_end - jl;

@@ -82,4 +82,92 @@ __device__ __forceinline__ int nc_int_t(int j, int n) {
   return (m & 1) ? 32 : (m == 2 ? 12 : 14);
 }
 
+// ---------------------------------------------- fp64 inner-dimension tables
+// The built-in families are functions of a separable sum s + t, where s
+// gathers the outer dimensions of a grid row and t = g_last(x_j) the node's
+// last coordinate.  For fp64 grids the node value is formed from a per-row
+// factor and a per-node table entry instead of one fp64 exp/cos per node
+// (on GB300 an FP64 warp instruction occupies the FP64 unit for ~64 cycles):
+//   ExpSum   c exp(s + b + t)      = [c exp(s + b)] * exp(t)
+//   Gaussian c exp(-(s + t))       = [c exp(-s)]    * exp(-t)
+//   Oscill.  c cos(2 pi b + s + t) = [c cos p] cos t - [c sin p] sin t,  p = 2 pi b + s
+//   SumSin   c (s + sin(a x))      = c * (s + t')
+// Every node is still evaluated (a product of two normal numbers is correct
+// to 2 ulp).  Rows whose factor is not a normal number, and tables with an
+// entry that is not, take the direct formula.
+constexpr int kTabMax = 1024;  // last-dimension nodes a table holds
+
+struct InnerTab {
+  double w[kTabMax];   // unscaled 1-D weight of the last dimension
+  double t1[kTabMax];  // exp(t), exp(-t), cos(t) or sin(a x)
+  double t2[kTabMax];  // sin(t) (oscillatory)
+};
+
+__device__ __forceinline__ bool normal_factor(double v) {
+  return isfinite(v) && fabs(v) >= 2.2250738585072014e-308;
+}
+
+// Builds the table for nodes 0..n-1 of the last dimension (all threads of
+// the CTA); returns, in every thread, whether all entries are usable.
+template <int FAM>
+__device__ bool build_inner_tab(InnerTab& tb, const Geo<double>& g, const Family<double>& fam,
+                                int last, int n, bool gl, int rule,
+                                const double* __restrict__ gl_nodes,
+                                const double* __restrict__ gl_w) {
+  int bad = 0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const double x = gl ? __dadd_rn(__dmul_rn(g.half[last], __ldg(gl_nodes + j)), g.mid[last])
+                        : linspace_node<double>(g.a[last], g.b[last], g.step[last], n, j);
+    tb.w[j] = gl ? __ldg(gl_w + j) : (double)nc_int(rule, j, n);
+    const double t = fam_term<FAM, double>(fam, last, x);
+    if (FAM == TQ_FN_OSCILLATORY) {
+      double sn, cs;
+      sincos(t, &sn, &cs);
+      tb.t1[j] = cs;
+      tb.t2[j] = sn;
+    } else if (FAM == TQ_FN_SUM_SIN) {
+      tb.t1[j] = t;
+    } else {
+      const double e = exp(FAM == TQ_FN_GAUSSIAN ? -t : t);
+      tb.t1[j] = e;
+      bad |= !normal_factor(e);
+    }
+  }
+  return !__syncthreads_or(bad);
+}
+
+// The row's factors for the separable sum s of its outer dimensions.
+struct RowFactor {
+  double r1, r2;
+  bool ok;
+};
+template <int FAM>
+__device__ __forceinline__ RowFactor row_factor(const Family<double>& fam, double s) {
+  RowFactor f;
+  if (FAM == TQ_FN_OSCILLATORY) {
+    double sn, cs;
+    sincos(2.0 * CUDART_PI * fam.b + s, &sn, &cs);
+    f.r1 = fam.c * cs;
+    f.r2 = fam.c * sn;
+    f.ok = true;
+  } else if (FAM == TQ_FN_SUM_SIN) {
+    f.r1 = s;
+    f.r2 = fam.c;
+    f.ok = true;
+  } else {
+    f.r1 = fam.c * exp(FAM == TQ_FN_GAUSSIAN ? -s : s + fam.b);
+    f.r2 = 0.0;
+    f.ok = normal_factor(f.r1) || (f.r1 == 0.0 && fam.c == 0.0);
+  }
+  return f;
+}
+// The integrand at a node of the row from the row's factors and the node's
+// table entries.
+template <int FAM>
+__device__ __forceinline__ double tab_value(const RowFactor& f, double t1, double t2) {
+  if (FAM == TQ_FN_OSCILLATORY) return fma(f.r1, t1, -(f.r2 * t2));
+  if (FAM == TQ_FN_SUM_SIN) return f.r2 * (f.r1 + t1);
+  return f.r1 * t1;
+}
+
 }  // namespace tq
