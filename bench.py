@@ -470,7 +470,6 @@ def run_gpu(args):
     clocks = ClockSampler(str(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv") if (ROOT / "gpurun_out").is_dir()
                           else f"/tmp/tq_clocks_{rank}.csv", local)
     step_ms, evals = [], 0
-    launches0 = L.launches[0]
     with clocks:
         # keep the GPU under the same load for about a second first, so the
         # 200 ms clock samples cover the load the timed steps run under
@@ -480,6 +479,7 @@ def run_gpu(args):
             one(20_000 + k_soak, domain_dev)
             k_soak += 1
         barrier()
+        launches0 = L.launches[0]
         for k in range(args.steps):
             flush.fill_(k & 0xFF)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -497,7 +497,7 @@ def run_gpu(args):
     # run as individual launches, CUDA events around every fused sampling
     # launch on the launching (current) stream
     sampler_events, sampler_points = [], []
-    other_events = {"update_map": [], "finish": [], "get_nh": [], "warmup_fused": []}
+    other_events = {"update_map": [], "finish": [], "finish_update_map": [], "get_nh": [], "warmup_fused": []}
     orig_iter = V.VegasDevice.iterate_fused
     originals = {name: getattr(V.VegasDevice, name) for name in other_events}
 

@@ -349,6 +349,14 @@ int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, const double* p
 int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, void* workspace,
                               size_t workspace_bytes, void* stream);
 
+/* tq_vegas_finish_iteration followed by tq_vegas_update_map (the end of one
+ * stratified iteration with the map improved, vegas.py:303 then
+ * vegas.py:313 -> vegas_map.py:185-261).  For maps of at most 1024
+ * intervals per dimension both run in one launch side by side (they touch
+ * disjoint parts of the state); larger maps take the two calls. */
+int tq_vegas_finish_update_map(const tq_vegas_state* st, double beta, double alpha,
+                               void* workspace, size_t workspace_bytes, void* stream);
+
 /* Materialised path (arbitrary torch integrands, injected uniforms). */
 
 /* y[M][d] = stratified points from uniforms u[M][d] (get_Y); M must equal

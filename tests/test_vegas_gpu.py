@@ -334,6 +334,30 @@ def test_large_map_cases_match_oracle(case, dtype, cuda):
     _check_large_map(OV, dtype, cuda, weights, counts, tol32=5e-5)
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("B", [2, 50, 1024])
+@pytest.mark.parametrize("case", ["uniform", "random", "zeros"])
+def test_small_map_cases_match_oracle(case, B, dtype, cuda):
+    """One-CTA-per-row map update (at most 1024 intervals): uniform weights
+    (every cumulative sum an exact multiple of delta), random weights, and
+    empty intervals."""
+    from oracle import vegas as OV
+
+    rng = np.random.default_rng({"uniform": 11, "random": 12, "zeros": 13}[case] + B)
+    d = 4
+    counts = rng.integers(1, 30, size=(d, B)).astype(np.int64)
+    if case == "uniform":
+        weights = 2.5 * counts.astype(np.float64)
+    else:
+        weights = rng.uniform(0.05, 4.0, size=(d, B)) * counts
+    if case == "zeros" and B > 2:
+        z = rng.random((d, B)) < 0.35
+        z[:, 0] = True
+        counts[z] = 0
+        weights[z] = 0.0
+    _check_large_map(OV, dtype, cuda, weights, counts)
+
+
 def test_default_interval_count_vegas(cuda):
     """The reference's default map size (N_increment // 10 intervals) at a
     size that takes the large-map path."""

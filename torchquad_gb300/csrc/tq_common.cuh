@@ -112,22 +112,32 @@ __device__ __forceinline__ F2 f2_add(F2 a, float b) {
 __device__ __forceinline__ F2 f2_shfl_down(F2 a, int off) {
   return F2{__shfl_down_sync(0xffffffffu, a.hi, off), __shfl_down_sync(0xffffffffu, a.lo, off)};
 }
+__device__ __forceinline__ F2 f2_shfl_up(F2 a, int off) {
+  return F2{__shfl_up_sync(0xffffffffu, a.hi, off), __shfl_up_sync(0xffffffffu, a.lo, off)};
+}
 __device__ __forceinline__ double f2_value(F2 a) { return (double)a.hi + (double)a.lo; }
+// The double-float rounded to the nearest float.
+__device__ __forceinline__ float f2_round(F2 a) { return __fadd_rn(a.hi, a.lo); }
 
 // "Last CTA finishes" pattern: every CTA writes its partial, fences, takes a
 // ticket; the CTA that draws the last ticket reduces all partials in index
 // order (deterministic) and resets the ticket for the next launch.  No CTA
 // waits on another, so nothing can spin.
-__device__ __forceinline__ bool last_block_arrives(unsigned* ticket) {
+// `count` CTAs take part (a kernel whose CTAs play several roles counts
+// each role's CTAs on its own ticket).
+__device__ __forceinline__ bool last_block_of(unsigned* ticket, unsigned count) {
   __shared__ bool is_last;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned t = atomicAdd(ticket, 1u);
-    is_last = (t == gridDim.x * gridDim.y * gridDim.z - 1);
+    is_last = (t == count - 1);
   }
   __syncthreads();
   return is_last;
+}
+__device__ __forceinline__ bool last_block_arrives(unsigned* ticket) {
+  return last_block_of(ticket, gridDim.x * gridDim.y * gridDim.z);
 }
 
 // ------------------------------------------------------------ Philox4x32-10

@@ -6,6 +6,8 @@
 // Reference (torchquad v0.5.0): vegas.py (driver), vegas_map.py (adaptive
 // map), vegas_stratification.py (stratified sampling).
 
+#include <type_traits>
+
 #include "tq_vegas_sample.cuh"
 
 namespace tq {
@@ -148,15 +150,15 @@ __device__ __forceinline__ void block_sum3(double& x, double& y, double& z, doub
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
+__device__ void finish_body(const FinishArgs& a, unsigned bid, unsigned nblk) {
   __shared__ double sh[96];
   const tq_vegas_state& st = a.st;
   const double V = a.V;  // V_cubes (vegas_stratification.py:29)
   const T Vt = (T)V, V2t = (T)(V * V);
   const T beta = (T)a.beta;
   double res = 0.0, s2 = 0.0, dsum = 0.0;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < st.n_cubes;
-       c += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t c = (int64_t)bid * blockDim.x + threadIdx.x; c < st.n_cubes;
+       c += (int64_t)nblk * blockDim.x) {
     const int64_t nn = st.neval[c];
     const double J = st.jf[c], J2 = st.jf2[c];
     const double inv = 1.0 / (double)nn;
@@ -174,16 +176,16 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
   }
   block_sum3(res, s2, dsum, sh);
   if (threadIdx.x == 0) {
-    a.partials[3 * blockIdx.x] = Acc{res, 0.0};
-    a.partials[3 * blockIdx.x + 1] = Acc{s2, 0.0};
-    a.partials[3 * blockIdx.x + 2] = Acc{dsum, 0.0};
+    a.partials[3 * bid] = Acc{res, 0.0};
+    a.partials[3 * bid + 1] = Acc{s2, 0.0};
+    a.partials[3 * bid + 2] = Acc{dsum, 0.0};
   }
-  if (last_block_arrives(a.ticket) && threadIdx.x < 32) {
+  if (last_block_of(a.ticket, nblk) && threadIdx.x < 32) {
     // one warp, fixed assignment of partials to lanes and a fixed tree:
     // deterministic; the three compensated chains interleave
     const int lane = threadIdx.x;
     Acc r{0, 0}, q{0, 0}, ds{0, 0};
-    for (unsigned i = lane; i < gridDim.x; i += 32) {
+    for (unsigned i = lane; i < nblk; i += 32) {
       acc_add(r, __ldcg(&a.partials[3 * i].s));
       acc_add(q, __ldcg(&a.partials[3 * i + 1].s));
       acc_add(ds, __ldcg(&a.partials[3 * i + 2].s));
@@ -214,6 +216,11 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(kBlock) vegas_finish_kernel(FinishArgs a) {
+  finish_body<T>(a, blockIdx.x, gridDim.x);
+}
+
 // fp32 states: the per-cube terms in fp32 (the reference computes them in
 // the state's dtype), every sum as a double-float on the FP32 pipe: per
 // thread, over the CTA, and across CTAs in the last one.  The only FP64
@@ -228,14 +235,14 @@ __device__ __forceinline__ void f2_warp_sum3(F2& x, F2& y, F2& z) {
   }
 }
 
-__global__ void __launch_bounds__(kBlock) vegas_finish_f32_kernel(FinishArgs a) {
+__device__ void finish_f32_body(const FinishArgs& a, unsigned bid, unsigned nblk) {
   __shared__ F2 sh[3][kBlock / 32];
   const tq_vegas_state& st = a.st;
   const float Vt = (float)a.V, V2t = (float)(a.V * a.V);
   const float beta = (float)a.beta;
   F2 res{0.f, 0.f}, s2{0.f, 0.f}, dsum{0.f, 0.f};
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < st.n_cubes;
-       c += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t c = (int64_t)bid * blockDim.x + threadIdx.x; c < st.n_cubes;
+       c += (int64_t)nblk * blockDim.x) {
     const int64_t nn = st.neval[c];
     const float cnt = (float)nn;  // the reference's JF / neval in the state dtype
     const float jT = __double2float_rn(st.jf[c]), j2T = __double2float_rn(st.jf2[c]);
@@ -269,14 +276,14 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_f32_kernel(FinishArgs a) 
     dsum = lane < kBlock / 32 ? sh[2][lane] : zero;
     f2_warp_sum3(res, s2, dsum);
     if (lane == 0) {
-      part[6 * blockIdx.x] = res;
-      part[6 * blockIdx.x + 2] = s2;
-      part[6 * blockIdx.x + 4] = dsum;
+      part[6 * bid] = res;
+      part[6 * bid + 2] = s2;
+      part[6 * bid + 4] = dsum;
     }
   }
-  if (last_block_arrives(a.ticket) && warp == 0) {
+  if (last_block_of(a.ticket, nblk) && warp == 0) {
     F2 r{0.f, 0.f}, q{0.f, 0.f}, ds{0.f, 0.f};
-    for (unsigned i = lane; i < gridDim.x; i += 32) {  // fixed assignment and tree: deterministic
+    for (unsigned i = lane; i < nblk; i += 32) {  // fixed assignment and tree: deterministic
       const float2 pr = __ldcg((const float2*)&part[6 * i]);
       const float2 pq = __ldcg((const float2*)&part[6 * i + 2]);
       const float2 pd = __ldcg((const float2*)&part[6 * i + 4]);
@@ -302,6 +309,10 @@ __global__ void __launch_bounds__(kBlock) vegas_finish_f32_kernel(FinishArgs a) 
       *a.ticket = 0u;
     }
   }
+}
+
+__global__ void __launch_bounds__(kBlock) vegas_finish_f32_kernel(FinishArgs a) {
+  finish_f32_body(a, blockIdx.x, gridDim.x);
 }
 
 // --------------------------------------------------------- map update
@@ -751,8 +762,8 @@ inline size_t map_row_smem(int64_t B, size_t ts) {
 
 // The last CTA to arrive (all others have finished reading the weights)
 // resets the weights and counts of the whole map (_reset_weight).
-__device__ void clear_map_by_last(const tq_vegas_state& st, unsigned* ticket) {
-  if (last_block_arrives(ticket)) {
+__device__ void clear_map_by_last(const tq_vegas_state& st, unsigned* ticket, unsigned nrows) {
+  if (last_block_of(ticket, nrows)) {
     const int64_t n = (int64_t)st.dim * st.n_bins;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
       st.weights[i] = 0.0;
@@ -763,12 +774,12 @@ __device__ void clear_map_by_last(const tq_vegas_state& st, unsigned* ticket) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kRowThreads) vegas_map_rows_kernel(tq_vegas_state st, double alpha,
-                                                                      void* smooth_out, unsigned* ticket) {
+__device__ void map_rows_body(const tq_vegas_state& st, double alpha, void* smooth_out, unsigned* ticket,
+                              int k, unsigned nrows) {
   extern __shared__ __align__(16) unsigned char row_smem[];
   __shared__ double red[32];
   __shared__ int rownz[kMaxDim];
-  const int k = blockIdx.x, d = st.dim;
+  const int d = st.dim;
   const int B = (int)st.n_bins;
   T* w = (T*)row_smem;                                 // [B] averaged, filled weights
   T* wt = w + B;                                       // [B]
@@ -796,7 +807,7 @@ __global__ void __launch_bounds__(kRowThreads) vegas_map_rows_kernel(tq_vegas_st
   for (int kk = 0; kk < d; ++kk) zero_row |= !rownz[kk];
   if (zero_row) {  // the map cannot be updated (:187-196): only the reset
     if (k == 0 && threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
-    if (!smooth_out) clear_map_by_last(st, ticket);
+    if (!smooth_out) clear_map_by_last(st, ticket, nrows);
     return;
   }
   // EQ 17 and the filling of empty intervals (:118-145).  A sweep over a row
@@ -933,7 +944,267 @@ __global__ void __launch_bounds__(kRowThreads) vegas_map_rows_kernel(tq_vegas_st
   T* dxo = (T*)st.dx_edges + (int64_t)k * B;
   for (int e = threadIdx.x; e <= B; e += blockDim.x) xo[e] = nx[e];
   for (int b = threadIdx.x; b < B; b += blockDim.x) dxo[b] = sub_rn(nx[b + 1], nx[b]);  // :259
-  clear_map_by_last(st, ticket);
+  clear_map_by_last(st, ticket, nrows);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRowThreads) vegas_map_rows_kernel(tq_vegas_state st, double alpha,
+                                                                      void* smooth_out, unsigned* ticket) {
+  map_rows_body<T>(st, alpha, smooth_out, ticket, blockIdx.x, gridDim.x);
+}
+
+// fp32 maps: the same update with every fp64 sum and scan of the generic
+// kernel as a double-float on the FP32 pipe (the reference's fp64
+// cumulative sums of fp32 values are exact in both forms whenever they are
+// exact in fp64).  The delta multiple of a cumulative sum C = hi + lo is the
+// largest k with k * delta <= C, decided from the exact residual (k * delta
+// as a TwoProduct): multiples agree with the fp64 truncation except where
+// C / delta lies within about 2^-46 of an integer without being one.
+__device__ F2 f2_block_sum_all(F2 v, F2* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = f2_add(v, f2_shfl_down(v, o));
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  F2 t{0.f, 0.f};
+  for (int i = 0; i < nw; ++i) t = f2_add(t, sh[i]);
+  __syncthreads();
+  return t;
+}
+
+__device__ F2 f2_cta_exclusive_scan(F2 x, F2* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  F2 xi = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const F2 v = f2_shfl_up(xi, o);
+    if (lane >= o) xi = f2_add(v, xi);
+  }
+  F2 ex = f2_shfl_up(xi, 1);
+  if (lane == 0) ex = F2{0.f, 0.f};
+  __syncthreads();
+  if (lane == 31) sh[warp] = xi;
+  __syncthreads();
+  if (warp == 0) {
+    F2 y = lane < nw ? sh[lane] : F2{0.f, 0.f};
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const F2 v = f2_shfl_up(y, o);
+      if (lane >= o) y = f2_add(v, y);
+    }
+    F2 yx = f2_shfl_up(y, 1);
+    if (lane == 0) yx = F2{0.f, 0.f};
+    sh[lane] = yx;
+  }
+  __syncthreads();
+  const F2 r = f2_add(sh[warp], ex);
+  __syncthreads();
+  return r;
+}
+
+// C = c.hi + c.lo >= k * delta, exactly up to the last two roundings.
+__device__ __forceinline__ bool f2_at_least(F2 c, int k, float delta) {
+  const float kf = (float)k;
+  const float ph = __fmul_rn(kf, delta);
+  const float pl = __fmaf_rn(kf, delta, -ph);  // k * delta = ph + pl exactly
+  const float r = __fsub_rn(__fadd_rn(__fsub_rn(c.hi, ph), c.lo), pl);
+  return r >= 0.f;
+}
+
+__device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* smooth_out, unsigned* ticket,
+                                  int k, unsigned nrows) {
+  using T = float;
+  extern __shared__ __align__(16) unsigned char row_smem[];
+  __shared__ F2 red[32];
+  __shared__ int rownz[kMaxDim];
+  const int d = st.dim;
+  const int B = (int)st.n_bins;
+  T* w = (T*)row_smem;
+  T* wt = w + B;
+  T* sw = wt + B;
+  T* vv = sw + B;
+  T* nx = vv + (B + 1);
+  int32_t* mk = (int32_t*)(nx + (B + 1));
+  int32_t* ind = mk + B;
+  unsigned char* z = (unsigned char*)(ind + (B + 1));
+  unsigned char* zt = z + B;
+  if (threadIdx.x < d) rownz[threadIdx.x] = 0;
+  __syncthreads();
+  for (int kk = 0; kk < d; ++kk) {
+    int nz = 0;
+    for (int b = threadIdx.x; b < B; b += blockDim.x) {
+      const int64_t c = st.counts[(int64_t)kk * B + b];
+      const T wi = (T)st.weights[(int64_t)kk * B + b];
+      nz |= (c == 0 ? wi : div_rn(wi, (T)c)) != (T)0;
+    }
+    if (nz) rownz[kk] = 1;
+  }
+  __syncthreads();
+  int zero_row = 0;
+  for (int kk = 0; kk < d; ++kk) zero_row |= !rownz[kk];
+  if (zero_row) {
+    if (k == 0 && threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
+    if (!smooth_out) clear_map_by_last(st, ticket, nrows);
+    return;
+  }
+  int anyz = 0;
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {
+    const int64_t c = st.counts[(int64_t)k * B + b];
+    const T wi = (T)st.weights[(int64_t)k * B + b];
+    z[b] = c == 0;
+    anyz |= c == 0;
+    w[b] = c == 0 ? wi : div_rn(wi, (T)c);
+  }
+  if (__syncthreads_or(anyz)) {
+    for (int sweep = 0; sweep < 10; ++sweep) {
+      for (int b = threadIdx.x; b < B; b += blockDim.x) {
+        wt[b] = (b < B - 1 && z[b]) ? w[b + 1] : w[b];
+        zt[b] = (b < B - 1) ? (z[b] && z[b + 1]) : z[b];
+      }
+      __syncthreads();
+      int left = 0;
+      for (int b = threadIdx.x; b < B; b += blockDim.x) {
+        w[b] = (b > 0 && zt[b]) ? wt[b - 1] : wt[b];
+        z[b] = (b > 0) ? (zt[b] && zt[b - 1]) : zt[b];
+        left |= z[b];
+      }
+      if (!__syncthreads_or(left)) break;
+    }
+  }
+  F2 acc{0.f, 0.f};
+  for (int b = threadIdx.x; b < B; b += blockDim.x) acc = f2_add(acc, w[b]);
+  const T sum = f2_round(f2_block_sum_all(acc, red));  // :151
+  acc = F2{0.f, 0.f};
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {  // EQ 18-19
+    T v;
+    if (b == 0)
+      v = add_rn(mul_rn((T)7, w[0]), w[1]);
+    else if (b == B - 1)
+      v = add_rn(w[B - 2], mul_rn((T)7, w[B - 1]));
+    else
+      v = add_rn(add_rn(w[b - 1], mul_rn((T)6, w[b])), w[b + 1]);
+    v = div_rn(v, mul_rn((T)8, sum));
+    if (v != (T)0) {
+      const T t = div_rn(sub_rn(v, (T)1), logf(v));
+      v = alpha == 0.5 ? sqrtf(t) : powf(t, (T)alpha);
+    }
+    sw[b] = v;
+    acc = f2_add(acc, v);
+    if (smooth_out) ((T*)smooth_out)[(int64_t)k * B + b] = v;
+  }
+  if (smooth_out) return;
+  const T delta = div_rn(f2_round(f2_block_sum_all(acc, red)), (T)B);  // :201
+  // :210-213: cumulative sums of sw[:-1], their delta multiples
+  const int b0 = threadIdx.x * kRowPer;
+  T x[kRowPer];
+  F2 s{0.f, 0.f};
+#pragma unroll
+  for (int j = 0; j < kRowPer; ++j) {
+    x[j] = b0 + j < B - 1 ? sw[b0 + j] : (T)0;
+    s = f2_add(s, x[j]);
+  }
+  F2 cum = f2_cta_exclusive_scan(s, red);
+#pragma unroll
+  for (int j = 0; j < kRowPer; ++j) {
+    if (b0 + j < B - 1) {
+      cum = f2_add(cum, x[j]);
+      int q = (int)floorf(__fdiv_rn(cum.hi, delta));
+      q = q < 0 ? 0 : (q > B + 1 ? B + 1 : q);
+      if (q > 0 && !f2_at_least(cum, q, delta)) --q;
+      else if (f2_at_least(cum, q + 1, delta)) ++q;
+      mk[b0 + j] = q > B ? B : q;
+    }
+  }
+  for (int e = threadIdx.x; e <= B; e += blockDim.x) {
+    vv[e] = (T)0;
+    ind[e] = 0;
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {  // :214-230
+    const int from = b == 0 ? 0 : mk[b - 1];
+    const int to = b == B - 1 ? B + 1 : mk[b];
+    for (int e = from; e < to; ++e) ind[e] = b;
+    if (b < B - 1 && (b == 0 || mk[b] != mk[b - 1])) {
+      const int q = mk[b];
+      T a = (T)0;
+      for (int e = b; e < B - 1 && mk[e] == q; ++e) a = add_rn(a, sw[e]);
+      vv[q] = a;
+    }
+  }
+  __syncthreads();
+  // :233 d_accu and EQ 22
+  const T* xe = (const T*)st.x_edges + (int64_t)k * (B + 1);
+  const T* dxe = (const T*)st.dx_edges + (int64_t)k * B;
+  s = F2{0.f, 0.f};
+#pragma unroll
+  for (int j = 0; j < kRowPer; ++j) {
+    x[j] = b0 + j < B - 1 ? sub_rn(delta, vv[b0 + j]) : (T)0;
+    s = f2_add(s, x[j]);
+  }
+  cum = f2_cta_exclusive_scan(s, red);
+#pragma unroll
+  for (int j = 0; j < kRowPer; ++j) {
+    const int e = b0 + j;
+    if (e < B - 1) {
+      cum = f2_add(cum, x[j]);
+      int ii = ind[e];
+      ii = ii < 0 ? 0 : (ii > B - 1 ? B - 1 : ii);
+      nx[e + 1] = add_rn(xe[ii], mul_rn(div_rn(f2_round(cum), sw[ii]), dxe[ii]));
+    }
+  }
+  if (threadIdx.x == 0) {
+    nx[0] = xe[0];
+    nx[B] = xe[B];
+  }
+  __syncthreads();
+  int bad = 0;
+  for (int e = threadIdx.x; e <= B; e += blockDim.x) bad |= !isfinite(nx[e]);
+  if (__syncthreads_or(bad)) {
+    if (threadIdx.x == 0) {
+      atomicAdd(st.flags + 1, 1);
+      for (int e = 1; e < B; ++e) vv[e] = mul_rn((T)0.5, add_rn(nx[e - 1], nx[e + 1]));
+      for (int e = 1; e < B; ++e)
+        if (!isfinite(nx[e])) nx[e] = vv[e];
+      for (int e = 0; e <= B; ++e)
+        if (!isfinite(nx[e])) {
+          atomicAdd(st.flags + 2, 1);
+          break;
+        }
+    }
+    __syncthreads();
+  }
+  T* xo = (T*)st.x_edges + (int64_t)k * (B + 1);
+  T* dxo = (T*)st.dx_edges + (int64_t)k * B;
+  for (int e = threadIdx.x; e <= B; e += blockDim.x) xo[e] = nx[e];
+  for (int b = threadIdx.x; b < B; b += blockDim.x) dxo[b] = sub_rn(nx[b + 1], nx[b]);  // :259
+  clear_map_by_last(st, ticket, nrows);
+}
+
+__global__ void __launch_bounds__(kRowThreads) vegas_map_rows_f32_kernel(tq_vegas_state st, double alpha,
+                                                                          void* smooth_out, unsigned* ticket) {
+  map_rows_f32_body(st, alpha, smooth_out, ticket, blockIdx.x, gridDim.x);
+}
+
+// finish_iteration and update_map in one launch (maps of at most kSmallMap
+// intervals): CTAs 0..d-1 update the map rows, the others end the
+// iteration.  The two read and write disjoint parts of the state, so they
+// run side by side; each role counts its own CTAs on its own ticket.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) vegas_finish_map_kernel(FinishArgs a, double alpha,
+                                                                  unsigned* map_ticket) {
+  const unsigned d = (unsigned)a.st.dim;
+  if (blockIdx.x < d) {
+    if constexpr (std::is_same<T, float>::value)
+      map_rows_f32_body(a.st, alpha, nullptr, map_ticket, blockIdx.x, d);
+    else
+      map_rows_body<T>(a.st, alpha, nullptr, map_ticket, blockIdx.x, d);
+  } else {
+    if constexpr (std::is_same<T, float>::value)
+      finish_f32_body(a, blockIdx.x - d, gridDim.x - d);
+    else
+      finish_body<T>(a, blockIdx.x - d, gridDim.x - d);
+  }
 }
 
 // ----------------------------------------------------------- init
@@ -1265,10 +1536,16 @@ static int launch_update_map(const tq_vegas_state* st, double alpha, void* works
     }                                                                                          \
     kfn<<<st->dim, kRowThreads, smem, s>>>(*st, alpha, smooth_out, ws.t_map);                  \
   }
-  if (st->dtype == TQ_F64)
+  if (st->dtype == TQ_F64) {
     TQ_ROWS_LAUNCH(double)
-  else
-    TQ_ROWS_LAUNCH(float)
+  } else {
+    auto kfn = vegas_map_rows_f32_kernel;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return set_cuda_error(e);
+    }
+    kfn<<<st->dim, kRowThreads, smem, s>>>(*st, alpha, smooth_out, ws.t_map);
+  }
 #undef TQ_ROWS_LAUNCH
   return launch_status();
 }
@@ -1316,6 +1593,40 @@ extern "C" int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, 
     vegas_finish_kernel<double><<<g, kBlock, 0, s>>>(a);
   else
     vegas_finish_f32_kernel<<<g, kBlock, 0, s>>>(a);
+  return launch_status();
+}
+
+extern "C" int tq_vegas_finish_update_map(const tq_vegas_state* st, double beta, double alpha,
+                                          void* workspace, size_t workspace_bytes, void* stream) {
+  if (st && st->n_bins > kSmallMap) {
+    const int rc = tq_vegas_finish_iteration(st, beta, workspace, workspace_bytes, stream);
+    if (rc != TQ_OK) return rc;
+    return tq_vegas_update_map(st, alpha, workspace, workspace_bytes, stream);
+  }
+  TQ_VEGAS_WS();
+  FinishArgs a;
+  a.st = *st;
+  a.beta = beta;
+  a.V = pow(1.0 / (double)st->n_strat, (double)st->dim);
+  a.partials = ws.partials;
+  a.ticket = ws.t_finish;
+  const unsigned g = (unsigned)finish_blocks(st) + (unsigned)st->dim;
+  const size_t smem = map_row_smem(st->n_bins, dtype_size(st->dtype));
+#define TQ_FINISH_MAP(T)                                                                      \
+  {                                                                                           \
+    auto kfn = vegas_finish_map_kernel<T>;                                                    \
+    if (smem > 48 * 1024) {                                                                   \
+      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                           (int)smem);                                        \
+      if (e != cudaSuccess) return set_cuda_error(e);                                         \
+    }                                                                                         \
+    kfn<<<g, kBlock, smem, s>>>(a, alpha, ws.t_map);                                          \
+  }
+  if (st->dtype == TQ_F64)
+    TQ_FINISH_MAP(double)
+  else
+    TQ_FINISH_MAP(float)
+#undef TQ_FINISH_MAP
   return launch_status();
 }
 

@@ -148,6 +148,18 @@ class VegasDevice:
                 "tq_vegas_finish_iteration")
         L.count_launches(1)
 
+    def finish_update_map(self, beta, alpha):
+        """finish (running statistics slot) then update_map, one launch for
+        maps of at most 1024 intervals per dimension."""
+        p, n = self._ws()
+        L.check(L.lib().tq_vegas_finish_update_map(self.ref, float(beta), float(alpha), p, n,
+                                                   L.stream_handle()), "tq_vegas_finish_update_map")
+        L.count_launches(self.finish_update_map_launches)
+
+    @property
+    def finish_update_map_launches(self):
+        return 1 if self.n_bins <= 1024 else 1 + self.update_map_launches
+
     def strat_points(self, u):
         y = torch.empty_like(u)
         L.check(L.lib().tq_vegas_strat_points(self.ref, u.data_ptr(), u.shape[0], y.data_ptr(),

@@ -78,9 +78,10 @@ class _FusedPlan:
         for _ in range(5):
             d.get_nh()
             d.iterate_fused(self.family, d.params, self.use_grid_improve)
-            d.finish(BETA)
             if self.use_grid_improve:
-                d.update_map(ALPHA)
+                d.finish_update_map(BETA, ALPHA)
+            else:
+                d.finish(BETA)
 
     def _capture(self, seq):
         g = torch.cuda.CUDAGraph()
@@ -105,7 +106,7 @@ class _FusedPlan:
     def run_block(self):
         if self.g_block is not None and not FORCE_EAGER[0]:
             self.g_block.replay()
-            L.count_launches(5 * (4 + (self.dev.update_map_launches if self.use_grid_improve else 0)))
+            L.count_launches(5 * (3 + (self.dev.finish_update_map_launches if self.use_grid_improve else 1)))
         else:
             self._block_seq()
 

@@ -155,7 +155,7 @@ class _VegasSession:
                 self.graph = g
             if self.graph is not None:
                 self.graph.replay()
-                L.count_launches(5 * (4 + d.update_map_launches))
+                L.count_launches(5 * (3 + d.finish_update_map_launches))
             else:
                 self._block()
             v.it += 5
@@ -168,8 +168,7 @@ class _VegasSession:
         for _ in range(5):
             d.get_nh()
             d.iterate_fused(self.req.integrand.family, self.params, True)
-            d.finish(BETA)
-            d.update_map(ALPHA)
+            d.finish_update_map(BETA, ALPHA)
 
     def done(self):
         """After the block's event: True if the request is finished."""
