@@ -1443,12 +1443,13 @@ static int launch_sample(const tq_vegas_state* st, int family, const double* par
   a.edges_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, true) <= limit;
   const size_t smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, a.edges_smem);
   const int64_t cap = (int64_t)sm_count() * TQ_SAMPLE_MIN_BLOCKS;  // resident CTAs
-  int64_t tiles = max_points > 0 ? (max_points + kTile - 1) / kTile : cap;
+  // known point counts (warm-up): about two 32-point tiles per warp
+  int64_t tiles = max_points > 0 ? (max_points + 2 * kTile - 1) / (2 * kTile) : cap;
   if (tiles > cap) tiles = cap;
   if (tiles < 1) tiles = 1;
   const dim3 grid((unsigned)tiles);
-  if (st->dtype == TQ_F32 && !warm && st->dim <= 8)
-    return launch_sample_f32_dims(a, family, st->dim, grid.x, smem, s);
+  if (st->dtype == TQ_F32 && st->dim <= 8)
+    return launch_sample_f32_dims(a, family, st->dim, warm, grid.x, smem, s);
 #define TQ_SAMPLE_LAUNCH(T, WARMB)                                                          \
   {                                                                                         \
     auto kfn = vegas_sample_kernel<T, FAM, WARMB, 0>;                                       \

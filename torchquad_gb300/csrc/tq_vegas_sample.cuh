@@ -383,9 +383,9 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
   }
 }
 
-// fp32 iterations with 1 <= dim <= 8: the dimension-specialised sampler
-// (tq_vegas_sample_d.cu).
-int launch_sample_f32_dims(const SampleArgs& a, int family, int dim, unsigned grid, size_t smem,
-                           cudaStream_t s);
+// fp32 states with 1 <= dim <= 8: the dimension-specialised sampler
+// (tq_vegas_sample_d.cu), iterations and warm-up.
+int launch_sample_f32_dims(const SampleArgs& a, int family, int dim, bool warm, unsigned grid,
+                           size_t smem, cudaStream_t s);
 
 }  // namespace tq
