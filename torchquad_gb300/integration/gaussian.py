@@ -20,6 +20,12 @@ from .. import _lib as L
 from .grid_integrator import GridIntegrator
 
 
+# Gauss-Legendre roots/weights and their device copies, shared by instances
+# that use numpy's leggauss (a pure function of n).
+_LEGGAUSS = {}
+_GL_DEVICE = {}
+
+
 class Gaussian(GridIntegrator):
     """Gauss-Legendre on [-1, 1] by default; base of custom Gaussian rules.
 
@@ -75,11 +81,19 @@ class Gaussian(GridIntegrator):
                 raise NotImplementedError(f"N {N} is not an int and lacks an `item` method")
         if root_args in self._cache:
             return self._cache[root_args]
-        if self._root_fn is numpy.polynomial.legendre.leggauss and root_args[0] > 20000:
+        default = self._root_fn is numpy.polynomial.legendre.leggauss
+        if default and root_args[0] > 20000:
             raise ValueError(
                 f"{root_args[0]} Gauss-Legendre nodes per dimension: numpy.polynomial.legendre.leggauss "
                 "builds an n x n matrix; use at most 20000")
-        self._cache[root_args] = self._root_fn(*root_args)
+        # leggauss is a pure function of n: its results are shared by all
+        # instances (the reference caches per instance)
+        if default and root_args in _LEGGAUSS:
+            self._cache[root_args] = _LEGGAUSS[root_args]
+        else:
+            self._cache[root_args] = self._root_fn(*root_args)
+            if default:
+                _LEGGAUSS[root_args] = self._cache[root_args]
         return self._cache[root_args]
 
     @staticmethod
@@ -93,14 +107,19 @@ class Gaussian(GridIntegrator):
     # ---- kernel plumbing
     def _gl_tables(self, n, device):
         key = (n, self._root_args, str(device))
+        shared = self._root_fn is numpy.polynomial.legendre.leggauss
         t = self._dev_cache.get(key)
+        if t is None and shared:
+            t = _GL_DEVICE.get(key)
         if t is None:
             r, w = self._cached_points_and_weights(n)
             t = (
                 torch.as_tensor(numpy.asarray(r, dtype=numpy.float64)).to(device),
                 torch.as_tensor(numpy.asarray(w, dtype=numpy.float64)).to(device),
             )
-            self._dev_cache[key] = t
+            if shared:
+                _GL_DEVICE[key] = t
+        self._dev_cache[key] = t
         return t
 
     def _result_dtype(self, domain):

@@ -8,6 +8,7 @@ current CUDA device, where every kernel of this package runs.
 from __future__ import annotations
 
 import warnings
+import weakref
 
 import torch
 
@@ -49,9 +50,35 @@ def _check_integration_domain(integration_domain):
         raise ValueError("integration_domain must have 2 values per boundary")
     if torch.jit.is_tracing():
         return dim
+    if _validated(integration_domain):
+        return dim
     if torch.min(integration_domain[:, 1] - integration_domain[:, 0]) < 0.0:
         raise ValueError("integration_domain has invalid boundary values")
+    _remember_valid(integration_domain)
     return dim
+
+
+# Device tensors already found valid, by identity, with the autograd version
+# counter (bumped by every in-place write) and the storage address at the
+# time: the check of a device tensor reads its values back (a device
+# synchronisation), so an unchanged tensor is not checked again.
+_VALID = {}
+
+
+def _validated(t):
+    e = _VALID.get(id(t))
+    return e is not None and e[0]() is t and e[1] == t._version and e[2] == t.data_ptr()
+
+
+def _remember_valid(t):
+    if t.device.type != "cuda":
+        return
+    key = id(t)
+    try:
+        ref = weakref.ref(t, lambda _r, k=key: _VALID.pop(k, None))
+    except TypeError:
+        return
+    _VALID[key] = (ref, t._version, t.data_ptr())
 
 
 def _setup_integration_domain(dim, integration_domain, backend):
