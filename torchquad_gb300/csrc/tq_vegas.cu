@@ -757,7 +757,7 @@ constexpr int kRowThreads = 256;
 constexpr int kRowPer = kSmallMap / kRowThreads;  // consecutive intervals per thread in the scans
 
 inline size_t map_row_smem(int64_t B, size_t ts) {
-  return (((5 * B + 2) * ts + (2 * B + 1) * 4 + 2 * B) + 15) & ~size_t(15);
+  return (((6 * B + 3) * ts + (2 * B + 1) * 4 + 2 * B) + 15) & ~size_t(15);
 }
 
 // The last CTA to arrive (all others have finished reading the weights)
@@ -1025,18 +1025,32 @@ __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* 
   T* sw = wt + B;
   T* vv = sw + B;
   T* nx = vv + (B + 1);
-  int32_t* mk = (int32_t*)(nx + (B + 1));
+  T* xs = nx + (B + 1);  // [B+1] old edges
+  int32_t* mk = (int32_t*)(xs + (B + 1));
   int32_t* ind = mk + B;
   unsigned char* z = (unsigned char*)(ind + (B + 1));
   unsigned char* zt = z + B;
+  // one pass over global memory for the weights: the zero-row test over
+  // every row with this row's averages and empty intervals
   if (threadIdx.x < d) rownz[threadIdx.x] = 0;
   __syncthreads();
+  const T* xe_g = (const T*)st.x_edges + (int64_t)k * (B + 1);
+  const T* dxe_g = (const T*)st.dx_edges + (int64_t)k * B;
+  T* xe = xs;   // old edges
+  T* dxe = wt;  // old widths (wt is free once the fill sweeps are done)
+  int anyz = 0;
   for (int kk = 0; kk < d; ++kk) {
     int nz = 0;
     for (int b = threadIdx.x; b < B; b += blockDim.x) {
       const int64_t c = st.counts[(int64_t)kk * B + b];
       const T wi = (T)st.weights[(int64_t)kk * B + b];
-      nz |= (c == 0 ? wi : div_rn(wi, (T)c)) != (T)0;
+      const T av = c == 0 ? wi : div_rn(wi, (T)c);
+      nz |= av != (T)0;
+      if (kk == k) {
+        z[b] = c == 0;
+        anyz |= c == 0;
+        w[b] = av;
+      }
     }
     if (nz) rownz[kk] = 1;
   }
@@ -1047,14 +1061,6 @@ __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* 
     if (k == 0 && threadIdx.x == 0) atomicAdd(st.flags + 0, 1);
     if (!smooth_out) clear_map_by_last(st, ticket, nrows);
     return;
-  }
-  int anyz = 0;
-  for (int b = threadIdx.x; b < B; b += blockDim.x) {
-    const int64_t c = st.counts[(int64_t)k * B + b];
-    const T wi = (T)st.weights[(int64_t)k * B + b];
-    z[b] = c == 0;
-    anyz |= c == 0;
-    w[b] = c == 0 ? wi : div_rn(wi, (T)c);
   }
   if (__syncthreads_or(anyz)) {
     for (int sweep = 0; sweep < 10; ++sweep) {
@@ -1071,6 +1077,10 @@ __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* 
       }
       if (!__syncthreads_or(left)) break;
     }
+  }
+  if (!smooth_out) {  // the old edges, read while the weights are smoothed
+    for (int e = threadIdx.x; e <= B; e += blockDim.x) xe[e] = xe_g[e];
+    for (int b = threadIdx.x; b < B; b += blockDim.x) dxe[b] = dxe_g[b];
   }
   F2 acc{0.f, 0.f};
   for (int b = threadIdx.x; b < B; b += blockDim.x) acc = f2_add(acc, w[b]);
@@ -1134,8 +1144,6 @@ __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* 
   }
   __syncthreads();
   // :233 d_accu and EQ 22
-  const T* xe = (const T*)st.x_edges + (int64_t)k * (B + 1);
-  const T* dxe = (const T*)st.dx_edges + (int64_t)k * B;
   s = F2{0.f, 0.f};
 #pragma unroll
   for (int j = 0; j < kRowPer; ++j) {
