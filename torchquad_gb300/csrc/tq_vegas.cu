@@ -757,13 +757,19 @@ constexpr int kRowThreads = 256;
 constexpr int kRowPer = kSmallMap / kRowThreads;  // consecutive intervals per thread in the scans
 
 inline size_t map_row_smem(int64_t B, size_t ts) {
-  return (((6 * B + 3) * ts + (2 * B + 1) * 4 + 2 * B) + 15) & ~size_t(15);
+  return (((7 * B + 3) * ts + (2 * B + 1) * 4 + 2 * B) + 15) & ~size_t(15);
 }
 
 // The last CTA to arrive (all others have finished reading the weights)
-// resets the weights and counts of the whole map (_reset_weight).
+// resets the weights and counts of the whole map (_reset_weight).  It reads
+// nothing the other CTAs wrote, and their reads of the weights were consumed
+// before they took their tickets, so the ticket needs no fence.
 __device__ void clear_map_by_last(const tq_vegas_state& st, unsigned* ticket, unsigned nrows) {
-  if (last_block_of(ticket, nrows)) {
+  __shared__ bool is_last;
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = atomicAdd(ticket, 1u) == nrows - 1;
+  __syncthreads();
+  if (is_last) {
     const int64_t n = (int64_t)st.dim * st.n_bins;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
       st.weights[i] = 0.0;
@@ -967,10 +973,14 @@ __device__ F2 f2_block_sum_all(F2 v, F2* sh) {
   __syncthreads();
   if (lane == 0) sh[warp] = v;
   __syncthreads();
-  F2 t{0.f, 0.f};
-  for (int i = 0; i < nw; ++i) t = f2_add(t, sh[i]);
+  if (warp == 0) {  // the warp partials in a fixed tree
+    F2 t = lane < nw ? sh[lane] : F2{0.f, 0.f};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t = f2_add(t, f2_shfl_down(t, o));
+    if (lane == 0) sh[32] = t;
+  }
   __syncthreads();
-  return t;
+  return sh[32];
 }
 
 __device__ F2 f2_cta_exclusive_scan(F2 x, F2* sh) {
@@ -1016,7 +1026,7 @@ __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* 
                                   int k, unsigned nrows) {
   using T = float;
   extern __shared__ __align__(16) unsigned char row_smem[];
-  __shared__ F2 red[32];
+  __shared__ F2 red[33];
   __shared__ int rownz[kMaxDim];
   const int d = st.dim;
   const int B = (int)st.n_bins;
@@ -1025,34 +1035,35 @@ __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* 
   T* sw = wt + B;
   T* vv = sw + B;
   T* nx = vv + (B + 1);
-  T* xs = nx + (B + 1);  // [B+1] old edges
-  int32_t* mk = (int32_t*)(xs + (B + 1));
+  T* xe = nx + (B + 1);  // [B+1] old edges
+  T* dxe = xe + (B + 1);  // [B] old widths
+  int32_t* mk = (int32_t*)(dxe + B);
   int32_t* ind = mk + B;
   unsigned char* z = (unsigned char*)(ind + (B + 1));
   unsigned char* zt = z + B;
-  // one pass over global memory for the weights: the zero-row test over
-  // every row with this row's averages and empty intervals
+  // one pass over global memory: the zero-row test over every row (all
+  // elements of the map at once), this row's averages and empty intervals,
+  // and this row's edges
   if (threadIdx.x < d) rownz[threadIdx.x] = 0;
   __syncthreads();
   const T* xe_g = (const T*)st.x_edges + (int64_t)k * (B + 1);
   const T* dxe_g = (const T*)st.dx_edges + (int64_t)k * B;
-  T* xe = xs;   // old edges
-  T* dxe = wt;  // old widths (wt is free once the fill sweeps are done)
+  if (!smooth_out) {
+    for (int e = threadIdx.x; e <= B; e += blockDim.x) xe[e] = xe_g[e];
+    for (int b = threadIdx.x; b < B; b += blockDim.x) dxe[b] = dxe_g[b];
+  }
   int anyz = 0;
-  for (int kk = 0; kk < d; ++kk) {
-    int nz = 0;
-    for (int b = threadIdx.x; b < B; b += blockDim.x) {
-      const int64_t c = st.counts[(int64_t)kk * B + b];
-      const T wi = (T)st.weights[(int64_t)kk * B + b];
-      const T av = c == 0 ? wi : div_rn(wi, (T)c);
-      nz |= av != (T)0;
-      if (kk == k) {
-        z[b] = c == 0;
-        anyz |= c == 0;
-        w[b] = av;
-      }
+  for (int i = threadIdx.x; i < d * B; i += blockDim.x) {
+    const int64_t c = st.counts[i];
+    const T wi = (T)st.weights[i];
+    const T av = c == 0 ? wi : div_rn(wi, (T)c);
+    const int kk = i / B, b = i - kk * B;
+    if (av != (T)0 && !rownz[kk]) rownz[kk] = 1;
+    if (kk == k) {
+      z[b] = c == 0;
+      anyz |= c == 0;
+      w[b] = av;
     }
-    if (nz) rownz[kk] = 1;
   }
   __syncthreads();
   int zero_row = 0;
@@ -1078,10 +1089,6 @@ __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* 
       if (!__syncthreads_or(left)) break;
     }
   }
-  if (!smooth_out) {  // the old edges, read while the weights are smoothed
-    for (int e = threadIdx.x; e <= B; e += blockDim.x) xe[e] = xe_g[e];
-    for (int b = threadIdx.x; b < B; b += blockDim.x) dxe[b] = dxe_g[b];
-  }
   F2 acc{0.f, 0.f};
   for (int b = threadIdx.x; b < B; b += blockDim.x) acc = f2_add(acc, w[b]);
   const T sum = f2_round(f2_block_sum_all(acc, red));  // :151
@@ -1105,26 +1112,20 @@ __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* 
   }
   if (smooth_out) return;
   const T delta = div_rn(f2_round(f2_block_sum_all(acc, red)), (T)B);  // :201
-  // :210-213: cumulative sums of sw[:-1], their delta multiples
-  const int b0 = threadIdx.x * kRowPer;
-  T x[kRowPer];
+  // :210-213: cumulative sums of sw[:-1] (each thread a contiguous chunk,
+  // one interval for maps up to 257 intervals), their delta multiples
+  const int per = (B - 1 + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int b0 = threadIdx.x * per, b1 = min(B - 1, b0 + per);
   F2 s{0.f, 0.f};
-#pragma unroll
-  for (int j = 0; j < kRowPer; ++j) {
-    x[j] = b0 + j < B - 1 ? sw[b0 + j] : (T)0;
-    s = f2_add(s, x[j]);
-  }
+  for (int b = b0; b < b1; ++b) s = f2_add(s, sw[b]);
   F2 cum = f2_cta_exclusive_scan(s, red);
-#pragma unroll
-  for (int j = 0; j < kRowPer; ++j) {
-    if (b0 + j < B - 1) {
-      cum = f2_add(cum, x[j]);
-      int q = (int)floorf(__fdiv_rn(cum.hi, delta));
-      q = q < 0 ? 0 : (q > B + 1 ? B + 1 : q);
-      if (q > 0 && !f2_at_least(cum, q, delta)) --q;
-      else if (f2_at_least(cum, q + 1, delta)) ++q;
-      mk[b0 + j] = q > B ? B : q;
-    }
+  for (int b = b0; b < b1; ++b) {
+    cum = f2_add(cum, sw[b]);
+    int q = (int)floorf(__fdiv_rn(cum.hi, delta));
+    q = q < 0 ? 0 : (q > B + 1 ? B + 1 : q);
+    if (q > 0 && !f2_at_least(cum, q, delta)) --q;
+    else if (f2_at_least(cum, q + 1, delta)) ++q;
+    mk[b] = q > B ? B : q;
   }
   for (int e = threadIdx.x; e <= B; e += blockDim.x) {
     vv[e] = (T)0;
@@ -1145,21 +1146,13 @@ __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha, void* 
   __syncthreads();
   // :233 d_accu and EQ 22
   s = F2{0.f, 0.f};
-#pragma unroll
-  for (int j = 0; j < kRowPer; ++j) {
-    x[j] = b0 + j < B - 1 ? sub_rn(delta, vv[b0 + j]) : (T)0;
-    s = f2_add(s, x[j]);
-  }
+  for (int e = b0; e < b1; ++e) s = f2_add(s, sub_rn(delta, vv[e]));
   cum = f2_cta_exclusive_scan(s, red);
-#pragma unroll
-  for (int j = 0; j < kRowPer; ++j) {
-    const int e = b0 + j;
-    if (e < B - 1) {
-      cum = f2_add(cum, x[j]);
-      int ii = ind[e];
-      ii = ii < 0 ? 0 : (ii > B - 1 ? B - 1 : ii);
-      nx[e + 1] = add_rn(xe[ii], mul_rn(div_rn(f2_round(cum), sw[ii]), dxe[ii]));
-    }
+  for (int e = b0; e < b1; ++e) {
+    cum = f2_add(cum, sub_rn(delta, vv[e]));
+    int ii = ind[e];
+    ii = ii < 0 ? 0 : (ii > B - 1 ? B - 1 : ii);
+    nx[e + 1] = add_rn(xe[ii], mul_rn(div_rn(f2_round(cum), sw[ii]), dxe[ii]));
   }
   if (threadIdx.x == 0) {
     nx[0] = xe[0];
