@@ -81,3 +81,55 @@ def test_builtin_integrands_match_oracle_on_cpu():
         got = f(x).numpy()
         want = OI.evaluate(f.family, f.params_vector().numpy(), x.numpy())
         assert np.allclose(got, want, rtol=1e-15, atol=0)
+
+
+def test_batch_pack_layout():
+    """Host packing of a batch (numpy only): descriptor fields, offsets, the
+    tile prefix and domain checks, against a per-integral loop."""
+    import numpy as np
+
+    from torchquad_gb300 import batch as B
+
+    rng = np.random.default_rng(0)
+    fs, rules, Ns, doms = [], [], [], []
+    names = ["trapezoid", "simpson", "boole", "gausslegendre"]
+    for i in range(40):
+        d = int(rng.integers(1, 5))
+        fs.append(tq.GaussianPeak(d, a=rng.uniform(0.5, 5, d).tolist(), u=rng.uniform(0, 1, d).tolist()))
+        rules.append(names[i % 4])
+        Ns.append(int(10 ** rng.uniform(2, 4)))
+        lo = rng.uniform(-1, 0, d)
+        doms.append(np.stack([lo, lo + rng.uniform(0.5, 2, d)], axis=1).tolist())
+    desc, ts, par, dom, gln, glw, fam, tp = B.pack(fs, rules, Ns, doms, torch.float64, 1000)
+    po = do = 0
+    gl = {}
+    for i, (f, r, N) in enumerate(zip(fs, rules, Ns)):
+        rid = B.rule_id(r)
+        n = B.points_per_dim(rid, f.dim, N)
+        assert tuple(desc[i])[:4] == (rid, f.dim, n, n ** f.dim)
+        assert desc[i]["par_off"] == po and desc[i]["dom_off"] == do
+        assert np.array_equal(par[po:po + 2 + 2 * f.dim], f.params_vector().numpy())
+        assert np.array_equal(dom[do:do + 2 * f.dim], np.asarray(doms[i]).ravel())
+        if rid == 3:
+            if n not in gl:
+                gl[n] = int(desc[i]["gl_off"])
+            assert np.array_equal(gln[gl[n]:gl[n] + n], np.polynomial.legendre.leggauss(n)[0])
+        po += 2 + 2 * f.dim
+        do += 2 * f.dim
+    assert ts[0] == 0 and np.array_equal(np.diff(ts), (desc["total"] + 999) // 1000)
+    bad = [list(map(list, dm)) for dm in doms]
+    bad[7][0] = [1.0, 0.0]
+    with pytest.raises(ValueError, match="integral 7"):
+        B.pack(fs, rules, Ns, bad, torch.float64, 1000)
+
+
+def test_integrand_parameter_vector_cache():
+    """The cached host parameter vector follows in-place writes."""
+    import numpy as np
+
+    f = tq.GaussianPeak(3, a=[1.0, 2.0, 3.0], u=[0.1, 0.2, 0.3], c=2.0)
+    assert np.array_equal(f.params_numpy(), f.params_vector().numpy())
+    f.a[1] = 7.0
+    assert f.params_numpy()[3] == 7.0
+    g = tq.Oscillatory(2, a=[1.0, -1.0], b=torch.tensor(0.3, dtype=torch.float64))
+    assert np.array_equal(g.params_numpy(), g.params_vector().numpy())

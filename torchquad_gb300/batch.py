@@ -87,6 +87,81 @@ def _gl(n):
     return t
 
 
+_N_CACHE = {}
+
+
+def _n_for(rid, dim, N):
+    key = (rid, dim, N)
+    n = _N_CACHE.get(key)
+    if n is None:
+        n = _N_CACHE[key] = points_per_dim(rid, dim, N)
+    return n
+
+
+def pack(integrands, rules, Ns, domains, dtype, tile_pts):
+    """Host side of a batch (numpy only): descriptors, tile prefix, packed
+    parameters, domains (in the batch dtype) and Gauss-Legendre tables."""
+    m = len(integrands)
+    if not (len(rules) == len(Ns) == len(domains) == m) or m == 0:
+        raise ValueError("integrands, rules, Ns and domains must have the same non-zero length")
+    family = None
+    for f in integrands:
+        if not isinstance(f, BuiltinIntegrand) or (family is not None and f.family != family):
+            raise ValueError("one batch takes built-in integrands of a single family")
+        family = f.family
+    rule_cache = {}
+    desc = np.zeros(m, dtype=DESC_DTYPE)
+    dims = np.fromiter((f.dim for f in integrands), dtype=np.int64, count=m)
+    if dims.min() < 1 or dims.max() > L.TQ_MAX_DIM:
+        i = int(np.argmax((dims < 1) | (dims > L.TQ_MAX_DIM)))
+        raise ValueError(f"integral {i}: dim {int(dims[i])} out of range")
+    rids = np.empty(m, dtype=np.int32)
+    ns = np.empty(m, dtype=np.int64)
+    for i, (r, N) in enumerate(zip(rules, Ns)):
+        rid = rule_cache.get(r) if isinstance(r, (str, int)) else None
+        if rid is None:
+            rid = rule_id(r)
+            if isinstance(r, (str, int)):
+                rule_cache[r] = rid
+        rids[i] = rid
+        ns[i] = _n_for(rid, int(dims[i]), int(N))
+    dom = np.concatenate([np.asarray(d, dtype=np.float64).reshape(-1) for d in domains])
+    if dom.size != 2 * int(dims.sum()):
+        raise ValueError("each integration_domain must have dim rows of [low, high]")
+    bad = dom[1::2] < dom[0::2]
+    if bad.any():
+        edge = int(np.argmax(bad))
+        i = int(np.searchsorted(np.cumsum(dims), edge, side="right"))
+        raise ValueError(f"integral {i}: integration_domain has invalid boundary values")
+    pars = [f.params_numpy() for f in integrands]
+    psize = np.fromiter((p.size for p in pars), dtype=np.int64, count=m)
+    par = np.concatenate(pars)
+    gl_index, gln, glw, gl_off = {}, [], [], 0
+    goff = np.zeros(m, dtype=np.int64)
+    for i in np.nonzero(rids == L.TQ_RULE_GAUSS)[0]:
+        n = int(ns[i])
+        if n not in gl_index:
+            rr, ww = _gl(n)
+            gl_index[n] = gl_off
+            gln.append(rr)
+            glw.append(ww)
+            gl_off += n
+        goff[i] = gl_index[n]
+    desc["rule"] = rids
+    desc["dim"] = dims
+    desc["n"] = ns
+    desc["total"] = ns ** dims
+    desc["par_off"] = np.concatenate([[0], np.cumsum(psize)[:-1]])
+    desc["dom_off"] = np.concatenate([[0], np.cumsum(2 * dims)[:-1]])
+    desc["gl_off"] = goff
+    tiles = (desc["total"] + tile_pts - 1) // tile_pts
+    ts = np.zeros(m + 1, dtype=np.int64)
+    np.cumsum(tiles, out=ts[1:])
+    npdt = np.float32 if dtype == torch.float32 else np.float64
+    glcat = (np.concatenate(gln), np.concatenate(glw)) if gln else (np.zeros(1), np.zeros(1))
+    return desc, ts, par, dom.astype(npdt), glcat[0], glcat[1], family, tile_pts
+
+
 @dataclass
 class BatchPlan:
     """Device-resident packed batch (reusable across calls)."""
@@ -163,48 +238,9 @@ class BatchedGrid:
         integrands of one family; rules: names ("simpson", ...) or TQ ids;
         Ns: total points as for integrate(N=...); domains: [dim][2] each."""
         device = L.require_cuda()
-        m = len(integrands)
-        if not (len(rules) == len(Ns) == len(domains) == m) or m == 0:
-            raise ValueError("integrands, rules, Ns and domains must have the same non-zero length")
-        fams = {f.family for f in integrands}
-        if len(fams) != 1 or not all(isinstance(f, BuiltinIntegrand) for f in integrands):
-            raise ValueError("one batch takes built-in integrands of a single family")
-        family = fams.pop()
-        tile_pts = int(tile_points or self.default_shape[2])
-        desc = np.zeros(m, dtype=DESC_DTYPE)
-        par, dom, gln, glw = [], [], [], []
-        par_off = dom_off = gl_off = 0
-        gl_index = {}
-        for i, (f, r, N, d) in enumerate(zip(integrands, rules, Ns, domains)):
-            rid = rule_id(r)
-            dim = f.dim
-            if dim < 1 or dim > L.TQ_MAX_DIM:
-                raise ValueError(f"integral {i}: dim {dim} out of range")
-            d = np.asarray(d, dtype=np.float64).reshape(dim, 2)
-            if np.any(d[:, 1] < d[:, 0]):
-                raise ValueError(f"integral {i}: integration_domain has invalid boundary values")
-            n = points_per_dim(rid, dim, int(N))
-            total = n**dim
-            g = 0
-            if rid == L.TQ_RULE_GAUSS:
-                if n not in gl_index:
-                    rr, ww = _gl(n)
-                    gl_index[n] = gl_off
-                    gln.append(rr)
-                    glw.append(ww)
-                    gl_off += n
-                g = gl_index[n]
-            pv = f.params_vector().numpy()
-            desc[i] = (rid, dim, n, total, par_off, dom_off, g)
-            par.append(pv)
-            dom.append(d.ravel())
-            par_off += pv.size
-            dom_off += 2 * dim
-        tiles = (desc["total"] + tile_pts - 1) // tile_pts
-        ts = np.zeros(m + 1, dtype=np.int64)
-        np.cumsum(tiles, out=ts[1:])
-        npdt = np.float32 if self.dtype == torch.float32 else np.float64
-        glcat = (np.concatenate(gln), np.concatenate(glw)) if gln else (np.zeros(1), np.zeros(1))
+        packed = pack(integrands, rules, Ns, domains, self.dtype, int(tile_points or self.default_shape[2]))
+        desc, ts, par, dom, gln, glw, family, tile_pts = packed
+        m = len(desc)
         total_points = int(desc["total"].sum())
         key = (self.dtype, family, int(math.log2(m)), int(math.log2(max(1, total_points))))
         return BatchPlan(
@@ -212,14 +248,14 @@ class BatchedGrid:
             family=family,
             n_int=m,
             desc_np=desc,
-            descs=torch.from_numpy(desc.view(np.uint8).copy()).to(device),
+            descs=torch.from_numpy(desc.view(np.uint8)).to(device),
             tile_start=torch.from_numpy(ts).to(device),
             n_tiles=int(ts[-1]),
             tile_pts=tile_pts,
-            params=torch.from_numpy(np.concatenate(par)).to(device),
-            domains=torch.from_numpy(np.concatenate(dom).astype(npdt)).to(device),
-            gl_nodes=torch.from_numpy(glcat[0]).to(device),
-            gl_weights=torch.from_numpy(glcat[1]).to(device),
+            params=torch.from_numpy(par).to(device),
+            domains=torch.from_numpy(dom).to(device),
+            gl_nodes=torch.from_numpy(gln).to(device),
+            gl_weights=torch.from_numpy(glw).to(device),
             total_points=total_points,
             shape_key=key,
         )

@@ -23,6 +23,7 @@ from __future__ import annotations
 
 import math
 
+import numpy as np
 import torch
 
 from . import _lib as L
@@ -61,6 +62,12 @@ class BuiltinIntegrand:
         self.b = _as_scalar(b)
         self.c = _as_scalar(c)
         self._dev_params = {}
+        self._np_key = None
+        self._np = None
+        if not any(isinstance(v, torch.Tensor) for v in (a, u, b, c)):
+            # plain numbers: the host vector without torch operations
+            self._np = np.concatenate([[float(c), float(b)], self.a.numpy(), self.u.numpy()])
+            self._np_key = self._params_key()
 
     # parameters that may carry gradients
     def parameters(self):
@@ -80,14 +87,28 @@ class BuiltinIntegrand:
             ]
         )
 
+    def _params_key(self):
+        # identity and autograd version counter (bumped by in-place writes)
+        # of each parameter tensor
+        return tuple((id(p), p._version) for p in (self.c, self.b, self.a, self.u))
+
+    def params_numpy(self):
+        """The parameter vector as a cached fp64 numpy array, refreshed when a
+        parameter tensor is replaced or written in place."""
+        key = self._params_key()
+        if key != self._np_key:
+            self._np = self.params_vector().numpy()
+            self._np_key = key
+        return self._np
+
     def device_params(self, device) -> torch.Tensor:
         """Cached device copy of the parameter vector (re-uploaded if changed)."""
-        host = self.params_vector()
+        host = self.params_numpy()
         key = (str(device),)
         cached = self._dev_params.get(key)
-        if cached is not None and torch.equal(cached[0], host):
+        if cached is not None and cached[0] is host:
             return cached[1]
-        dev = host.to(device, non_blocking=False)
+        dev = torch.from_numpy(host).to(device, non_blocking=False)
         self._dev_params[key] = (host, dev)
         return dev
 

@@ -388,7 +388,7 @@ class IntegrationServer:
                     cnt = min(self.mc_chunk, r.N - st["done_pts"])
                     desc[i] = (r.dim, 0, st["done_pts"], cnt, r.seed, 0, po, do)
                     st["chunk"] = cnt
-                    pv = r.integrand.params_vector().numpy()
+                    pv = r.integrand.params_numpy()
                     par.append(pv)
                     dom.append(np.asarray(r.domain, dtype=np.float64).ravel())
                     po += pv.size
