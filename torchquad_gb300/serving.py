@@ -8,9 +8,10 @@ time.  A scheduler thread
   the HBM budget, and releases both when the request completes;
 * launches all newly admitted Simpson requests as one batched grid launch
   (``tq_batch_grid``);
-* advances every active Monte Carlo request by one fixed-size chunk of its
-  own Philox stream per tick, all of them in one launch (``tq_batch_mc``),
-  stopping a request at its N or its target relative error;
+* advances every active Monte Carlo request by one chunk of its own Philox
+  stream per tick (chunks double from ``mc_chunk`` to ``mc_chunk_max``), all
+  of them in one launch (``tq_batch_mc``), stopping a request at its N or
+  its target relative error;
 * runs each VEGAS request on its own stream with its map and stratification
   resident on the device, one block of five iterations at a time (the
   reference's abort test, vegas.py:161-209, decides after each block), so
@@ -188,7 +189,8 @@ class _VegasSession:
 class IntegrationServer:
     """Continuous-batching integration server on one CUDA device."""
 
-    def __init__(self, hbm_budget_bytes=None, max_active=64, mc_chunk=1 << 21, mc_tile=1 << 16,
+    def __init__(self, hbm_budget_bytes=None, max_active=64, mc_chunk=1 << 21, mc_chunk_max=1 << 25,
+                 mc_tile=1 << 16,
                  grid_tile=1 << 15, device=None, streams=8):
         self.device = device or L.require_cuda()
         if hbm_budget_bytes is None:
@@ -198,6 +200,7 @@ class IntegrationServer:
         self.free_bytes = self.budget
         self.max_active = int(max_active)
         self.mc_chunk, self.mc_tile, self.grid_tile = int(mc_chunk), int(mc_tile), int(grid_tile)
+        self.mc_chunk_max = max(int(mc_chunk_max), self.mc_chunk)
         self._ids = itertools.count()
         self._pending = deque()
         self._lock = threading.Lock()
@@ -320,7 +323,8 @@ class IntegrationServer:
             if req.method == "vegas":
                 self._vegas.append(_VegasSession(req, self.device, next(self._stream_rr)))
             elif req.method == "montecarlo":
-                self._mc.append({"req": req, "done_pts": 0, "acc": [0.0, 0.0, 0.0, 0.0]})
+                self._mc.append({"req": req, "done_pts": 0, "acc": [0.0, 0.0, 0.0, 0.0],
+                                 "next_chunk": self.mc_chunk})
             else:
                 new_grid.append(req)
         if new_grid:
@@ -385,7 +389,10 @@ class IntegrationServer:
                 po = do = 0
                 for i, st in enumerate(sts):
                     r = st["req"]
-                    cnt = min(self.mc_chunk, r.N - st["done_pts"])
+                    # a request's chunks double from mc_chunk up to mc_chunk_max:
+                    # few ticks for large N, fine steps for the target-error test
+                    cnt = min(st["next_chunk"], r.N - st["done_pts"])
+                    st["next_chunk"] = min(2 * st["next_chunk"], self.mc_chunk_max)
                     desc[i] = (r.dim, 0, st["done_pts"], cnt, r.seed, 0, po, do)
                     st["chunk"] = cnt
                     pv = r.integrand.params_numpy()
