@@ -590,7 +590,18 @@ __global__ void __launch_bounds__(kMapThreads) map_multiples_kernel(tq_vegas_sta
   for (int j = 0; j < kMapPer; ++j) {
     if (b0 + j < B - 1) {
       cum += (double)v[j];
-      const int64_t q = (int64_t)(cum / delta);
+      int64_t q;
+      if constexpr (std::is_same<T, float>::value) {
+        // floor(cum / delta) without an fp64 division: a float estimate,
+        // then the exact test q * delta <= cum (q < 2^24 and delta a float,
+        // so the product is exact in fp64)
+        q = (int64_t)floorf(__fdiv_rn(__double2float_rn(cum), (float)delta));
+        q = q < 0 ? 0 : (q > B + 1 ? B + 1 : q);
+        if (q > 0 && (double)q * delta > cum) --q;
+        else if ((double)(q + 1) * delta <= cum) ++q;
+      } else {
+        q = (int64_t)(cum / delta);
+      }
       mk[b0 + j] = (int32_t)(q < 0 ? 0 : (q > B ? B : q));
     }
   }
