@@ -51,6 +51,26 @@ CONFIG = {
 }
 
 
+def reduce_over_ranks(t_local, e2e_t, evals, e2e_evals, ws, device):
+    """Replicas: the slowest rank's times (MAX) and all ranks' evaluations
+    (SUM); value = all evaluations / the slowest time."""
+    if ws <= 1:
+        return t_local, e2e_t, evals, e2e_evals
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([t_local, e2e_t], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([float(evals), float(e2e_evals)], dtype=torch.float64, device=device)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(t[1]), int(n[0]), int(n[1])
+
+
+def rank_seed(rank, k):
+    """Seed of timed integration k on a rank: distinct across ranks and steps."""
+    return rank * 1_000_003 + k
+
+
 def _dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -467,8 +487,7 @@ def run_gpu(args):
     barrier()
 
     # ---- device-resident inputs
-    clocks = ClockSampler(str(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv") if (ROOT / "gpurun_out").is_dir()
-                          else f"/tmp/tq_clocks_{rank}.csv", local)
+    clocks = ClockSampler(os.environ.get("TQ_CLOCKS_CSV", f"/tmp/tq_clocks_{rank}.csv"), local)
     step_ms, evals = [], 0
     with clocks:
         # keep the GPU under the same load for about a second first, so the
@@ -484,7 +503,7 @@ def run_gpu(args):
             flush.fill_(k & 0xFF)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            v, r = one(rank * 1_000_003 + k, domain_dev)
+            v, r = one(rank_seed(rank, k), domain_dev)
             e1.record()
             torch.cuda.synchronize()
             step_ms.append(e0.elapsed_time(e1))
@@ -542,7 +561,7 @@ def run_gpu(args):
         for k in range(args.steps):
             flush.fill_(k & 0xFF)
             n0 = len(sampler_events)
-            v, _ = one(rank * 1_000_003 + k, domain_dev)
+            v, _ = one(rank_seed(rank, k), domain_dev)
             torch.cuda.synchronize()
             stats = v._dev.stats[: v.it, 2].cpu()
             sampler_points += [float(stats[j]) for j in range(len(sampler_events) - n0)]
@@ -599,18 +618,8 @@ def run_gpu(args):
     fp32_peak = max(peaks)
 
     # ---- reduce over ranks
-    t_max = t_local
-    e2e_t = sum(e2e_ms) / 1000.0
-    tot_evals, tot_e2e = evals, e2e_evals
-    if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([t_local, e2e_t], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        n = torch.tensor([float(evals), float(e2e_evals)], dtype=torch.float64, device=dev)
-        dist.all_reduce(n, op=dist.ReduceOp.SUM)
-        t_max, e2e_t = float(t[0]), float(t[1])
-        tot_evals, tot_e2e = int(n[0]), int(n[1])
+    t_max, e2e_t, tot_evals, tot_e2e = reduce_over_ranks(t_local, sum(e2e_ms) / 1000.0, evals, e2e_evals,
+                                                         ws, dev)
     if rank != 0:
         if ws > 1:
             import torch.distributed as dist
@@ -618,7 +627,9 @@ def run_gpu(args):
             dist.destroy_process_group()
         return 0
 
-    # algorithmic FP32 work of one sampled point (d = 6); see the design doc
+    # algorithmic FP32 work of one sampled point: d x (stratified y: add,
+    # div; map: mul, floor, sub, mul, add; Jacobian mul; domain map mul, add;
+    # separable term 4) + outer exp + 3 muls = 16 d + 7
     flops_per_point = 16 * DIM + 7
     pts = sum(sampler_points) / max(1, len(sampler_points))
     avg_ms = sum(sampler_ms) / max(1, len(sampler_ms))
