@@ -304,17 +304,22 @@ def _check_large_map(OV, dtype, cuda, weights, counts, tol32=2e-5):
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
-@pytest.mark.parametrize("case", ["zeros", "peaked", "zero_row"])
+@pytest.mark.parametrize("case", ["zeros", "raw_zeros", "peaked", "zero_row"])
 def test_large_map_cases_match_oracle(case, dtype, cuda):
     """Tiled map update: empty intervals filled across tile boundaries and
-    beyond ten neighbours, concentrated weights (long runs of equal delta
+    beyond ten neighbours (closed form), empty intervals that carry weights
+    (the sweeps themselves), concentrated weights (long runs of equal delta
     multiples, multiples that skip), and a row without weight (map reset)."""
     from oracle import vegas as OV
 
-    rng = np.random.default_rng({"zeros": 5, "peaked": 6, "zero_row": 7}[case])
+    rng = np.random.default_rng({"zeros": 5, "raw_zeros": 8, "peaked": 6, "zero_row": 7}[case])
     d, B = (5, 40000) if case != "zero_row" else (3, 3000)
     counts = rng.integers(1, 20, size=(d, B)).astype(np.int64)
     weights = rng.uniform(0.1, 3.0, size=(d, B)) * counts
+    if case == "raw_zeros":  # empty intervals with weights set directly: the fill sweeps shift them
+        z = rng.random((d, B)) < 0.3
+        z[:, 3000:3030] = True
+        counts[z] = 0
     if case == "zeros":
         z = rng.random((d, B)) < 0.3
         z[:, 2040:2065] = True  # a run of 25 across the first tile boundary

@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(kMapThreads) map_fill_kernel(tq_vegas_state st
   const int k = blockIdx.y;
   const int64_t B = st.n_bins, nt = gridDim.x;
   const int64_t t0 = (int64_t)blockIdx.x * kMapTile, e0 = t0 - kFillHalo;
-  int anyz = 0;
+  int anyz = 0, rawz = 0;
   for (int i = threadIdx.x; i < E; i += blockDim.x) {
     const int64_t b = e0 + i;
     T wv = (T)0;
@@ -465,8 +465,17 @@ __global__ void __launch_bounds__(kMapThreads) map_fill_kernel(tq_vegas_state st
     w_s[i] = wv;
     z_s[i] = zv;
     anyz |= zv;
+    rawz |= zv && wv != (T)0;
   }
-  if (__syncthreads_or(anyz)) {
+  // Empty intervals whose weights are zero (the only kind accumulation
+  // produces): the 10 sweeps have a closed form.  Each sweep moves a fill
+  // front one interval in from the nearest non-empty neighbour on each side,
+  // the right one first, so an empty interval takes the value of the nearer
+  // of its nearest non-empty neighbours within 10 intervals (the right one
+  // on a tie) and stays empty beyond that.
+  bool closed_form = false;
+  if (__syncthreads_or(anyz)) closed_form = !__syncthreads_or(rawz);
+  if (!closed_form && __syncthreads_or(anyz)) {
     for (int sweep = 0; sweep < 10; ++sweep) {
       for (int i = threadIdx.x; i < E; i += blockDim.x) {
         const bool right = e0 + i < B - 1 && i + 1 < E;
@@ -487,7 +496,22 @@ __global__ void __launch_bounds__(kMapThreads) map_fill_kernel(tq_vegas_state st
   for (int i = threadIdx.x; i < kMapTile; i += blockDim.x) {
     const int64_t b = t0 + i;
     if (b < B) {
-      const T v = w_s[kFillHalo + i];
+      const int j = kFillHalo + i;
+      T v = w_s[j];
+      if (closed_form && z_s[j]) {
+        int dr = 11, dl = 11;
+        for (int q = 1; q <= 10 && b + q < B; ++q)
+          if (!z_s[j + q]) {
+            dr = q;
+            break;
+          }
+        for (int q = 1; q <= 10 && b - q >= 0; ++q)
+          if (!z_s[j - q]) {
+            dl = q;
+            break;
+          }
+        if (dr <= 10 || dl <= 10) v = dr <= dl ? w_s[j + dr] : w_s[j - dl];
+      }
       wf[b] = v;
       acc += (double)v;
     }
