@@ -648,8 +648,12 @@ __global__ void __launch_bounds__(kMapThreads) map_multiples_kernel(tq_vegas_sta
 // ind[e] = #{b : mk[b] <= e}, which is b for e in [mk[b-1], mk[b]), and
 // vv[q] = the sequential sum (in T, as the reference's scatter-add) of sw
 // over the run of multiple q.
+constexpr int kRunHalo = 64;  // intervals past the tile staged for runs that cross its end
+
 template <typename T>
 __global__ void __launch_bounds__(kMapThreads) map_runs_kernel(tq_vegas_state st, MapTiles m) {
+  __shared__ int32_t mk_s[kMapTile + kRunHalo + 1];  // [0] = mk[t0 - 1]
+  __shared__ T sw_s[kMapTile + kRunHalo];
   if (*m.zero) return;
   const int k = blockIdx.y;
   const int64_t B = st.n_bins;
@@ -658,16 +662,28 @@ __global__ void __launch_bounds__(kMapThreads) map_runs_kernel(tq_vegas_state st
   const T* sw = (const T*)m.sw + k * B;
   T* vv = (T*)m.vv + k * (B + 1);
   int32_t* ind = m.ind + k * (B + 1);
+  // the multiples of intervals t0-1 .. t0+tile+halo-1 (those below B-1) and
+  // their smoothed weights, so that runs are summed from shared memory
+  const int64_t n_s = min((int64_t)(kMapTile + kRunHalo), B - 1 - t0);
+  for (int i = threadIdx.x; i <= kMapTile + kRunHalo; i += blockDim.x) {
+    const int64_t b = t0 - 1 + i;
+    if (i == 0 || i - 1 < n_s) mk_s[i] = b >= 0 ? mk[b] : 0;
+    if (i < n_s) sw_s[i] = sw[t0 + i];
+  }
+  __syncthreads();
   for (int i = threadIdx.x; i < kMapTile; i += blockDim.x) {
     const int64_t b = t0 + i;
     if (b >= B) break;
-    const int64_t from = b == 0 ? 0 : mk[b - 1];
-    const int64_t to = b == B - 1 ? B + 1 : mk[b];
+    const int64_t from = b == 0 ? 0 : mk_s[i];
+    const int64_t to = b == B - 1 ? B + 1 : mk_s[i + 1];
     for (int64_t e = from; e < to; ++e) ind[e] = (int32_t)b;
-    if (b < B - 1 && (b == 0 || mk[b] != mk[b - 1])) {
-      const int32_t q = mk[b];
+    if (b < B - 1 && (b == 0 || mk_s[i + 1] != mk_s[i])) {
+      const int32_t q = mk_s[i + 1];
       T a = (T)0;
-      for (int64_t e = b; e < B - 1 && mk[e] == q; ++e) a = add_rn(a, sw[e]);
+      int64_t e = b;
+      for (; e - t0 < n_s && mk_s[e - t0 + 1] == q; ++e) a = add_rn(a, sw_s[e - t0]);
+      if (e - t0 >= n_s)  // a run longer than the staged halo
+        for (; e < B - 1 && mk[e] == q; ++e) a = add_rn(a, sw[e]);
       vv[q] = a;
     }
   }
