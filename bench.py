@@ -24,6 +24,7 @@ per host core in parallel processes.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -581,7 +582,9 @@ def run_gpu(args):
 
     # ---- end to end through the public API with host inputs
     e2e_ms, e2e_evals = [], 0
-    h2d = 2 * DIM * 4 + (2 + 2 * DIM) * 8 + 8  # domain, integrand parameters, RNG offset
+    # domain bounds, integrand parameters, RNG offset and loop settings travel
+    # as the launch arguments of one tq_vegas_begin_run (a tq_vegas_run)
+    h2d = ctypes.sizeof(L.VegasRun)
     d2h_per = []
     barrier()
     for k in range(args.steps):
@@ -595,9 +598,9 @@ def run_gpu(args):
         val = r.item()
         e2e_ms.append((time.perf_counter() - t0) * 1000.0)
         e2e_evals += v._nr_of_fevals
-        # per abort test: stats of all iterations so far + flags; then offset and result
-        checks = v.it // 5
-        d2h_per.append(sum(32 * 5 * (i + 1) + 16 for i in range(checks)) + 8 + 4)
+        # one read-back per run (control, flags, RNG offset, statistics rows),
+        # then the result
+        d2h_per.append(v._dev._rb.numel() * 8 + 4)
         assert math.isfinite(val)
     barrier()
 

@@ -271,13 +271,20 @@ typedef struct tq_vegas_state {
                          * [3] a finish found its slot >= n_stat_slots       */
   double* scalars;      /* [4]: [0] sum of the unnormalised dh              */
   const void* domain;   /* [d][2] dtype                                        */
-  int64_t* control;     /* [8] per-iteration inputs read by the kernels, so a
-                         * sequence of launches can be captured once and
+  int64_t* control;     /* [16] per-iteration inputs read by the kernels, so
+                         * a sequence of launches can be captured once and
                          * replayed: [0] nevals_exp (VEGAS._starting_N),
                          * [1] statistics slot of the next finish (advanced by
                          * tq_vegas_finish_iteration), [2] 1 if dh awaits
                          * normalisation (set by finish, cleared by get_nh),
-                         * [3] Philox seed, [4] Philox stream id           */
+                         * [3] Philox seed, [4] Philox stream id; the loop
+                         * state of tq_vegas_begin_run/tq_vegas_abort_test:
+                         * [5] N, [6] N_increment, [7] max_iterations,
+                         * [8] eps_rel, [9] eps_abs (IEEE double bits),
+                         * [10] warm-up evaluations, [11] iterations done,
+                         * [12] stop reason (0 go on, 1 accuracy reached,
+                         * 2 evaluation budget, 3 iteration limit, 4 out of
+                         * statistics slots), [13] evaluations so far        */
 } tq_vegas_state;
 
 enum {
@@ -299,6 +306,57 @@ int tq_vegas_init(const tq_vegas_state* st, void* stream);
  * (a one-thread kernel, so it orders with the other launches). */
 int tq_vegas_set_control(const tq_vegas_state* st, int mask, int64_t nevals_exp, int64_t slot,
                          int64_t normalize, uint64_t seed, uint64_t stream_id, void* stream);
+
+/* ---- the iteration loop on the device (tq_vegas_loop.cu) -------------------
+ * VEGAS.integrate's loop (vegas.py:141-160): blocks of five iterations, then
+ * _check_abort_conditions (:161-209), until it says stop.  With these two
+ * calls and the capture helpers below a whole integration is one CUDA graph:
+ * warm-up, then a WHILE node whose body is a block plus tq_vegas_abort_test. */
+typedef struct {
+  int64_t nevals_exp;     /* VEGAS._starting_N of the first block            */
+  int64_t N;              /* evaluation budget                                */
+  int64_t N_increment;    /* VEGAS._N_increment                               */
+  int64_t max_iterations;
+  int64_t warm_evals;     /* evaluations spent by the warm-up                 */
+  double eps_rel, eps_abs;
+  uint64_t seed, stream_id; /* Philox key and stream of the run              */
+  uint64_t rng_offset;    /* Philox block offset the run starts at           */
+  int32_t n_params;       /* entries of params copied to params_dev           */
+  int32_t n_domain;       /* 0, or 2*dim: domain values for st->domain        */
+  double params[2 + 2 * TQ_MAX_DIM]; /* built-in integrand parameters      */
+  double domain[2 * TQ_MAX_DIM];     /* [dim][2] bounds, rounded to the
+                                      * state's dtype when written         */
+} tq_vegas_run;
+
+/* The per-call inputs of a run in one one-thread launch: control [0], [3..10]
+ * from `run`, [11..12] = 0, [13] = warm_evals; *st->rng_offset;
+ * run->params[0..n_params) into params_dev (the parameter vector the fused
+ * kernels read); and, if n_domain = 2*dim, the domain into st->domain (so a
+ * domain given as host values needs no copy of its own). */
+int tq_vegas_begin_run(const tq_vegas_state* st, const tq_vegas_run* run, double* params_dev,
+                       void* stream);
+
+/* _check_abort_conditions with _get_result, _get_error and _get_chisq
+ * (vegas.py:161-209, 318-362) after a block of five iterations, on the
+ * device in fp64: reads the block's five statistics rows (result, variance)
+ * ending at control[1], sets control[13] = warm-up + points of all
+ * iterations, control[11] += 5, control[12] = stop reason, and adapts
+ * control[0] (nevals_exp) as the reference adapts _starting_N.  Every sum is
+ * taken left to right from zero and x / 0 follows IEEE, as in the
+ * reference's tensor arithmetic.  cond_handle != 0: the
+ * cudaGraphConditionalHandle of the WHILE node this runs in, set to 0 to
+ * stop. */
+int tq_vegas_abort_test(const tq_vegas_state* st, uint64_t cond_handle, void* stream);
+
+/* Capture helpers for a device-side loop (CUDA graph conditional nodes).
+ * During a stream capture on `stream`, tq_capture_while_begin appends a
+ * WHILE node (condition 1 at every graph launch) after the captured work,
+ * makes it the stream's capture dependency and starts capturing the node's
+ * body on body_stream (another, idle stream of the device); *cond_handle
+ * receives the node's handle.  tq_capture_while_end ends the body capture;
+ * the capture on `stream` goes on after the node. */
+int tq_capture_while_begin(void* stream, void* body_stream, uint64_t* cond_handle);
+int tq_capture_while_end(void* body_stream);
 
 /* One warm-up iteration, fused (vegas.py:228-256 without the map update):
  * y = u * 0.999999 with u from the Philox stream (control seed and stream

@@ -372,3 +372,97 @@ def test_default_interval_count_vegas(cuda):
     r = v.integrate(f, 3, N=2_000_000, integration_domain=dom, seed=3)
     assert v.map.N_intervals == 2_000_000 // 25 // 10
     assert abs(r.item() - 1.0) < 5 * v._get_error() + 1e-3
+
+
+def _abort_cases():
+    rng = np.random.default_rng(5)
+    cases = []
+    for k in range(60):
+        r = list(1.0 + 0.01 * rng.standard_normal(5))
+        s = list(np.abs(1e-4 * rng.standard_normal(5)) + 1e-8)
+        cases.append(dict(r=r, s=s, eps_rel=float(rng.choice([0.0, 1e-6, 1e-2, 1.0])),
+                          eps_abs=float(rng.choice([0.0, 1e-3])), it=int(rng.choice([5, 10, 15, 20])),
+                          sN=int(rng.integers(1000, 100000)), inc=int(rng.integers(1000, 50000)),
+                          N=int(rng.choice([10**6, 10**7])), max_it=int(rng.choice([10, 20, 40]))))
+    base = dict(eps_rel=0.0, eps_abs=0.0, it=5, sN=4000, inc=4000, N=10**6, max_it=20)
+    cases += [
+        dict(base, r=[1.0] * 5, s=[0.0] * 5),                          # constant integrand
+        dict(base, r=[0.0] * 5, s=[0.0] * 5),                          # zero integrand
+        dict(base, r=[1.0, 2.0, 1.0, 1.0, 1.0], s=[0.0, 1.0, 1.0, 1.0, 1.0]),  # x / 0 in chi2
+        dict(base, r=[1.0, 1.1, 0.9, 1.0, 1.05], s=[1e-2] * 5, eps_rel=1.0),    # accuracy
+        dict(base, r=[1.0, 5.0, -3.0, 1.0, 2.0], s=[1e-6] * 5),        # chi2 / 5 > 1
+        dict(base, r=[1.0] * 5, s=[1e-4] * 5, N=30000),                # budget
+        dict(base, r=[1.0] * 5, s=[1e-4] * 5, it=20, max_it=20),       # iteration limit
+    ]
+    return cases
+
+
+def test_device_abort_test_matches_host_logic(cuda):
+    """tq_vegas_abort_test (the every-fifth-iteration test on the device)
+    takes the host _check_abort_conditions' decision and adapted
+    _starting_N, including zero variances and x / 0."""
+    d = VegasDevice(2, torch.float64, 4, 2, cuda, stats_slots=64)
+    zeros = np.zeros(6)
+    for case in _abort_cases():
+        it, warm = case["it"], 777
+        pts = np.arange(1, it + 1) * 1000
+        d.begin_run(case["sN"], case["N"], case["inc"], case["max_it"], warm, case["eps_rel"],
+                    case["eps_abs"], 0, 0, 0, zeros)
+        st = torch.zeros((it, 4), dtype=torch.float64)
+        st[:, 2] = torch.tensor(pts, dtype=torch.float64)
+        st[it - 5:, 0] = torch.tensor(case["r"], dtype=torch.float64)
+        st[it - 5:, 1] = torch.tensor(case["s"], dtype=torch.float64)
+        d.stats[:it] = st.to(cuda)
+        d.control[1] = it
+        d.control[11] = it - 5
+        d.abort_test(0)
+        d.read_back()
+        v = tq.VEGAS()
+        v.it, v.results, v.sigma2 = it, list(case["r"]), list(case["s"])
+        v._eps_rel, v._eps_abs = case["eps_rel"], case["eps_abs"]
+        v._starting_N, v._N_increment, v.N = case["sN"], case["inc"], case["N"]
+        v._max_iterations = case["max_it"]
+        v._nr_of_fevals = warm + int(pts.sum())
+        stop = v._check_abort_conditions()
+        c = d.host_control
+        assert int(c[L.VC_EVALS]) == v._nr_of_fevals
+        assert int(c[L.VC_IT]) == it
+        assert bool(c[L.VC_STOP]) == stop, case
+        assert int(c[L.VC_NEVALS]) == v._starting_N, case
+
+
+def test_fused_graph_and_eager_runs_agree(cuda):
+    """The captured run (warm-up + WHILE node with the device abort test)
+    and the same launches run eagerly give the same integration."""
+    from torchquad_gb300.integration import vegas as V
+    f = tq.GaussianPeak.normal(4, 0.5, 0.1)
+    dom = torch.tensor([[0.0, 1.0]] * 4, dtype=torch.float32, device=cuda)
+    out = []
+    for eager in (False, True):
+        V.FORCE_EAGER[0] = eager
+        try:
+            for seed in (1, 2, 3):  # the second call of a shape captures the graph
+                v = tq.VEGAS()
+                r = v.integrate(f, 4, N=400_000, integration_domain=dom, seed=seed)
+            out.append((r.item(), v.it, v._nr_of_fevals, v._starting_N, v.rng.offset,
+                        list(v.results), list(v.sigma2)))
+        finally:
+            V.FORCE_EAGER[0] = False
+    assert out[0] == out[1]
+
+
+def test_fused_host_domain_and_dh_normalised(cuda):
+    """A domain given as host values (launch arguments) integrates exactly
+    like the same domain as a tensor; dh comes out normalised (once)."""
+    f = tq.GaussianPeak.normal(3, 0.4, 0.1)
+    dom_list = [[0.0, 1.0], [-0.5, 1.0], [0.1, 0.9]]
+    a, b = tq.VEGAS(), tq.VEGAS()
+    ra = a.integrate(f, 3, N=200_000, integration_domain=dom_list, seed=4)
+    dh_a = a.strat.dh.clone()
+    rb = b.integrate(f, 3, N=200_000, seed=4,
+                     integration_domain=torch.tensor(dom_list, dtype=torch.get_default_dtype(), device=cuda))
+    assert ra.dtype == rb.dtype == torch.get_default_dtype()
+    assert ra.item() == rb.item() and a.it == b.it and a._nr_of_fevals == b._nr_of_fevals
+    assert abs(float(dh_a.double().sum()) - 1.0) < 1e-5
+    assert torch.equal(b.strat.dh, dh_a)
+    assert torch.equal(b.strat.dh, dh_a)  # a second access does not divide again

@@ -65,6 +65,31 @@ class VegasState(ctypes.Structure):
 TQ_VC_NEVALS, TQ_VC_SLOT, TQ_VC_NORMALIZE, TQ_VC_SEED, TQ_VC_STREAM = 1, 2, 4, 8, 16
 
 
+class VegasRun(ctypes.Structure):
+    """Mirror of ``tq_vegas_run`` (include/torchquad_gb300.h)."""
+
+    _fields_ = [
+        ("nevals_exp", c_int64),
+        ("N", c_int64),
+        ("N_increment", c_int64),
+        ("max_iterations", c_int64),
+        ("warm_evals", c_int64),
+        ("eps_rel", c_double),
+        ("eps_abs", c_double),
+        ("seed", c_uint64),
+        ("stream_id", c_uint64),
+        ("rng_offset", c_uint64),
+        ("n_params", ctypes.c_int32),
+        ("n_domain", ctypes.c_int32),
+        ("params", c_double * (2 + 2 * TQ_MAX_DIM)),
+        ("domain", c_double * (2 * TQ_MAX_DIM)),
+    ]
+
+
+# control block fields of the device-side VEGAS loop (tq_vegas_state.control)
+VC_NEVALS, VC_SLOT, VC_IT, VC_STOP, VC_EVALS = 0, 1, 11, 12, 13
+
+
 _VS = POINTER(VegasState)
 
 # name -> (restype, argtypes); every symbol the header declares.
@@ -122,6 +147,10 @@ SIGNATURES = {
     "tq_vegas_workspace_size": (c_size_t, [_VS]),
     "tq_vegas_init": (c_int, [_VS, c_void_p]),
     "tq_vegas_set_control": (c_int, [_VS, c_int, c_int64, c_int64, c_int64, c_uint64, c_uint64, c_void_p]),
+    "tq_vegas_begin_run": (c_int, [_VS, POINTER(VegasRun), c_void_p, c_void_p]),
+    "tq_vegas_abort_test": (c_int, [_VS, c_uint64, c_void_p]),
+    "tq_capture_while_begin": (c_int, [c_void_p, c_void_p, POINTER(c_uint64)]),
+    "tq_capture_while_end": (c_int, [c_void_p]),
     "tq_vegas_warmup_fused": (c_int, [_VS, c_int, c_void_p, c_int64, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_update_map": (c_int, [_VS, c_double, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_smooth_weights": (c_int, [_VS, c_double, c_void_p, c_void_p, c_size_t, c_void_p]),

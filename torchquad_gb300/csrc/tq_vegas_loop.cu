@@ -1,0 +1,234 @@
+// The VEGAS iteration loop on the device: the per-call inputs of a run and
+// the abort test after every fifth iteration, so that a whole integration
+// (warm-up, then blocks of five iterations while the test says go on) is
+// one CUDA graph with a WHILE conditional node and no host round trip.
+//
+// Reference (torchquad v0.5.0): vegas.py:100-209 (VEGAS.integrate and
+// _check_abort_conditions), :318-362 (_get_result, _get_error, _get_chisq).
+
+#include <math.h>
+#include <string.h>
+
+#include "tq_common.cuh"
+
+namespace tq {
+
+enum : int {
+  kCtlNevals = 0,
+  kCtlSlot = 1,
+  kCtlNormalize = 2,
+  kCtlSeed = 3,
+  kCtlStream = 4,
+  kCtlN = 5,
+  kCtlNInc = 6,
+  kCtlMaxIt = 7,
+  kCtlEpsRel = 8,
+  kCtlEpsAbs = 9,
+  kCtlWarm = 10,
+  kCtlIt = 11,
+  kCtlStop = 12,
+  kCtlEvals = 13,
+};
+
+struct RunArgs {
+  tq_vegas_run run;
+  int64_t* control;
+  uint64_t* rng_offset;
+  double* params_dev;
+  void* domain;  // the state's [dim][2] domain buffer
+  int dtype;
+};
+
+__global__ void vegas_begin_run_kernel(RunArgs a) {
+  int64_t* c = a.control;
+  const tq_vegas_run& r = a.run;
+  c[kCtlNevals] = r.nevals_exp;
+  c[kCtlSeed] = (int64_t)r.seed;
+  c[kCtlStream] = (int64_t)r.stream_id;
+  c[kCtlN] = r.N;
+  c[kCtlNInc] = r.N_increment;
+  c[kCtlMaxIt] = r.max_iterations;
+  c[kCtlEpsRel] = __double_as_longlong(r.eps_rel);
+  c[kCtlEpsAbs] = __double_as_longlong(r.eps_abs);
+  c[kCtlWarm] = r.warm_evals;
+  c[kCtlIt] = 0;
+  c[kCtlStop] = 0;
+  c[kCtlEvals] = r.warm_evals;
+  *a.rng_offset = r.rng_offset;
+  for (int i = 0; i < r.n_params; ++i) a.params_dev[i] = r.params[i];
+  for (int i = 0; i < r.n_domain; ++i) {
+    if (a.dtype == TQ_F64)
+      ((double*)a.domain)[i] = r.domain[i];
+    else
+      ((float*)a.domain)[i] = __double2float_rn(r.domain[i]);
+  }
+}
+
+// IEEE quotient (x / 0 is +-inf or NaN, as the reference's tensor arithmetic
+// gives); written out so the compiler's fast paths cannot change it.
+__device__ __forceinline__ double qdiv(double x, double y) { return __ddiv_rn(x, y); }
+
+// The decision of _check_abort_conditions for the five results r[] and
+// variances s[] of the block that just ended, in the host code's operation
+// order (every sum left to right from zero).  Returns the stop reason
+// (0: go on) and updates *sN (VEGAS._starting_N).
+__device__ int abort_decision(const double* r, const double* s, int64_t it, int64_t evals,
+                              int64_t N, int64_t n_inc, int64_t max_it, double eps_rel,
+                              double eps_abs, int64_t* sN) {
+  // _get_result (EQ 30)
+  bool zero_var = false;
+  for (int i = 0; i < 5; ++i) zero_var = zero_var || s[i] == 0.0;
+  double res;
+  if (zero_var) {
+    double t = 0.0;
+    for (int i = 0; i < 5; ++i) t = __dadd_rn(t, r[i]);
+    res = qdiv(t, 5.0);
+  } else {
+    double num = 0.0, den = 0.0;
+    for (int i = 0; i < 5; ++i) num = __dadd_rn(num, qdiv(r[i], s[i]));
+    for (int i = 0; i < 5; ++i) den = __dadd_rn(den, qdiv(1.0, s[i]));
+    res = qdiv(num, den);
+  }
+  const double res_abs = fabs(res);
+  // _get_error (EQ 31)
+  double inv = 0.0;
+  for (int i = 0; i < 5; ++i)
+    if (s[i] != 0.0) inv = __dadd_rn(inv, qdiv(1.0, s[i]));
+  const double err = inv == 0.0 ? s[0] : qdiv(1.0, __dsqrt_rn(inv));
+  // _get_chisq (EQ 32)
+  double chi2 = 0.0;
+  for (int i = 0; i < 5; ++i) {
+    if (r[i] != res) {
+      const double d = __dsub_rn(r[i], res);
+      chi2 = __dadd_rn(chi2, qdiv(__dmul_rn(d, d), s[i]));
+    }
+  }
+  const double q = qdiv(chi2, 5.0);
+  if ((err <= __dmul_rn(eps_rel, res_abs) || err <= eps_abs) && q < 1.0) return 1;
+  if (q < 1.0) {
+    if (res_abs == 0.0) {
+      *sN += n_inc;
+    } else {
+      const double acc = qdiv(err, res_abs);
+      const double x = __dmul_rn((double)*sN, __dsqrt_rn(qdiv(acc, __dadd_rn(eps_rel, 1e-8))));
+      // int(): truncation toward zero (saturating on the device where the
+      // host would raise for an infinite value)
+      const int64_t t = __double2ll_rz(x);
+      *sN = min(*sN + n_inc, t);
+    }
+  } else if (q > 1.0) {
+    *sN += n_inc;
+  }
+  if (evals + *sN * 5 > N) return 2;
+  if (it + 5 > max_it) return 3;
+  return 0;
+}
+
+struct AbortArgs {
+  int64_t* control;
+  const double* stats;
+  int64_t n_stat_slots;
+  cudaGraphConditionalHandle handle;
+  int use_handle;
+};
+
+__global__ void vegas_abort_kernel(AbortArgs a) {
+  int64_t* c = a.control;
+  const int64_t it = c[kCtlIt] + 5;
+  const int64_t slot = c[kCtlSlot];  // rows [slot - 5, slot) hold this block
+  int stop;
+  if (slot < 5 || slot > a.n_stat_slots) {
+    stop = 4;  // the statistics slots ran out: nothing valid to test
+  } else {
+    // _nr_of_fevals: the warm-up plus the points of every iteration so far
+    int64_t evals = c[kCtlWarm];
+    for (int64_t i = 0; i < slot; ++i) evals += (int64_t)a.stats[4 * i + 2];
+    c[kCtlEvals] = evals;
+    double r[5], s[5];
+    for (int i = 0; i < 5; ++i) {
+      r[i] = a.stats[4 * (slot - 5 + i)];
+      s[i] = a.stats[4 * (slot - 5 + i) + 1];
+    }
+    int64_t sN = c[kCtlNevals];
+    stop = abort_decision(r, s, it, evals, c[kCtlN], c[kCtlNInc], c[kCtlMaxIt],
+                          __longlong_as_double(c[kCtlEpsRel]), __longlong_as_double(c[kCtlEpsAbs]),
+                          &sN);
+    c[kCtlNevals] = sN;
+  }
+  c[kCtlIt] = it;
+  c[kCtlStop] = stop;
+  if (a.use_handle) cudaGraphSetConditional(a.handle, stop == 0 ? 1u : 0u);
+}
+
+}  // namespace tq
+
+using namespace tq;
+
+extern "C" int tq_vegas_begin_run(const tq_vegas_state* st, const tq_vegas_run* run,
+                                  double* params_dev, void* stream) {
+  if (!st || !run || !st->control || !st->rng_offset) return TQ_ERR_ARG;
+  if (run->n_params < 0 || run->n_params > 2 + 2 * TQ_MAX_DIM || (run->n_params > 0 && !params_dev))
+    return TQ_ERR_ARG;
+  if (run->max_iterations < 0 || run->N < 0 || run->N_increment < 0 || run->nevals_exp < 0)
+    return TQ_ERR_ARG;
+  if (run->n_domain != 0 && (run->n_domain != 2 * st->dim || !st->domain || !valid_dtype(st->dtype)))
+    return TQ_ERR_ARG;
+  RunArgs a;
+  memcpy(&a.run, run, sizeof(tq_vegas_run));
+  a.control = st->control;
+  a.rng_offset = st->rng_offset;
+  a.params_dev = params_dev;
+  a.domain = const_cast<void*>(st->domain);
+  a.dtype = st->dtype;
+  vegas_begin_run_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(a);
+  return launch_status();
+}
+
+extern "C" int tq_vegas_abort_test(const tq_vegas_state* st, uint64_t cond_handle, void* stream) {
+  if (!st || !st->control || !st->stats || st->n_stat_slots < 1) return TQ_ERR_ARG;
+  AbortArgs a;
+  a.control = st->control;
+  a.stats = st->stats;
+  a.n_stat_slots = st->n_stat_slots;
+  a.handle = (cudaGraphConditionalHandle)cond_handle;
+  a.use_handle = cond_handle != 0;
+  vegas_abort_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(a);
+  return launch_status();
+}
+
+extern "C" int tq_capture_while_begin(void* stream, void* body_stream, uint64_t* cond_handle) {
+  if (!cond_handle || stream == body_stream) return TQ_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaStreamCaptureStatus status;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edges = nullptr;
+  size_t n_deps = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(s, &status, nullptr, &graph, &deps, &edges, &n_deps);
+  if (e != cudaSuccess) return set_cuda_error(e);
+  if (status != cudaStreamCaptureStatusActive || !graph) return TQ_ERR_ARG;
+  cudaGraphConditionalHandle h;
+  e = cudaGraphConditionalHandleCreate(&h, graph, 1u, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return set_cuda_error(e);
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, graph, deps, edges, n_deps, &p);
+  if (e != cudaSuccess) return set_cuda_error(e);
+  e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  if (e != cudaSuccess) return set_cuda_error(e);
+  e = cudaStreamBeginCaptureToGraph((cudaStream_t)body_stream, p.conditional.phGraph_out[0], nullptr,
+                                    nullptr, 0, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return set_cuda_error(e);
+  *cond_handle = (uint64_t)h;
+  return TQ_OK;
+}
+
+extern "C" int tq_capture_while_end(void* body_stream) {
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture((cudaStream_t)body_stream, &g);
+  return e == cudaSuccess ? TQ_OK : set_cuda_error(e);
+}

@@ -7,6 +7,7 @@ also owns its scratch workspace (its size depends on the state's shape).
 from __future__ import annotations
 
 import ctypes
+import weakref
 
 import torch
 
@@ -37,15 +38,16 @@ class VegasDevice:
         self.jf2 = torch.zeros((self.n_cubes,), dtype=torch.float64, device=device)
         self.neval = torch.zeros((self.n_cubes,), dtype=torch.int64, device=device)
         self.cube_start = torch.zeros((self.n_cubes + 1,), dtype=torch.int64, device=device)
-        self.rng_offset = torch.zeros((1,), dtype=torch.int64, device=device)
-        self.stats = torch.zeros((max(1, stats_slots), 4), dtype=torch.float64, device=device)
-        self.flags = torch.zeros((4,), dtype=torch.int32, device=device)
         self.scalars = torch.zeros((4,), dtype=torch.float64, device=device)
-        self.control = torch.zeros((8,), dtype=torch.int64, device=device)
+        self._alloc_readback(max(1, stats_slots))
         self.params = torch.zeros((2 + 2 * dim,), dtype=torch.float64, device=device)
         if domain is None:
             domain = torch.tensor([[0.0, 1.0]] * dim, **f)
-        self.domain = domain.detach().to(device=device, dtype=dtype).contiguous()
+        # the state's own copy (never an alias of the caller's tensor)
+        self.domain = domain.detach().to(device=device, dtype=dtype).clone().contiguous()
+        self._domain_src = None
+        self.dh_pending = False  # dh awaits update_DH's normalisation (see stratification.dh)
+        self._run = L.VegasRun()
         self.struct = L.VegasState()
         self._fill_struct()
         self.ref = ctypes.byref(self.struct)
@@ -68,19 +70,88 @@ class VegasDevice:
             setattr(s, name, getattr(self, name).data_ptr())
         s.n_stat_slots = self.stats.shape[0]
 
+    # Everything the host reads back after a run sits in one int64 buffer, so
+    # one copy brings it: control [16], flags [8] (int32), rng_offset [1],
+    # padding, stats [slots][4] (fp64).
+    _RB_CONTROL, _RB_FLAGS, _RB_OFFSET, _RB_STATS = 0, 16, 20, 24
+
+    def _alloc_readback(self, slots, old=None):
+        buf = torch.zeros((self._RB_STATS + 4 * slots,), dtype=torch.int64, device=self.device)
+        if old is not None:
+            buf[: old.numel()] = old
+        self._rb = buf
+        self.control = buf[self._RB_CONTROL:self._RB_FLAGS]
+        self.flags = buf[self._RB_FLAGS:self._RB_OFFSET].view(torch.int32)
+        self.rng_offset = buf[self._RB_OFFSET:self._RB_OFFSET + 1]
+        self.stats = buf[self._RB_STATS:].view(torch.float64).view(slots, 4)
+        self._rb_host = torch.empty(buf.shape, dtype=torch.int64, pin_memory=True)
+        h = self._rb_host.numpy()
+        self.host_control = h[self._RB_CONTROL:self._RB_FLAGS]
+        self.host_flags = h[self._RB_FLAGS:self._RB_OFFSET].view("int32")
+        self.host_rng_offset = h[self._RB_OFFSET:self._RB_OFFSET + 1]
+        self.host_stats = h[self._RB_STATS:].view("float64").reshape(slots, 4)
+
     def ensure_slots(self, n):
         if n > self.stats.shape[0]:
-            new = torch.zeros((max(n, 2 * self.stats.shape[0]), 4), dtype=torch.float64, device=self.device)
-            new[: self.stats.shape[0]] = self.stats
-            self.stats = new
-            self.struct.stats = self.stats.data_ptr()
+            self._alloc_readback(max(n, 2 * self.stats.shape[0]), old=self._rb)
+            for name in ("control", "flags", "rng_offset", "stats"):
+                setattr(self.struct, name, getattr(self, name).data_ptr())
             self.struct.n_stat_slots = self.stats.shape[0]
 
+    def read_back(self):
+        """Copy control, flags, RNG offset and stats to the host (one copy,
+        then a wait for the stream); the host_* numpy views then hold them."""
+        self._rb_host.copy_(self._rb, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
     def set_domain(self, domain):
-        """Copy a domain into the state's own buffer (its address stays)."""
+        """Copy a domain into the state's own buffer (its address stays);
+        skipped when it is the tensor copied last time, unchanged since."""
+        src = self._domain_src
+        if src is not None and src[0]() is domain and src[1] == domain._version:
+            return
         self.domain.copy_(domain.detach().to(device=self.device, dtype=self.dtype))
+        try:
+            self._domain_src = (weakref.ref(domain), domain._version)
+        except TypeError:
+            self._domain_src = None
+
+    def begin_run(self, nevals, N, n_inc, max_it, warm_evals, eps_rel, eps_abs, seed, sid, offset,
+                  params, domain_values=None):
+        """Per-call inputs of a device-side run (one launch): control
+        fields, the RNG offset, the integrand parameters (fp64 numpy) and,
+        if given, the domain as host values ([dim][2] floats)."""
+        r = self._run
+        r.nevals_exp, r.N, r.N_increment = int(nevals), int(N), int(n_inc)
+        r.max_iterations, r.warm_evals = int(max_it), int(warm_evals)
+        r.eps_rel, r.eps_abs = float(eps_rel), float(eps_abs)
+        mask = (1 << 64) - 1
+        r.seed, r.stream_id, r.rng_offset = int(seed) & mask, int(sid) & mask, int(offset) & mask
+        n = len(params)
+        r.n_params = n
+        ctypes.memmove(r.params, params.ctypes.data, 8 * n)
+        if domain_values is not None:
+            r.n_domain = 2 * self.dim
+            k = 0
+            for lo, hi in domain_values:
+                r.domain[k], r.domain[k + 1] = lo, hi
+                k += 2
+            self._domain_src = None
+        else:
+            r.n_domain = 0
+        L.check(L.lib().tq_vegas_begin_run(self.ref, ctypes.byref(r), self.params.data_ptr(),
+                                           L.stream_handle()), "tq_vegas_begin_run")
+        L.count_launches(1)
+
+    def abort_test(self, cond_handle=0):
+        """The every-fifth-iteration abort test on the device (control[11..13],
+        control[0]); inside a captured WHILE node, cond_handle stops it."""
+        L.check(L.lib().tq_vegas_abort_test(self.ref, int(cond_handle), L.stream_handle()),
+                "tq_vegas_abort_test")
+        L.count_launches(1)
 
     def reinit(self):
+        self.dh_pending = False
         L.check(L.lib().tq_vegas_init(self.ref, L.stream_handle()), "tq_vegas_init")
         L.count_launches(1)
 
@@ -133,6 +204,7 @@ class VegasDevice:
             L.TQ_VC_NORMALIZE if normalize is not None else 0)
         if mask:
             self.set_control(mask, nevals=nevals_exp or 0, normalize=int(bool(normalize)))
+        self.dh_pending = False  # the device normalises here if control[2] says so
         p, n = self._ws()
         L.check(L.lib().tq_vegas_get_nh(self.ref, p, n, L.stream_handle()), "tq_vegas_get_nh")
         L.count_launches(2)

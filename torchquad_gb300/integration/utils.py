@@ -118,6 +118,29 @@ def _setup_integration_domain(dim, integration_domain, backend):
     return t
 
 
+def _host_domain_values(dim, integration_domain, backend):
+    """For a domain given as host values (None, a list, a tuple or an array),
+    the [dim][2] bounds as floats, with the checks of
+    _setup_integration_domain; None for a tensor domain.  Lets a fused
+    kernel take the bounds as launch arguments instead of a device copy."""
+    if isinstance(integration_domain, torch.Tensor):
+        return None
+    _check_backend(backend)
+    if backend is None:
+        _check_backend(_get_default_backend())
+    if integration_domain is None:
+        return [(-1.0, 1.0)] * dim
+    if hasattr(integration_domain, "__array__") and not isinstance(integration_domain, (list, tuple)):
+        integration_domain = integration_domain.tolist()
+    values = [(float(b[0]), float(b[1])) if len(b) == 2 else tuple(b) for b in integration_domain]
+    if len(values) != dim or any(len(v) != 2 for v in values):
+        raise ValueError(
+            "The integration domain has an unexpected shape. "
+            f"Expected {(dim, 2)}, got ({len(values)}, ...)"
+        )
+    return values
+
+
 def _is_host_list(domain):
     return domain is None or not isinstance(domain, torch.Tensor)
 

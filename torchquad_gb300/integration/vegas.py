@@ -15,6 +15,7 @@ Two drivers with the reference's algorithm and defaults:
 """
 from __future__ import annotations
 
+import ctypes
 import math
 import warnings
 
@@ -24,7 +25,7 @@ from .. import _lib as L
 from ..integrands import BuiltinIntegrand
 from .base_integrator import BaseIntegrator
 from .rng import RNG
-from .utils import _setup_integration_domain
+from .utils import _host_domain_values, _setup_integration_domain
 from ._vegas_state import VegasDevice, n_strat_for
 from .vegas_map import VEGASMap
 from .vegas_stratification import VEGASStratification
@@ -34,13 +35,17 @@ BETA = 0.75  # vegas_stratification.py:13
 
 
 class _FusedPlan:
-    """Device state plus captured CUDA graphs for one fused VEGAS shape.
+    """Device state plus one captured CUDA graph for a fused VEGAS shape.
 
-    The warm-up (state reset + five warm-up sampling/map-update pairs) and a
-    block of five stratified iterations (get_NH, fused sampling, finish, map
-    update) read every changing input from the state's control block, so
-    they are captured once and replayed for every later block and call with
-    the same shape.  The first use runs the launches eagerly."""
+    A whole integration is one graph: the warm-up (state reset and five
+    warm-up sampling/map-update pairs), then a WHILE conditional node whose
+    body is a block of five stratified iterations (get_NH, fused sampling,
+    finish and map update) followed by the device-side abort test, which
+    ends the loop (vegas.py:141-209).  Every changing input sits in the
+    state's control block (written by begin_run), so the graph is captured
+    once and launched for every call with the same shape, and the host reads
+    the results back once per call.  The first use runs the same launches
+    eagerly, with the loop on the host."""
 
     _cache = {}
     _MAX = 8
@@ -49,8 +54,7 @@ class _FusedPlan:
         self.dev, self.family = dev, family
         self.use_grid_improve, self.use_warmup, self.ns = use_grid_improve, use_warmup, ns
         self.uses = 0
-        self.g_warm = None
-        self.g_block = None
+        self.graph = None
 
     @classmethod
     def get(cls, make_dev, shape_key, family, use_grid_improve, use_warmup, ns, max_iterations):
@@ -83,32 +87,68 @@ class _FusedPlan:
             else:
                 d.finish(BETA)
 
-    def _capture(self, seq):
+    def _warm_launches(self):
+        per = (1 if self.ns > 0 else 0) + self.dev.update_map_launches
+        return 1 + (5 * per if self.use_warmup else 0)
+
+    def _block_launches(self):  # five iterations and the abort test
+        return 5 * (3 + (self.dev.finish_update_map_launches if self.use_grid_improve else 1)) + 1
+
+    def _capture(self):
+        """Records warm-up + WHILE(block, abort test) without running it."""
         g = torch.cuda.CUDAGraph()
+        body = torch.cuda.Stream(device=self.dev.device)
+        h = ctypes.c_uint64(0)
         with torch.cuda.graph(g):
-            seq()
+            self._warm_seq()
+            L.check(L.lib().tq_capture_while_begin(L.stream_handle(), body.cuda_stream, ctypes.byref(h)),
+                    "tq_capture_while_begin")
+            try:
+                with torch.cuda.stream(body):
+                    self._block_seq()
+                    self.dev.abort_test(h.value)
+            finally:
+                L.check(L.lib().tq_capture_while_end(body.cuda_stream), "tq_capture_while_end")
         return g
 
-    def run_warmup(self):
+    def run(self):
+        """Warm-up, then blocks until the abort test stops; the results are
+        left in the state's host copy (dev.host_*)."""
         self.uses += 1
-        if self.g_warm is None and self.uses > 1 and _graphs_enabled():
+        d = self.dev
+        if self.graph is None and self.uses > 1 and _graphs_enabled():
             torch.cuda.synchronize()
-            # capture records the launches without running them
-            self.g_warm = self._capture(self._warm_seq)
-            self.g_block = self._capture(self._block_seq)
-        if self.g_warm is not None and not FORCE_EAGER[0]:
-            self.g_warm.replay()
-            L.count_launches(1 + (5 * ((1 if self.ns > 0 else 0) + self.dev.update_map_launches)
-                                  if self.use_warmup else 0))
-        else:
-            self._warm_seq()
-
-    def run_block(self):
-        if self.g_block is not None and not FORCE_EAGER[0]:
-            self.g_block.replay()
-            L.count_launches(5 * (3 + (self.dev.finish_update_map_launches if self.use_grid_improve else 1)))
-        else:
+            self.graph = self._capture()
+        if self.graph is not None and not FORCE_EAGER[0]:
+            self.graph.replay()
+            d.read_back()
+            L.count_launches(self._warm_launches()
+                             + int(d.host_control[L.VC_IT]) // 5 * self._block_launches())
+            return
+        self._warm_seq()
+        while True:
             self._block_seq()
+            d.abort_test(0)
+            d.read_back()
+            if d.host_control[L.VC_STOP]:
+                return
+
+
+def _sum_lr(xs):
+    t = 0.0
+    for x in xs:
+        t = t + x
+    return t
+
+
+def _ieee_div(a, b):
+    """a / b with IEEE results for b == 0 (inf or nan, as the reference's
+    tensor arithmetic gives) instead of Python's ZeroDivisionError."""
+    if b != 0.0 or b != b:
+        return a / b
+    if a != a or a == 0.0:
+        return math.nan
+    return math.copysign(math.inf, a) * math.copysign(1.0, b)
 
 
 # Set [True] to run the captured sequences as individual launches (for
@@ -147,9 +187,18 @@ class VEGAS(BaseIntegrator):
         self._starting_N = N // (self._max_iterations + 5)
         self._N_increment = N // (self._max_iterations + 5)
         self._fn = fn
-        domain = _setup_integration_domain(dim, integration_domain, backend)
+        # a domain given as host values goes to the fused kernels as launch
+        # arguments; a tensor domain is used where it lives
+        domain_values = _host_domain_values(dim, integration_domain, backend)
+        if domain_values is not None:
+            domain = None
+            device = L.require_cuda()
+            self.dtype = torch.get_default_dtype()
+        else:
+            domain = _setup_integration_domain(dim, integration_domain, backend)
+            device = domain.device
+            self.dtype = domain.dtype
         self.backend = "torch"
-        self.dtype = domain.dtype
         if self.dtype not in (torch.float32, torch.float64):
             raise ValueError(f"unsupported domain dtype {self.dtype}")
         if rng is None:
@@ -157,15 +206,6 @@ class VEGAS(BaseIntegrator):
         elif seed is not None:
             raise ValueError("seed and rng cannot both be passed")
         self.rng = rng
-
-        domain_starts = domain[:, 0]
-        domain_sizes = domain[:, 1] - domain_starts
-        domain_volume = torch.prod(domain_sizes)
-
-        def transformed_integrand(x):
-            return fn(x * domain_sizes + domain_starts) * domain_volume
-
-        self._fn = transformed_integrand
 
         N_intervals = n_intervals if n_intervals is not None else max(2, self._N_increment // 10)
         n_strat = n_strat_for(self._N_increment, dim)
@@ -177,58 +217,72 @@ class VEGAS(BaseIntegrator):
             isinstance(fn, BuiltinIntegrand)
             and type(rng) is RNG
             and fn.dim == dim
-            and not (torch.is_grad_enabled() and (domain.requires_grad or fn.requires_grad()))
+            and not (torch.is_grad_enabled()
+                     and ((domain is not None and domain.requires_grad) or fn.requires_grad()))
         )
         if fused:
             ns = self._starting_N // 5 if use_warmup else 0
             plan = _FusedPlan.get(
-                lambda: VegasDevice(dim, self.dtype, N_intervals, n_strat, domain.device, domain,
+                lambda: VegasDevice(dim, self.dtype, N_intervals, n_strat, device, domain,
                                     stats_slots=max_iterations + 10),
-                (str(domain.device), torch.cuda.current_stream().cuda_stream, dim, self.dtype,
+                (str(device), torch.cuda.current_stream().cuda_stream, dim, self.dtype,
                  N_intervals, n_strat), fn.family,
                 use_grid_improve, use_warmup, ns, max_iterations)
             self._dev = plan.dev
         else:
+            if domain is None:
+                domain = torch.tensor(domain_values, dtype=self.dtype).to(device)
             plan = None
-            self._dev = VegasDevice(dim, self.dtype, N_intervals, n_strat, domain.device, domain,
+            self._dev = VegasDevice(dim, self.dtype, N_intervals, n_strat, device, domain,
                                     stats_slots=max(8, max_iterations + 10))
         self.map = VEGASMap(N_intervals, dim, None, self.dtype, _device_state=self._dev)
         self.strat = VEGASStratification(self._N_increment, dim, rng, None, self.dtype,
                                          _device_state=self._dev)
         if fused:
-            return self._integrate_fused(plan, fn, domain, use_warmup)
+            return self._integrate_fused(plan, fn, domain, domain_values, use_warmup)
+
+        domain_starts = domain[:, 0]
+        domain_sizes = domain[:, 1] - domain_starts
+        domain_volume = torch.prod(domain_sizes)
+
+        def transformed_integrand(x):
+            return fn(x * domain_sizes + domain_starts) * domain_volume
+
+        self._fn = transformed_integrand
         return self._integrate_materialised(domain, use_warmup)
 
     # ------------------------------------------------------------ fused
-    def _integrate_fused(self, plan, fn, domain, use_warmup):
+    def _integrate_fused(self, plan, fn, domain, domain_values, use_warmup):
+        """The whole run on the device (warm-up, blocks of five iterations,
+        the abort test after each block); one read-back at the end gives the
+        host the reference's attributes (it, results, sigma2, evaluations,
+        _starting_N) and the RNG offset."""
         rng = self.rng
-        ns = plan.ns
         dev = plan.dev
-        dev.set_domain(domain)
-        dev.params.copy_(fn.device_params(domain.device))
-        dev.rng_offset.fill_(rng.offset)
-        dev.set_control(L.TQ_VC_NEVALS | L.TQ_VC_SEED | L.TQ_VC_STREAM, nevals=self._starting_N,
-                        seed=rng.seed, sid=rng.stream_id)
+        if domain_values is None:
+            dev.set_domain(domain)
+        warm_evals = 5 * plan.ns if use_warmup else 0
+        dev.dh_pending = False
+        dev.begin_run(self._starting_N, self.N, self._N_increment, self._max_iterations, warm_evals,
+                      self._eps_rel, self._eps_abs, rng.seed, rng.stream_id, rng.offset,
+                      fn.params_numpy(), domain_values)
         self.alpha = ALPHA
-        plan.run_warmup()
-        warm_evals = 5 * ns if use_warmup else 0
-        self._nr_of_fevals = warm_evals
-        while True:
-            dev.set_control(L.TQ_VC_NEVALS, nevals=self._starting_N)
-            plan.run_block()
-            self.it += 5
-            stats = dev.stats[: self.it].cpu()  # one host sync per five iterations
-            self.map.check_flags()
-            self.results = [float(v) for v in stats[self.it - 5 : self.it, 0]]
-            self.sigma2 = [float(v) for v in stats[self.it - 5 : self.it, 1]]
-            self._nr_of_fevals = warm_evals + int(stats[: self.it, 2].sum())
-            if self._check_abort_conditions():
-                break
-        rng.offset = int(dev.rng_offset.item())
-        # leave dh normalised, as update_DH does
-        s = dev.scalars[0].to(self.dtype)
-        dev.dh.copy_(torch.where(s != 0, dev.dh / s, dev.dh))
-        return torch.tensor(self._get_result(), dtype=self.dtype, device=domain.device)
+        plan.run()
+        c = dev.host_control
+        if int(c[L.VC_STOP]) == 4:
+            raise RuntimeError("VEGAS ran out of statistics slots")
+        self.it = it = int(c[L.VC_IT])
+        self._starting_N = int(c[L.VC_NEVALS])
+        self._nr_of_fevals = int(c[L.VC_EVALS])
+        st = dev.host_stats
+        self.results = [float(v) for v in st[it - 5 : it, 0]]
+        self.sigma2 = [float(v) for v in st[it - 5 : it, 1]]
+        self.map.check_flags(dev.host_flags)
+        rng.offset = int(dev.host_rng_offset[0])
+        # update_DH leaves dh normalised; done on first access
+        # (VEGASStratification.dh)
+        dev.dh_pending = True
+        return torch.full((), self._get_result(), dtype=self.dtype, device=dev.device)
 
     # ----------------------------------------------------- materialised
     def _integrate_materialised(self, domain, use_warmup):
@@ -322,21 +376,29 @@ class VEGAS(BaseIntegrator):
         self.sigma2 = []
         return False
 
+    # The sums below run left to right from zero, as the reference's sums of
+    # 0-d tensors do (Python's builtin sum of floats is compensated since
+    # 3.12); tq_vegas_abort_test takes them the same way on the device.
     def _get_result(self):
         """Inverse-variance weighted mean of the iteration results (EQ 30)."""
         if any(s == 0.0 for s in self.sigma2):
-            return sum(self.results) / len(self.results)
-        num = sum(r / s for r, s in zip(self.results, self.sigma2))
-        den = sum(1.0 / s for s in self.sigma2)
+            return _sum_lr(self.results) / len(self.results)
+        num = _sum_lr(r / s for r, s in zip(self.results, self.sigma2))
+        den = _sum_lr(1.0 / s for s in self.sigma2)
         return num / den
 
     def _get_error(self):
         """Error estimate from the variances (EQ 31)."""
-        res = sum(1.0 / s for s in self.sigma2 if s != 0.0)
+        res = _sum_lr(1.0 / s for s in self.sigma2 if s != 0.0)
         return self.sigma2[0] if res == 0 else 1.0 / math.sqrt(res)
 
     def _get_chisq(self):
         """Chi square of the iteration results (EQ 32)."""
         I_final = float(self._get_result())
         res = [float(r) for r in self.results]
-        return sum(((r - I_final) ** 2 / s for r, s in zip(res, self.sigma2) if r != I_final), 0.0)
+        chi2 = 0.0
+        for r, s in zip(res, self.sigma2):
+            if r != I_final:
+                d = r - I_final
+                chi2 += _ieee_div(d * d, s)
+        return chi2

@@ -100,10 +100,11 @@ class VEGASMap:
         self._dev.update_map(self.alpha)
         self.check_flags()
 
-    def check_flags(self):
+    def check_flags(self, host_flags=None):
         """Emit the reference's warnings/errors for flags raised on the
-        device since the last check (synchronises)."""
-        f = self._dev.flags.cpu()
+        device since the last check (synchronises unless the flags were read
+        back already and are passed in)."""
+        f = self._dev.flags.cpu() if host_flags is None else host_flags
         if int(f[0]) > self._flags_seen:
             for _ in range(int(f[0]) - self._flags_seen):
                 _cannot_update_warning()

@@ -29,7 +29,13 @@ class VEGASStratification:
 
     @property
     def dh(self):
-        return self._dev.dh
+        d = self._dev
+        if d.dh_pending:  # a fused run ended with update_DH's normalisation pending
+            d.dh_pending = False
+            s = d.scalars[0].to(d.dtype)
+            d.dh.copy_(torch.where(s != 0, d.dh / s, d.dh))
+            d.control[2] = 0  # normalised: get_NH must not divide again
+        return d.dh
 
     @property
     def JF(self):
