@@ -55,6 +55,8 @@ class _FusedPlan:
         self.use_grid_improve, self.use_warmup, self.ns = use_grid_improve, use_warmup, ns
         self.uses = 0
         self.graph = None
+        self._side = torch.cuda.Stream(device=dev.device)
+        self._fork, self._join = torch.cuda.Event(), torch.cuda.Event()
 
     @classmethod
     def get(cls, make_dev, shape_key, family, use_grid_improve, use_warmup, ns, max_iterations):
@@ -78,21 +80,33 @@ class _FusedPlan:
                 d.update_map(ALPHA)
 
     def _block_seq(self):
+        # The map update of an iteration gates only the next sampling
+        # launch, while get_NH needs only the end of the iteration: the map
+        # update runs on a side stream, beside finish and the next get_NH.
         d = self.dev
-        for _ in range(5):
+        main = torch.cuda.current_stream()
+        side, fork, join = self._side, self._fork, self._join
+        for i in range(5):
             d.get_nh()
+            if i > 0 and self.use_grid_improve:
+                main.wait_event(join)
             d.iterate_fused(self.family, d.params, self.use_grid_improve)
             if self.use_grid_improve:
-                d.finish_update_map(BETA, ALPHA)
-            else:
-                d.finish(BETA)
+                fork.record(main)
+                with torch.cuda.stream(side):
+                    side.wait_event(fork)
+                    d.update_map(ALPHA)
+                    join.record(side)
+            d.finish(BETA)
+        if self.use_grid_improve:
+            main.wait_event(join)
 
     def _warm_launches(self):
         per = (1 if self.ns > 0 else 0) + self.dev.update_map_launches
         return 1 + (5 * per if self.use_warmup else 0)
 
     def _block_launches(self):  # five iterations and the abort test
-        return 5 * (3 + (self.dev.finish_update_map_launches if self.use_grid_improve else 1)) + 1
+        return 5 * (4 + (self.dev.update_map_launches if self.use_grid_improve else 0)) + 1
 
     def _capture(self):
         """Records warm-up + WHILE(block, abort test) without running it."""
