@@ -132,23 +132,33 @@ struct AbortArgs {
   int use_handle;
 };
 
-__global__ void vegas_abort_kernel(AbortArgs a) {
+// One warp: the statistics rows are loaded by all lanes at once (the
+// evaluation count is an exact integer sum), the decision is lane 0's.
+__global__ void __launch_bounds__(32) vegas_abort_kernel(AbortArgs a) {
   int64_t* c = a.control;
-  const int64_t it = c[kCtlIt] + 5;
+  const int lane = threadIdx.x;
   const int64_t slot = c[kCtlSlot];  // rows [slot - 5, slot) hold this block
-  int stop;
-  if (slot < 5 || slot > a.n_stat_slots) {
-    stop = 4;  // the statistics slots ran out: nothing valid to test
-  } else {
-    // _nr_of_fevals: the warm-up plus the points of every iteration so far
-    int64_t evals = c[kCtlWarm];
-    for (int64_t i = 0; i < slot; ++i) evals += (int64_t)a.stats[4 * i + 2];
+  const bool ok = slot >= 5 && slot <= a.n_stat_slots;
+  int64_t evals = 0;  // _nr_of_fevals: the warm-up plus the points of every iteration so far
+  double rs = 0.0;    // lane i < 5: result of row slot-5+i; 5 <= i < 10: its variance
+  if (ok) {
+    for (int64_t i = lane; i < slot; i += 32) evals += (int64_t)a.stats[4 * i + 2];
+    if (lane < 10) rs = a.stats[4 * (slot - 5 + lane % 5) + lane / 5];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) evals += __shfl_down_sync(0xffffffffu, evals, o);
+  double r[5], s[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    r[i] = __shfl_sync(0xffffffffu, rs, i);
+    s[i] = __shfl_sync(0xffffffffu, rs, 5 + i);
+  }
+  if (lane != 0) return;
+  const int64_t it = c[kCtlIt] + 5;
+  int stop = 4;  // the statistics slots ran out: nothing valid to test
+  if (ok) {
+    evals += c[kCtlWarm];
     c[kCtlEvals] = evals;
-    double r[5], s[5];
-    for (int i = 0; i < 5; ++i) {
-      r[i] = a.stats[4 * (slot - 5 + i)];
-      s[i] = a.stats[4 * (slot - 5 + i) + 1];
-    }
     int64_t sN = c[kCtlNevals];
     stop = abort_decision(r, s, it, evals, c[kCtlN], c[kCtlNInc], c[kCtlMaxIt],
                           __longlong_as_double(c[kCtlEpsRel]), __longlong_as_double(c[kCtlEpsAbs]),
@@ -192,7 +202,7 @@ extern "C" int tq_vegas_abort_test(const tq_vegas_state* st, uint64_t cond_handl
   a.n_stat_slots = st->n_stat_slots;
   a.handle = (cudaGraphConditionalHandle)cond_handle;
   a.use_handle = cond_handle != 0;
-  vegas_abort_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(a);
+  vegas_abort_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(a);
   return launch_status();
 }
 

@@ -22,6 +22,8 @@
 
 #pragma once
 
+#include <type_traits>
+
 #include "tq_common.cuh"
 
 namespace tq {
@@ -172,22 +174,43 @@ __device__ Smem<T> carve(unsigned char* base, const SampleArgs& a) {
 }
 
 // Warp-private histogram update without atomics: lanes with the same key
-// form a group (__match_any_sync); the members add their values to the bin
-// one per round in lane order (a lane's rank in its group is its round), so
-// no two lanes write one bin in the same round and the order is fixed.  The
-// lowest member adds the group's count.
+// form a group (__match_any_sync) and sum their values by pointer jumping
+// along the group in lane order (ceil(log2(largest group)) shuffle steps: a
+// fixed tree, so the result does not depend on scheduling); the group's
+// lowest lane then adds the sum and the group's size to the bin.  Groups
+// have distinct keys, so no two lanes write one bin.  Stratified points of a
+// tile share cubes, so groups of 8 or more lanes are common.  The caller
+// orders successive calls on the same bins with __syncwarp().
 template <typename H>
 __device__ __forceinline__ void warp_hist_add(H* hw, unsigned* hc, int key, bool valid, H v) {
   const int lane = threadIdx.x & 31;
   const unsigned grp = __match_any_sync(0xffffffffu, key);
-  const unsigned rank = (unsigned)__popc(grp & ((1u << lane) - 1u));
-  const unsigned rounds = __reduce_max_sync(0xffffffffu, valid ? rank : 0u);
-  if (valid && rank == 0u) hc[key] += (unsigned)__popc(grp);
-  for (unsigned r = 0; r <= rounds; ++r) {
-    if (valid && rank == r) hw[key] += v;
-    __syncwarp();
+  const unsigned above = grp & ~((2u << lane) - 1u);  // members after this lane
+  int nxt = above ? __ffs(above) - 1 : 32;
+  const unsigned size = (unsigned)__popc(grp);
+  const unsigned largest = __reduce_max_sync(0xffffffffu, valid ? size : 1u);
+  for (unsigned span = 1; span < largest; span <<= 1) {
+    const H w = __shfl_sync(0xffffffffu, v, nxt & 31);
+    const int n2 = __shfl_sync(0xffffffffu, nxt, nxt & 31);
+    if (nxt < 32) {
+      v += w;
+      nxt = n2;
+    }
+  }
+  if (valid && (grp & ((1u << lane) - 1u)) == 0u) {
+    hw[key] += v;
+    hc[key] += size;
   }
 }
+
+// Philox blocks a point's D draws can touch: a point's first draw sits at
+// word (j*D) mod PB of its first block, at most PB - gcd(D, PB).
+__host__ __device__ constexpr int gcd_c(int a, int b) { return b == 0 ? a : gcd_c(b, a % b); }
+template <int D, int PB>
+struct DrawBlocks {
+  static constexpr int step = gcd_c(D, PB);               // first-word offsets are multiples
+  static constexpr int blocks = (PB - step + D + PB - 1) / PB;
+};
 
 // D > 0: the dimension is known at compile time (fully unrolled point
 // loops, D interval indices in registers); D = 0: any dimension up to
@@ -259,14 +282,13 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
     if (!WARM) {
       const int64_t cl = c0 + lane;
       csl = cl <= st.n_cubes ? st.cube_start[cl] : INT64_MAX;
-      int l = 0;  // largest l with cube_start[c0 + l] <= j
-#pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const int cand = l + step;
-        const int64_t v = __shfl_sync(0xffffffffu, csl, cand & 31);
-        if (cand < 32 && v <= j) l = cand;
-      }
-      slot = valid ? l : -1;
+      // bit p: a cube starts at point j0 + p (cube c0 holds j0, so the
+      // starts of cubes c0 + 1.. lie after j0); the slot of point j0 + p
+      // (largest l with cube_start[c0 + l] <= j) counts the starts in bits 1..p
+      const int64_t off = csl - j0;
+      const unsigned bit = (off > 0 && off < 32) ? (1u << (int)off) : 0u;
+      const unsigned starts = __reduce_or_sync(0xffffffffu, bit);
+      slot = valid ? __popc(starts & ((2u << lane) - 1u)) : -1;
     }
     H jfd = 0, jf2 = 0;
     int ids[KD];
@@ -279,18 +301,44 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
       const int lane0 = (int)(e0 % PB);
       int cur = -1;
       uint4 r = make_uint4(0, 0, 0, 0);
+      // fp32 with the dimension fixed: every lane computes the blocks its
+      // draws can touch at once (no divergent per-draw block branch) and
+      // picks its words by its first word's offset
+      constexpr bool kWords = std::is_same<T, float>::value && D > 0;
+      constexpr int NB = kWords ? DrawBlocks<(D > 0 ? D : 1), PB>::blocks : 1;
+      constexpr int GS = kWords ? DrawBlocks<(D > 0 ? D : 1), PB>::step : 1;
+      uint32_t words[4 * NB];
+      if constexpr (kWords) {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+          const uint4 rb = philox_block(seed, sid, blk0 + (uint64_t)b);
+          words[4 * b] = rb.x;
+          words[4 * b + 1] = rb.y;
+          words[4 * b + 2] = rb.z;
+          words[4 * b + 3] = rb.w;
+        }
+      }
       T jac = (T)1;
       T s = T(0);
 #pragma unroll
       for (int k = 0; k < KD; ++k) {
         if (k < d) {
-          const int le = lane0 + k;
-          const int bi = le / PB;
-          if (bi != cur) {
-            r = philox_block(seed, sid, blk0 + (uint64_t)bi);
-            cur = bi;
+          T u;
+          if constexpr (kWords) {
+            uint32_t w = words[k];
+#pragma unroll
+            for (int o = GS; o < PB; o += GS)
+              if (k + o < 4 * NB) w = lane0 == o ? words[k + o] : w;
+            u = (T)u32_to_unit_f(w);
+          } else {
+            const int le = lane0 + k;
+            const int bi = le / PB;
+            if (bi != cur) {
+              r = philox_block(seed, sid, blk0 + (uint64_t)bi);
+              cur = bi;
+            }
+            u = Uniform<T>::from(r, le - bi * PB);
           }
-          const T u = Uniform<T>::from(r, le - bi * PB);
           T y;
           if (WARM) {
             y = mul_rn(u, warm_scale<T>());
@@ -334,6 +382,7 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
           }
         }
       }
+      if (a.hist_smem) __syncwarp();  // the next tile's groups may differ
     }
     if (!WARM) {
       // points are in cube order: segmented inclusive scan over the warp,
