@@ -250,9 +250,6 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
       sm.hc[i] = 0u;
     }
   }
-  __syncthreads();
-  H* whw = a.hist_smem ? sm.hw + warp * DB : nullptr;
-  unsigned* whc = a.hist_smem ? sm.hc + warp * DB : nullptr;
 
   const int64_t M = WARM ? a.n_samples : st.cube_start[st.n_cubes];
   const uint64_t offset = *st.rng_offset;
@@ -266,19 +263,25 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
   // Warp tiles of 32 consecutive points; every cube has >= 2 points, so a
   // tile spans at most 17 cubes.  Each warp takes a contiguous range of
   // tiles (balanced to one tile), finds the cube of its first point once and
-  // then walks the cube boundaries tile by tile.
+  // then walks the cube boundaries tile by tile.  The search (dependent
+  // global loads) runs before the barrier, beside the loads of the map and
+  // the integrand parameters.
   const int64_t n_tiles = (M + 31) / 32;
   const int64_t n_warps = (int64_t)gridDim.x * kWarps;
   const int64_t gw = (int64_t)blockIdx.x * kWarps + warp;
   const int64_t t_begin = gw * n_tiles / n_warps, t_end = (gw + 1) * n_tiles / n_warps;
   int64_t c0 = 0;  // cube of the tile's first point
   if (!WARM && t_begin < t_end) c0 = warp_find_cube(st.cube_start, st.n_cubes, t_begin * 32);
+  __syncthreads();
+  H* whw = a.hist_smem ? sm.hw + warp * DB : nullptr;
+  unsigned* whc = a.hist_smem ? sm.hc + warp * DB : nullptr;
   for (int64_t wt = t_begin; wt < t_end; ++wt) {
     const int64_t j0 = wt * 32;
     const int64_t j = j0 + lane;
     const bool valid = j < M;
     int slot = -1;
     int64_t csl = 0;
+    unsigned starts = 0u;
     if (!WARM) {
       const int64_t cl = c0 + lane;
       csl = cl <= st.n_cubes ? st.cube_start[cl] : INT64_MAX;
@@ -287,7 +290,7 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
       // (largest l with cube_start[c0 + l] <= j) counts the starts in bits 1..p
       const int64_t off = csl - j0;
       const unsigned bit = (off > 0 && off < 32) ? (1u << (int)off) : 0u;
-      const unsigned starts = __reduce_or_sync(0xffffffffu, bit);
+      starts = __reduce_or_sync(0xffffffffu, bit);
       slot = valid ? __popc(starts & ((2u << lane) - 1u)) : -1;
     }
     H jfd = 0, jf2 = 0;
@@ -387,18 +390,21 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
     if (!WARM) {
       // points are in cube order: segmented inclusive scan over the warp,
       // then one global add per cube segment
+      // lane's segment starts at the last cube start at or before it
+      const unsigned upto = starts & ((2u << lane) - 1u);
+      const int head = upto ? 31 - __clz(upto) : 0;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const H a1 = __shfl_up_sync(0xffffffffu, jfd, o);
         const H a2 = __shfl_up_sync(0xffffffffu, jf2, o);
-        const int so = __shfl_up_sync(0xffffffffu, slot, o);
-        if (lane >= o && so == slot) {
+        if (lane - o >= head) {
           jfd += a1;
           jf2 += a2;
         }
       }
-      const int next = __shfl_down_sync(0xffffffffu, slot, 1);
-      if (slot >= 0 && (lane == 31 || next != slot)) {
+      // segment end: a cube starts at the next point, or this is the last
+      const bool seg_end = lane == 31 || (((starts >> 1) >> lane) & 1u) != 0u || j + 1 >= M;
+      if (slot >= 0 && seg_end) {
         atomicAdd(st.jf + c0 + slot, (double)jfd);
         atomicAdd(st.jf2 + c0 + slot, (double)jf2);
       }
