@@ -517,7 +517,8 @@ def run_gpu(args):
     # run as individual launches, CUDA events around every fused sampling
     # launch on the launching (current) stream
     sampler_events, sampler_points = [], []
-    other_events = {"update_map": [], "finish": [], "finish_update_map": [], "get_nh": [], "warmup_fused": []}
+    other_events = {"update_map": [], "finish": [], "finish_update_map": [], "get_nh": [], "get_nh_split": [],
+                    "warmup_fused": []}
     orig_iter = V.VegasDevice.iterate_fused
     originals = {name: getattr(V.VegasDevice, name) for name in other_events}
 
@@ -606,8 +607,6 @@ def run_gpu(args):
 
     # ---- FP32 FMA peak (measured in this run)
     out = torch.zeros(1, dtype=torch.float32, device=dev)
-    import ctypes
-
     flops = ctypes.c_double(0.0)
     peaks = []
     for _ in range(3):

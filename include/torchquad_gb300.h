@@ -284,7 +284,9 @@ typedef struct tq_vegas_state {
                          * [10] warm-up evaluations, [11] iterations done,
                          * [12] stop reason (0 go on, 1 accuracy reached,
                          * 2 evaluation budget, 3 iteration limit, 4 out of
-                         * statistics slots), [13] evaluations so far        */
+                         * statistics slots), [13] evaluations so far,
+                         * [14] 1 while cube_start is split (see
+                         * tq_vegas_get_nh_split)                          */
 } tq_vegas_state;
 
 enum {
@@ -386,6 +388,14 @@ int tq_vegas_smooth_weights(const tq_vegas_state* st, double alpha, void* smooth
  * (vegas_stratification.py:88-90) and control[2] is cleared. */
 int tq_vegas_get_nh(const tq_vegas_state* st, void* workspace, size_t workspace_bytes,
                     void* stream);
+/* get_NH without the fix-up launch: cube_start is left split (each
+ * 256-cube block's prefix local to the block, the block offsets in the
+ * workspace) and control[14] = 1.  tq_vegas_iterate_fused adds the offsets
+ * where it reads cube_start, and tq_vegas_finish_iteration (or
+ * tq_vegas_finish_update_map) writes them back and clears control[14].  For
+ * sequences that run exactly get_NH, the fused sampling and finish. */
+int tq_vegas_get_nh_split(const tq_vegas_state* st, void* workspace, size_t workspace_bytes,
+                          void* stream);
 
 /* One stratified iteration, fused (vegas.py:274-291): for every point of
  * every cube (cube_start order), y = (cube position + u) / n_strat

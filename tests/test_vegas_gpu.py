@@ -466,3 +466,43 @@ def test_fused_host_domain_and_dh_normalised(cuda):
     assert abs(float(dh_a.double().sum()) - 1.0) < 1e-5
     assert torch.equal(b.strat.dh, dh_a)
     assert torch.equal(b.strat.dh, dh_a)  # a second access does not divide again
+
+
+_STATE_TENSORS = ("x_edges", "dx_edges", "weights", "counts", "dh", "jf", "jf2", "neval",
+                  "cube_start", "rng_offset", "stats", "flags", "scalars", "control")
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_split_get_nh_matches_get_nh(dtype, cuda):
+    """get_NH leaving cube_start split (block offsets added by the sampler,
+    written back by finish) gives the same points, counts and final cube
+    prefix as get_NH with its fix-up launch."""
+    f = tq.GaussianPeak.normal(4, 0.5, 0.1)
+    params = f.device_params(cuda)
+    d = VegasDevice(4, dtype, 50, 20, cuda)  # 160000 cubes: 625 blocks of 256
+    d.set_control(L.TQ_VC_NEVALS | L.TQ_VC_SEED | L.TQ_VC_STREAM, nevals=700000, seed=3, sid=0)
+    d.warmup_fused(f.family, params, 50000)
+    d.update_map(0.5)
+    d.get_nh()
+    d.iterate_fused(f.family, params, True)
+    d.finish(0.75)
+    snap = {n: getattr(d, n).clone() for n in _STATE_TENSORS}
+    out = []
+    for split in (False, True):
+        for n in _STATE_TENSORS:
+            getattr(d, n).copy_(snap[n])
+        if split:
+            d.get_nh_split()
+            assert int(d.control[14].item()) == 1
+        else:
+            d.get_nh()
+        d.iterate_fused(f.family, params, True)
+        d.finish(0.75)
+        out.append({n: getattr(d, n).clone() for n in _STATE_TENSORS})
+    a, b = out
+    for n in ("neval", "cube_start", "counts", "rng_offset", "dh"):
+        assert torch.equal(a[n], b[n]), n
+    assert torch.equal(a["stats"][:, 2], b["stats"][:, 2])
+    assert int(b["control"][14].item()) == 0
+    assert torch.allclose(a["jf"], b["jf"], rtol=1e-12, atol=0)
+    assert torch.allclose(a["weights"], b["weights"], rtol=1e-12, atol=0)

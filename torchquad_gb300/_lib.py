@@ -155,6 +155,7 @@ SIGNATURES = {
     "tq_vegas_update_map": (c_int, [_VS, c_double, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_smooth_weights": (c_int, [_VS, c_double, c_void_p, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_get_nh": (c_int, [_VS, c_void_p, c_size_t, c_void_p]),
+    "tq_vegas_get_nh_split": (c_int, [_VS, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_iterate_fused": (c_int, [_VS, c_int, c_void_p, c_int, c_int64, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_finish_iteration": (c_int, [_VS, c_double, c_void_p, c_size_t, c_void_p]),
     "tq_vegas_finish_update_map": (c_int, [_VS, c_double, c_double, c_void_p, c_size_t, c_void_p]),

@@ -13,6 +13,10 @@ namespace tq {
 
 constexpr int kMaxDim = TQ_MAX_DIM;
 constexpr int kBlock = 256;  // threads per CTA of the streaming kernels
+// VEGAS control block entry: 1 while cube_start holds prefixes local to each
+// kBlock-cube block of get_NH, the block offsets being in the workspace
+// (tq_vegas_get_nh_split); the sampler adds them, finish writes them back.
+constexpr int kCtlSplit = 14;
 
 // ---------------------------------------------------------------- host side
 int set_cuda_error(cudaError_t e);  // records e, returns TQ_ERR_CUDA

@@ -17,6 +17,7 @@ struct NhArgs {
   tq_vegas_state st;
   int64_t* block_tot;  // [blocks]
   unsigned* ticket;
+  int split;  // leave cube_start block-local (see kCtlSplit)
 };
 
 template <typename T>
@@ -98,6 +99,7 @@ __global__ void __launch_bounds__(kBlock) vegas_nh_kernel(NhArgs a) {
     if (threadIdx.x == 0) {
       st.cube_start[st.n_cubes] = carry;
       st.control[2] = 0;
+      st.control[kCtlSplit] = a.split;
       *a.ticket = 0u;
     }
   }
@@ -116,6 +118,7 @@ struct FinishArgs {
   double V;       // V_cubes = (1/n_strat)^dim, computed on the host
   Acc* partials;  // [blocks][3]
   unsigned* ticket;
+  const int64_t* block_pre;  // block offsets of a split cube_start (kCtlSplit)
 };
 
 // Three plain fp64 tree sums over the CTA at once (pairwise: error O(log n)
@@ -157,8 +160,10 @@ __device__ void finish_body(const FinishArgs& a, unsigned bid, unsigned nblk) {
   const T Vt = (T)V, V2t = (T)(V * V);
   const T beta = (T)a.beta;
   double res = 0.0, s2 = 0.0, dsum = 0.0;
+  const bool split = st.control[kCtlSplit] != 0;
   for (int64_t c = (int64_t)bid * blockDim.x + threadIdx.x; c < st.n_cubes;
        c += (int64_t)nblk * blockDim.x) {
+    if (split) st.cube_start[c] += a.block_pre[c / kBlock];
     const int64_t nn = st.neval[c];
     const double J = st.jf[c], J2 = st.jf2[c];
     const double inv = 1.0 / (double)nn;
@@ -209,6 +214,7 @@ __device__ void finish_body(const FinishArgs& a, unsigned bid, unsigned nblk) {
       }
       st.control[1] = slot + 1;
       st.control[2] = 1;
+      st.control[kCtlSplit] = 0;  // cube_start is global again
       // the sum the reference normalises with is taken in the state dtype
       st.scalars[0] = (double)(T)(ds.s + ds.c);
       *a.ticket = 0u;
@@ -241,8 +247,10 @@ __device__ void finish_f32_body(const FinishArgs& a, unsigned bid, unsigned nblk
   const float Vt = (float)a.V, V2t = (float)(a.V * a.V);
   const float beta = (float)a.beta;
   F2 res{0.f, 0.f}, s2{0.f, 0.f}, dsum{0.f, 0.f};
+  const bool split = st.control[kCtlSplit] != 0;
   for (int64_t c = (int64_t)bid * blockDim.x + threadIdx.x; c < st.n_cubes;
        c += (int64_t)nblk * blockDim.x) {
+    if (split) st.cube_start[c] += a.block_pre[c / kBlock];
     const int64_t nn = st.neval[c];
     const float cnt = (float)nn;  // the reference's JF / neval in the state dtype
     const float jT = __double2float_rn(st.jf[c]), j2T = __double2float_rn(st.jf2[c]);
@@ -304,6 +312,7 @@ __device__ void finish_f32_body(const FinishArgs& a, unsigned bid, unsigned nblk
       }
       st.control[1] = slot + 1;
       st.control[2] = 1;
+      st.control[kCtlSplit] = 0;  // cube_start is global again
       // the sum the reference normalises with is taken in the state dtype
       st.scalars[0] = (double)__fadd_rn(ds.hi, ds.lo);
       *a.ticket = 0u;
@@ -1293,6 +1302,7 @@ __global__ void vegas_init_kernel(tq_vegas_state st) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st.control[1] = 0;
     st.control[2] = 0;
+    st.control[kCtlSplit] = 0;
   }
 }
 
@@ -1478,7 +1488,7 @@ extern "C" int tq_vegas_init(const tq_vegas_state* st, void* stream) {
 
 static int launch_sample(const tq_vegas_state* st, int family, const double* params,
                          int64_t n_samples, int use_map, int64_t max_points, bool warm,
-                         unsigned* ticket, cudaStream_t s) {
+                         unsigned* ticket, const int64_t* block_pre, cudaStream_t s) {
   SampleArgs a;
   a.st = *st;
   a.family = family;
@@ -1486,6 +1496,7 @@ static int launch_sample(const tq_vegas_state* st, int family, const double* par
   a.n_samples = n_samples;
   a.use_map = use_map;
   a.ticket = ticket;
+  a.block_pre = block_pre;
   a.small_cubes = st->n_cubes < (int64_t(1) << 32) && st->n_strat < (int64_t(1) << 31);
   a.ns_div = make_fastdiv((uint32_t)(a.small_cubes ? st->n_strat : 1));
   const size_t tsize = dtype_size(st->dtype);
@@ -1539,7 +1550,7 @@ extern "C" int tq_vegas_warmup_fused(const tq_vegas_state* st, int family, const
                                      void* stream) {
   TQ_VEGAS_WS();
   if (!params || n_samples < 1) return TQ_ERR_ARG;
-  return launch_sample(st, family, params, n_samples, 1, n_samples, true, ws.t_sample, s);
+  return launch_sample(st, family, params, n_samples, 1, n_samples, true, ws.t_sample, nullptr, s);
 }
 
 extern "C" int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, const double* params,
@@ -1548,7 +1559,7 @@ extern "C" int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, cons
   TQ_VEGAS_WS();
   if (!params || max_points < 0) return TQ_ERR_ARG;
   return launch_sample(st, family, params, 0, use_grid_improve ? 1 : 0, max_points, false,
-                       ws.t_sample, s);
+                       ws.t_sample, ws.block_tot, s);
 }
 
 static int launch_update_map(const tq_vegas_state* st, double alpha, void* workspace,
@@ -1614,22 +1625,33 @@ extern "C" int tq_vegas_smooth_weights(const tq_vegas_state* st, double alpha, v
   return launch_update_map(st, alpha, workspace, workspace_bytes, smoothed, stream);
 }
 
-extern "C" int tq_vegas_get_nh(const tq_vegas_state* st, void* workspace, size_t workspace_bytes,
-                               void* stream) {
+static int launch_nh(const tq_vegas_state* st, void* workspace, size_t workspace_bytes,
+                     void* stream, bool split) {
   TQ_VEGAS_WS();
   NhArgs a;
   a.st = *st;
   a.block_tot = ws.block_tot;
   a.ticket = ws.t_nh;
+  a.split = split ? 1 : 0;
   const unsigned g = (unsigned)nh_blocks(st);
   if (st->dtype == TQ_F64)
     vegas_nh_kernel<double><<<g, kBlock, 0, s>>>(a);
   else
     vegas_nh_kernel<float><<<g, kBlock, 0, s>>>(a);
   int e = launch_status();
-  if (e != TQ_OK) return e;
+  if (e != TQ_OK || split) return e;
   vegas_nh_fixup_kernel<<<g, kBlock, 0, s>>>(*st, ws.block_tot);
   return launch_status();
+}
+
+extern "C" int tq_vegas_get_nh(const tq_vegas_state* st, void* workspace, size_t workspace_bytes,
+                               void* stream) {
+  return launch_nh(st, workspace, workspace_bytes, stream, false);
+}
+
+extern "C" int tq_vegas_get_nh_split(const tq_vegas_state* st, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+  return launch_nh(st, workspace, workspace_bytes, stream, true);
 }
 
 extern "C" int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, void* workspace,
@@ -1641,6 +1663,7 @@ extern "C" int tq_vegas_finish_iteration(const tq_vegas_state* st, double beta, 
   a.V = pow(1.0 / (double)st->n_strat, (double)st->dim);
   a.partials = ws.partials;
   a.ticket = ws.t_finish;
+  a.block_pre = ws.block_tot;
   const unsigned g = (unsigned)finish_blocks(st);
   if (st->dtype == TQ_F64)
     vegas_finish_kernel<double><<<g, kBlock, 0, s>>>(a);
@@ -1663,6 +1686,7 @@ extern "C" int tq_vegas_finish_update_map(const tq_vegas_state* st, double beta,
   a.V = pow(1.0 / (double)st->n_strat, (double)st->dim);
   a.partials = ws.partials;
   a.ticket = ws.t_finish;
+  a.block_pre = ws.block_tot;
   const unsigned g = (unsigned)finish_blocks(st) + (unsigned)st->dim;
   const size_t smem = map_row_smem(st->n_bins, dtype_size(st->dtype));
 #define TQ_FINISH_MAP(T)                                                                      \

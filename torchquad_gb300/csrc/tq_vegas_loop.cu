@@ -68,44 +68,66 @@ __global__ void vegas_begin_run_kernel(RunArgs a) {
 // gives); written out so the compiler's fast paths cannot change it.
 __device__ __forceinline__ double qdiv(double x, double y) { return __ddiv_rn(x, y); }
 
-// The decision of _check_abort_conditions for the five results r[] and
-// variances s[] of the block that just ended, in the host code's operation
-// order (every sum left to right from zero).  Returns the stop reason
-// (0: go on) and updates *sN (VEGAS._starting_N).
-__device__ int abort_decision(const double* r, const double* s, int64_t it, int64_t evals,
-                              int64_t N, int64_t n_inc, int64_t max_it, double eps_rel,
-                              double eps_abs, int64_t* sN) {
+// _check_abort_conditions for the block that just ended, in the host code's
+// operation order (every sum left to right from zero), on one warp: lane i
+// < 5 holds result r_i and variance s_i of the block's i-th iteration.  The
+// quotients of the rows are taken by their own lanes at once (the same
+// operations as one thread would do); the sums and the decision are taken
+// by every lane alike.  Returns the stop reason (0: go on) and updates *sN
+// (VEGAS._starting_N).
+__device__ int abort_decision_warp(double r_mine, double s_mine, int64_t it, int64_t evals,
+                                   int64_t N, int64_t n_inc, int64_t max_it, double eps_rel,
+                                   double eps_abs, int64_t* sN) {
+  const int lane = threadIdx.x & 31;
+  const bool row = lane < 5;
+  const unsigned zeros = __ballot_sync(0xffffffffu, row && s_mine == 0.0);
+  const double q_mine = row ? qdiv(r_mine, s_mine) : 0.0;    // r_i / s_i
+  const double inv_mine = row ? qdiv(1.0, s_mine) : 0.0;     // 1 / s_i
+  double r[5], s[5], q[5], inv[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    r[i] = __shfl_sync(0xffffffffu, r_mine, i);
+    s[i] = __shfl_sync(0xffffffffu, s_mine, i);
+    q[i] = __shfl_sync(0xffffffffu, q_mine, i);
+    inv[i] = __shfl_sync(0xffffffffu, inv_mine, i);
+  }
   // _get_result (EQ 30)
-  bool zero_var = false;
-  for (int i = 0; i < 5; ++i) zero_var = zero_var || s[i] == 0.0;
   double res;
-  if (zero_var) {
+  if (zeros) {
     double t = 0.0;
     for (int i = 0; i < 5; ++i) t = __dadd_rn(t, r[i]);
     res = qdiv(t, 5.0);
   } else {
     double num = 0.0, den = 0.0;
-    for (int i = 0; i < 5; ++i) num = __dadd_rn(num, qdiv(r[i], s[i]));
-    for (int i = 0; i < 5; ++i) den = __dadd_rn(den, qdiv(1.0, s[i]));
+    for (int i = 0; i < 5; ++i) {
+      num = __dadd_rn(num, q[i]);
+      den = __dadd_rn(den, inv[i]);
+    }
     res = qdiv(num, den);
   }
   const double res_abs = fabs(res);
   // _get_error (EQ 31)
-  double inv = 0.0;
+  double isum = 0.0;
   for (int i = 0; i < 5; ++i)
-    if (s[i] != 0.0) inv = __dadd_rn(inv, qdiv(1.0, s[i]));
-  const double err = inv == 0.0 ? s[0] : qdiv(1.0, __dsqrt_rn(inv));
-  // _get_chisq (EQ 32)
-  double chi2 = 0.0;
-  for (int i = 0; i < 5; ++i) {
-    if (r[i] != res) {
-      const double d = __dsub_rn(r[i], res);
-      chi2 = __dadd_rn(chi2, qdiv(__dmul_rn(d, d), s[i]));
-    }
+    if (s[i] != 0.0) isum = __dadd_rn(isum, inv[i]);
+  const double err = isum == 0.0 ? s[0] : qdiv(1.0, __dsqrt_rn(isum));
+  // _get_chisq (EQ 32): each row's term on its lane, summed in row order
+  const bool use = row && r_mine != res;
+  double term = 0.0;
+  if (use) {
+    const double d = __dsub_rn(r_mine, res);
+    term = qdiv(__dmul_rn(d, d), s_mine);
   }
-  const double q = qdiv(chi2, 5.0);
-  if ((err <= __dmul_rn(eps_rel, res_abs) || err <= eps_abs) && q < 1.0) return 1;
-  if (q < 1.0) {
+  const unsigned used = __ballot_sync(0xffffffffu, use);
+  double chi2 = 0.0;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const double t = __shfl_sync(0xffffffffu, term, i);
+    if (used >> i & 1u) chi2 = __dadd_rn(chi2, t);
+  }
+  const double qc = qdiv(chi2, 5.0);
+  if ((err <= __dmul_rn(eps_rel, res_abs) || err <= eps_abs) && qc < 1.0) return 1;
+  if (qc < 1.0) {
     if (res_abs == 0.0) {
       *sN += n_inc;
     } else {
@@ -116,7 +138,7 @@ __device__ int abort_decision(const double* r, const double* s, int64_t it, int6
       const int64_t t = __double2ll_rz(x);
       *sN = min(*sN + n_inc, t);
     }
-  } else if (q > 1.0) {
+  } else if (qc > 1.0) {
     *sN += n_inc;
   }
   if (evals + *sN * 5 > N) return 2;
@@ -133,36 +155,34 @@ struct AbortArgs {
 };
 
 // One warp: the statistics rows are loaded by all lanes at once (the
-// evaluation count is an exact integer sum), the decision is lane 0's.
+// evaluation count is an exact integer sum); lane 0 writes the outcome.
 __global__ void __launch_bounds__(32) vegas_abort_kernel(AbortArgs a) {
   int64_t* c = a.control;
   const int lane = threadIdx.x;
   const int64_t slot = c[kCtlSlot];  // rows [slot - 5, slot) hold this block
   const bool ok = slot >= 5 && slot <= a.n_stat_slots;
   int64_t evals = 0;  // _nr_of_fevals: the warm-up plus the points of every iteration so far
-  double rs = 0.0;    // lane i < 5: result of row slot-5+i; 5 <= i < 10: its variance
+  double r_mine = 0.0, s_mine = 0.0;
   if (ok) {
     for (int64_t i = lane; i < slot; i += 32) evals += (int64_t)a.stats[4 * i + 2];
-    if (lane < 10) rs = a.stats[4 * (slot - 5 + lane % 5) + lane / 5];
+    if (lane < 5) {
+      r_mine = a.stats[4 * (slot - 5 + lane)];
+      s_mine = a.stats[4 * (slot - 5 + lane) + 1];
+    }
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) evals += __shfl_down_sync(0xffffffffu, evals, o);
-  double r[5], s[5];
-#pragma unroll
-  for (int i = 0; i < 5; ++i) {
-    r[i] = __shfl_sync(0xffffffffu, rs, i);
-    s[i] = __shfl_sync(0xffffffffu, rs, 5 + i);
-  }
-  if (lane != 0) return;
+  for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
   const int64_t it = c[kCtlIt] + 5;
   int stop = 4;  // the statistics slots ran out: nothing valid to test
+  int64_t sN = c[kCtlNevals];
+  evals += c[kCtlWarm];
+  if (ok)
+    stop = abort_decision_warp(r_mine, s_mine, it, evals, c[kCtlN], c[kCtlNInc], c[kCtlMaxIt],
+                               __longlong_as_double(c[kCtlEpsRel]),
+                               __longlong_as_double(c[kCtlEpsAbs]), &sN);
+  if (lane != 0) return;
   if (ok) {
-    evals += c[kCtlWarm];
     c[kCtlEvals] = evals;
-    int64_t sN = c[kCtlNevals];
-    stop = abort_decision(r, s, it, evals, c[kCtlN], c[kCtlNInc], c[kCtlMaxIt],
-                          __longlong_as_double(c[kCtlEpsRel]), __longlong_as_double(c[kCtlEpsAbs]),
-                          &sN);
     c[kCtlNevals] = sN;
   }
   c[kCtlIt] = it;

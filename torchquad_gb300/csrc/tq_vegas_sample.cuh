@@ -80,23 +80,31 @@ __device__ __forceinline__ T strat_y(int pos, T u, T nsf) {
   return y >= (T)1 ? warm_scale<T>() : y;
 }
 
-// Largest c in [0, n) with cs[c] <= target; cs strictly increasing, cs[0] = 0.
-// One warp, 32-ary search with coalesced probes.
-__device__ __forceinline__ int64_t warp_find_cube(const int64_t* __restrict__ cs, int64_t n,
+// cube_start[c] for c < n_cubes; pre != nullptr: cube_start is split
+// (kCtlSplit) and pre holds the offsets of its kBlock-cube blocks.
+__device__ __forceinline__ int64_t cube_start_at(const int64_t* __restrict__ cs,
+                                                 const int64_t* __restrict__ pre, int64_t c) {
+  return pre ? cs[c] + pre[c / kBlock] : cs[c];
+}
+
+// Largest c in [0, n) with cube_start[c] <= target; strictly increasing,
+// cube_start[0] = 0.  One warp, 32-ary search with coalesced probes.
+__device__ __forceinline__ int64_t warp_find_cube(const int64_t* __restrict__ cs,
+                                                  const int64_t* __restrict__ pre, int64_t n,
                                                   int64_t target) {
   const int lane = threadIdx.x & 31;
   int64_t lo = 0, hi = n;
   while (hi - lo > 32) {
     const int64_t step = (hi - lo + 31) / 32;
     const int64_t pos = lo + lane * step;
-    const bool ok = pos < hi && cs[pos] <= target;
+    const bool ok = pos < hi && cube_start_at(cs, pre, pos) <= target;
     const unsigned m = __ballot_sync(0xffffffffu, ok);
     const int last = 31 - __clz(m);
     lo = lo + last * step;
     hi = min(hi, lo + step);
   }
   const int64_t pos = lo + lane;
-  const bool ok = pos < hi && cs[pos] <= target;
+  const bool ok = pos < hi && cube_start_at(cs, pre, pos) <= target;
   const unsigned m = __ballot_sync(0xffffffffu, ok);
   return lo + (31 - __clz(m));
 }
@@ -112,6 +120,7 @@ struct SampleArgs {
   int small_cubes;    // n_cubes < 2^32: cube digits with 32-bit division
   FastDiv ns_div;     // division by n_strat
   unsigned* ticket;
+  const int64_t* block_pre;  // block offsets of a split cube_start (kCtlSplit)
 };
 
 // Histogram weight type in shared memory: fp32 atomics are native, so the
@@ -271,7 +280,8 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
   const int64_t gw = (int64_t)blockIdx.x * kWarps + warp;
   const int64_t t_begin = gw * n_tiles / n_warps, t_end = (gw + 1) * n_tiles / n_warps;
   int64_t c0 = 0;  // cube of the tile's first point
-  if (!WARM && t_begin < t_end) c0 = warp_find_cube(st.cube_start, st.n_cubes, t_begin * 32);
+  const int64_t* pre = (!WARM && st.control[kCtlSplit] != 0) ? a.block_pre : nullptr;
+  if (!WARM && t_begin < t_end) c0 = warp_find_cube(st.cube_start, pre, st.n_cubes, t_begin * 32);
   __syncthreads();
   H* whw = a.hist_smem ? sm.hw + warp * DB : nullptr;
   unsigned* whc = a.hist_smem ? sm.hc + warp * DB : nullptr;
@@ -284,7 +294,8 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
     unsigned starts = 0u;
     if (!WARM) {
       const int64_t cl = c0 + lane;
-      csl = cl <= st.n_cubes ? st.cube_start[cl] : INT64_MAX;
+      csl = cl < st.n_cubes ? cube_start_at(st.cube_start, pre, cl)
+                            : (cl == st.n_cubes ? st.cube_start[cl] : INT64_MAX);
       // bit p: a cube starts at point j0 + p (cube c0 holds j0, so the
       // starts of cubes c0 + 1.. lie after j0); the slot of point j0 + p
       // (largest l with cube_start[c0 + l] <= j) counts the starts in bits 1..p

@@ -209,6 +209,14 @@ class VegasDevice:
         L.check(L.lib().tq_vegas_get_nh(self.ref, p, n, L.stream_handle()), "tq_vegas_get_nh")
         L.count_launches(2)
 
+    def get_nh_split(self):
+        """get_NH leaving cube_start split until the next finish (one launch
+        instead of two); for the fused get_NH, sampling, finish sequence."""
+        self.dh_pending = False
+        p, n = self._ws()
+        L.check(L.lib().tq_vegas_get_nh_split(self.ref, p, n, L.stream_handle()), "tq_vegas_get_nh_split")
+        L.count_launches(1)
+
     def finish(self, beta, slot=None):
         """finish_iteration into statistics row `slot` (if given, written to
         the control block first; otherwise the device's running slot)."""

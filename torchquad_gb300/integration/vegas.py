@@ -87,7 +87,7 @@ class _FusedPlan:
         main = torch.cuda.current_stream()
         side, fork, join = self._side, self._fork, self._join
         for i in range(5):
-            d.get_nh()
+            d.get_nh_split()
             if i > 0 and self.use_grid_improve:
                 main.wait_event(join)
             d.iterate_fused(self.family, d.params, self.use_grid_improve)
@@ -106,7 +106,7 @@ class _FusedPlan:
         return 1 + (5 * per if self.use_warmup else 0)
 
     def _block_launches(self):  # five iterations and the abort test
-        return 5 * (4 + (self.dev.update_map_launches if self.use_grid_improve else 0)) + 1
+        return 5 * (3 + (self.dev.update_map_launches if self.use_grid_improve else 0)) + 1
 
     def _capture(self):
         """Records warm-up + WHILE(block, abort test) without running it."""
