@@ -500,9 +500,11 @@ def test_split_get_nh_matches_get_nh(dtype, cuda):
         d.finish(0.75)
         out.append({n: getattr(d, n).clone() for n in _STATE_TENSORS})
     a, b = out
-    for n in ("neval", "cube_start", "counts", "rng_offset", "dh"):
+    for n in ("neval", "cube_start", "counts", "rng_offset"):
         assert torch.equal(a[n], b[n]), n
     assert torch.equal(a["stats"][:, 2], b["stats"][:, 2])
     assert int(b["control"][14].item()) == 0
+    # the cube sums are fp64 atomics (order-dependent rounding), dh follows them
     assert torch.allclose(a["jf"], b["jf"], rtol=1e-12, atol=0)
+    assert torch.allclose(a["dh"], b["dh"], rtol=1e-5 if dtype == torch.float32 else 1e-11, atol=0)
     assert torch.allclose(a["weights"], b["weights"], rtol=1e-12, atol=0)
