@@ -644,6 +644,10 @@ def run_gpu(args):
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": 1000.0 * t_max / args.steps,
+        # rank 0's per-step device times: a single stalled step (the GPU or
+        # driver held up for tens of ms) shows here rather than only in the mean
+        "step_ms": [round(x, 4) for x in step_ms],
+        "step_ms_median": statistics.median(step_ms),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
