@@ -17,6 +17,21 @@ import numpy as np
 from .grid import linspace
 
 
+
+def _sum_lr(xs):
+    t = 0.0
+    for x in xs:
+        t = t + x
+    return t
+
+
+def _ieee_div(a, b):
+    if b != 0.0 or b != b:
+        return a / b
+    if a != a or a == 0.0:
+        return math.nan
+    return math.copysign(math.inf, a) * math.copysign(1.0, b)
+
 class Map:
     """vegas_map.py:9-261."""
 
@@ -279,15 +294,19 @@ class Vegas:
         self.results, self.sigma2 = [], []
         return False
 
+    # The reference adds 0-d tensors one after another; Python's builtin sum
+    # of floats is compensated (3.12), so the sums here run left to right.
     def get_result(self):  # :318-335
         if any(s == 0.0 for s in self.sigma2):
-            return sum(self.results) / len(self.results)
-        return sum(r / s for r, s in zip(self.results, self.sigma2)) / sum(1.0 / s for s in self.sigma2)
+            return _sum_lr(self.results) / len(self.results)
+        return _sum_lr(r / s for r, s in zip(self.results, self.sigma2)) / _sum_lr(
+            1.0 / s for s in self.sigma2)
 
     def get_error(self):  # :337-346
-        res = sum(1.0 / s for s in self.sigma2 if s != 0.0)
+        res = _sum_lr(1.0 / s for s in self.sigma2 if s != 0.0)
         return self.sigma2[0] if res == 0 else 1.0 / math.sqrt(res)
 
-    def get_chisq(self):  # :348-362
+    def get_chisq(self):  # :348-362 (x / 0 gives inf or nan, as tensors do)
         I = self.get_result()
-        return sum(((r - I) ** 2 / s for r, s in zip(self.results, self.sigma2) if r != I), 0.0)
+        return _sum_lr(_ieee_div((r - I) * (r - I), s)
+                       for r, s in zip(self.results, self.sigma2) if r != I)

@@ -22,7 +22,7 @@ def _integrand(case):
 
 
 def _tol(case):
-    # spec tolerances: 1e-12 relative in fp64, 1e-6 in fp32
+    # tolerances: 1e-12 relative in fp64, 1e-6 in fp32
     return 1e-12 if case["result_dtype"] == "float64" and case["dtype"] == "float64" else (
         1e-12 if case["rule"] == "GaussLegendre" else 1e-6)
 

@@ -133,3 +133,40 @@ def test_integrand_parameter_vector_cache():
     assert f.params_numpy()[3] == 7.0
     g = tq.Oscillatory(2, a=[1.0, -1.0], b=torch.tensor(0.3, dtype=torch.float64))
     assert np.array_equal(g.params_numpy(), g.params_vector().numpy())
+
+
+def test_vegas_abort_helpers_follow_tensor_arithmetic():
+    """The abort test's sums run left to right from zero (Python's builtin
+    sum of floats is compensated since 3.12) and x / 0 gives IEEE values,
+    as the reference's 0-d tensor arithmetic does."""
+    import math
+
+    from torchquad_gb300.integration.vegas import _ieee_div, _sum_lr
+
+    xs = [1e16, 1.0, -1e16, 1.0]
+    assert _sum_lr(xs) == ((1e16 + 1.0) + -1e16) + 1.0
+    assert _ieee_div(1.0, 0.0) == math.inf and _ieee_div(-2.0, 0.0) == -math.inf
+    assert _ieee_div(1.0, -0.0) == -math.inf and math.isnan(_ieee_div(0.0, 0.0))
+    assert _ieee_div(3.0, 2.0) == 1.5
+    v = tq.VEGAS()
+    v.it, v.results, v.sigma2 = 5, [1.0, 2.0, 1.0, 1.0, 1.0], [0.0, 1.0, 1.0, 1.0, 1.0]
+    v._eps_rel = v._eps_abs = 0.0
+    v._starting_N = v._N_increment = 4000
+    v.N, v._max_iterations, v._nr_of_fevals = 10**6, 20, 20000
+    assert v._get_chisq() == math.inf  # (1 - 1.2)^2 / 0
+    assert v._check_abort_conditions() is False and v._starting_N == 8000
+
+
+def test_host_domain_values():
+    from torchquad_gb300.integration.utils import _host_domain_values
+
+    assert _host_domain_values(2, None, None) == [(-1.0, 1.0)] * 2
+    assert _host_domain_values(2, [[0, 1], [2, 3.5]], None) == [(0.0, 1.0), (2.0, 3.5)]
+    assert _host_domain_values(2, np.array([[0.0, 1.0], [2.0, 3.0]]), None) == [(0.0, 1.0), (2.0, 3.0)]
+    assert _host_domain_values(2, torch.zeros(2, 2), None) is None
+    with pytest.raises(ValueError):
+        _host_domain_values(3, [[0, 1], [0, 1]], None)
+    with pytest.raises(ValueError):
+        _host_domain_values(2, [[0, 1, 2], [0, 1]], None)
+    with pytest.raises(ValueError):
+        _host_domain_values(2, [[0, 1], [0, 1]], "jax")
