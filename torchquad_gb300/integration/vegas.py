@@ -6,9 +6,10 @@ Two drivers with the reference's algorithm and defaults:
   warm-up step and iteration is one sampling kernel (Philox draws,
   stratified points, map transform, integrand, histograms and cube sums in
   registers/shared memory) plus the small get_NH / finish / map-update
-  kernels.  The host reads results back only at the every-fifth-iteration
-  abort test (vegas.py:170), the only place the reference's control flow
-  depends on them.
+  kernels.  The every-fifth-iteration abort test (vegas.py:161-209), the
+  only place the reference's control flow depends on results, runs on the
+  device too, so a whole integration is one CUDA graph launch (a WHILE node
+  over blocks of five iterations) and one read-back.
 * materialised — any torch integrand or any ``rng`` object: points are
   written to memory, the integrand runs on them, and the same kernels do the
   map transform, histograms, cube sums and updates.
