@@ -508,3 +508,20 @@ def test_split_get_nh_matches_get_nh(dtype, cuda):
     assert torch.allclose(a["jf"], b["jf"], rtol=1e-12, atol=0)
     assert torch.allclose(a["dh"], b["dh"], rtol=1e-5 if dtype == torch.float32 else 1e-11, atol=0)
     assert torch.allclose(a["weights"], b["weights"], rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("opts", [dict(use_grid_improve=False), dict(use_warmup=False),
+                                  dict(eps_rel=1e-2), dict(eps_rel=1e-3, max_iterations=40),
+                                  dict(eps_abs=1e-4)])
+def test_fused_options_match_materialised(opts, cuda):
+    """The reference's VEGAS options through the device-side loop (fused;
+    the second call of a shape replays the captured graph) against the host
+    loop of the materialised path on the same draws."""
+    f = tq.GaussianPeak(3, a=[5.0, 8.0, 3.0], u=[0.3, 0.5, 0.7])
+    dom = torch.tensor([[0.0, 1.0], [-1.0, 1.0], [0.0, 2.0]], dtype=torch.float64, device=cuda)
+    for seed in (11, 12):
+        a, b = tq.VEGAS(), tq.VEGAS()
+        ra = a.integrate(f, 3, N=40000, integration_domain=dom, seed=seed, **opts)
+        rb = b.integrate(lambda x: f(x), 3, N=40000, integration_domain=dom, seed=seed, **opts)
+        assert (a.it, a._nr_of_fevals, a._starting_N) == (b.it, b._nr_of_fevals, b._starting_N)
+        assert abs(ra.item() - rb.item()) <= 1e-9 * abs(rb.item())
