@@ -3,9 +3,12 @@
 Follows torchquad v0.5.0 vegas_map.py (VEGASMap :9-261), vegas_stratification.py
 (VEGASStratification :7-165) and vegas.py (VEGAS :13-362) operation by
 operation in the working dtype ``dt`` (np.float32 / np.float64).  The
-scatter-adds of utils.py:61-76 are done with np.bincount, i.e. accumulated
-in fp64 and rounded to dt once, instead of sequentially in dt.  Uniform
-numbers come from an injected stream with ``uniform(size, dtype)``.
+scatter-adds of utils.py:61-76 (torch's scatter_add_ on the CPU: one add
+per point, in point order, rounded to dt each time) are np.add.at, which
+adds the same way.  Uniform numbers come from an injected stream with
+``uniform(size, dtype)``.
+
+Test infrastructure only: the library never imports this module.
 """
 from __future__ import annotations
 
@@ -18,19 +21,12 @@ from .grid import linspace
 
 
 
-def _sum_lr(xs):
-    t = 0.0
+def _sum_lr(xs, zero=0.0):
+    t = zero
     for x in xs:
         t = t + x
     return t
 
-
-def _ieee_div(a, b):
-    if b != 0.0 or b != b:
-        return a / b
-    if a != a or a == 0.0:
-        return math.nan
-    return math.copysign(math.inf, a) * math.copysign(1.0, b)
 
 class Map:
     """vegas_map.py:9-261."""
@@ -68,9 +64,9 @@ class Map:
 
     def accumulate_weight(self, y, jf2):  # :99-111
         ID = self.interval_id(y)
+        jf2 = np.asarray(jf2, dtype=self.dt)
         for i in range(self.dim):
-            self.weights[i] = (self.weights[i].astype(np.float64)
-                               + np.bincount(ID[:, i], weights=jf2.astype(np.float64), minlength=self.B)).astype(self.dt)
+            np.add.at(self.weights[i], ID[:, i], jf2)
             self.counts[i] += np.bincount(ID[:, i], minlength=self.B)
 
     @staticmethod
@@ -175,9 +171,11 @@ class Strat:
 
     def accumulate_weight(self, nevals, w):  # :46-70
         idx = np.repeat(np.arange(self.N_cubes), nevals)
-        w64 = w.astype(np.float64)
-        self.JF = np.bincount(idx, weights=w64, minlength=self.N_cubes).astype(self.dt)
-        self.JF2 = np.bincount(idx, weights=w64 * w64, minlength=self.N_cubes).astype(self.dt)
+        w = np.asarray(w, dtype=self.dt)
+        self.JF = np.zeros(self.N_cubes, dtype=self.dt)
+        self.JF2 = np.zeros(self.N_cubes, dtype=self.dt)
+        np.add.at(self.JF, idx, w)
+        np.add.at(self.JF2, idx, (w * w).astype(self.dt))
         self.strat_counts = nevals.astype(self.dt)
         return self.JF, self.JF2
 
@@ -270,23 +268,30 @@ class Vegas:
             rec.update(x_edges_new=self.map.x_edges.copy(), dh_new=self.strat.dh.copy())
             self.record.append(rec)
 
+    # The reference keeps results and variances as 0-d tensors of the
+    # working dtype: the abort test and the estimate below round every
+    # operation to dt (numpy scalars), Python scalar operands rounded to dt
+    # first; sums run left to right from zero (Python's builtin sum of
+    # floats is compensated since 3.12); x / 0 gives inf or nan.
     def check_abort(self):  # :161-209
         if self.it % 5 > 0:
             return False
-        res_abs = abs(self.get_result())
-        err = self.get_error()
-        chi2 = self.get_chisq()
-        if (err <= self.eps_rel * res_abs or err <= self.eps_abs) and chi2 / 5.0 < 1.0:
-            return True
-        if chi2 / 5.0 < 1.0:
-            if res_abs == 0.0:
+        dt = self.dt
+        with np.errstate(all="ignore"):
+            res_abs = abs(self.get_result())
+            err = self.get_error()
+            q = self.get_chisq() / dt(5.0)
+            if (err <= dt(self.eps_rel) * res_abs or err <= dt(self.eps_abs)) and q < 1.0:
+                return True
+            if q < 1.0:
+                if res_abs == 0.0:
+                    self.starting_N += self.N_increment
+                else:
+                    acc = err / res_abs
+                    x = dt(self.starting_N) * np.sqrt(acc / dt(self.eps_rel + 1e-8))
+                    self.starting_N = min(self.starting_N + self.N_increment, int(x))
+            elif q > 1.0:
                 self.starting_N += self.N_increment
-            else:
-                acc = err / res_abs
-                self.starting_N = min(self.starting_N + self.N_increment,
-                                      int(self.starting_N * math.sqrt(acc / (self.eps_rel + 1e-8))))
-        elif chi2 / 5.0 > 1.0:
-            self.starting_N += self.N_increment
         if self.fevals + self.starting_N * 5 > self.N:
             return True
         if self.it + 5 > self.max_iterations:
@@ -294,19 +299,28 @@ class Vegas:
         self.results, self.sigma2 = [], []
         return False
 
-    # The reference adds 0-d tensors one after another; Python's builtin sum
-    # of floats is compensated (3.12), so the sums here run left to right.
+    def _rows(self):
+        dt = self.dt
+        return [dt(r) for r in self.results], [dt(s) for s in self.sigma2]
+
     def get_result(self):  # :318-335
-        if any(s == 0.0 for s in self.sigma2):
-            return _sum_lr(self.results) / len(self.results)
-        return _sum_lr(r / s for r, s in zip(self.results, self.sigma2)) / _sum_lr(
-            1.0 / s for s in self.sigma2)
+        dt = self.dt
+        rs, ss = self._rows()
+        with np.errstate(all="ignore"):
+            if any(s == 0.0 for s in ss):
+                return _sum_lr(rs, dt(0)) / dt(len(rs))
+            return _sum_lr((r / s for r, s in zip(rs, ss)), dt(0)) / _sum_lr((dt(1) / s for s in ss), dt(0))
 
     def get_error(self):  # :337-346
-        res = _sum_lr(1.0 / s for s in self.sigma2 if s != 0.0)
-        return self.sigma2[0] if res == 0 else 1.0 / math.sqrt(res)
+        dt = self.dt
+        _, ss = self._rows()
+        with np.errstate(all="ignore"):
+            res = _sum_lr((dt(1) / s for s in ss if s != 0.0), dt(0))
+            return ss[0] if res == 0 else dt(1) / np.sqrt(res)
 
-    def get_chisq(self):  # :348-362 (x / 0 gives inf or nan, as tensors do)
+    def get_chisq(self):  # :348-362
+        dt = self.dt
         I = self.get_result()
-        return _sum_lr(_ieee_div((r - I) * (r - I), s)
-                       for r, s in zip(self.results, self.sigma2) if r != I)
+        rs, ss = self._rows()
+        with np.errstate(all="ignore"):
+            return _sum_lr(((r - I) * (r - I) / s for r, s in zip(rs, ss) if r != I), dt(0))

@@ -15,6 +15,12 @@ def load(name):
         return json.load(fh)
 
 
+@lru_cache(None)
+def load_npz(name):
+    with np.load(HERE / name) as z:
+        return {k: z[k] for k in z.files}
+
+
 def f(h):
     return float.fromhex(h)
 

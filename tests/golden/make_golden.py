@@ -2,7 +2,7 @@
 
 Run in a container where the reference source is present:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py /root/reference [--only grid,vegas,c2_steps,abort]
 
 The reference's hard dependencies autoray and loguru are replaced by the
 small stand-ins in ``tests/golden/refshim`` (dispatch only, no arithmetic).
@@ -286,6 +286,145 @@ def gen_vegas_c2(tq):
                 fevals=int(integ._nr_of_fevals), iterations=int(integ.it), iters=iters)
 
 
+def gen_vegas_c2_steps(tq, out_path):
+    """Step-wise reference states of the plain VEGAS run at full size (dim
+    6, N = 1e7, 50 map intervals, 6^6 cubes, fp32, normal peak sigma 0.05,
+    seed 0, Philox draws): before and after iterations 1, 2, 5 and 10.
+    Written as a compressed .npz (arrays in the reference's own dtypes)."""
+    import numpy as np
+    import torch
+    import torchquad_gb300.integrands as I
+    from torchquad.integration import vegas as V
+
+    class Map50(V.VEGASMap):
+        def __init__(self, N_intervals, dim, backend, dtype, alpha=0.5):
+            super().__init__(50, dim, backend, dtype, alpha)
+
+    f = I.GaussianPeak.normal(6, 0.5, 0.05)
+    records = []
+    orig_run = V.VEGAS._run_iteration
+
+    def run(self):
+        pre = dict(x_edges=self.map.x_edges.clone(), dx_edges=self.map.dx_edges.clone(),
+                   dh=self.strat.dh.clone(), starting_N=self._starting_N, it=self.it,
+                   rng_offset=self.rng.stream.offset)
+        snap = {}
+        orig_update = self.map.update_map
+
+        def upd():
+            snap["counts"] = self.map.counts.clone()
+            snap["weights"] = self.map.weights.clone()
+            orig_update()
+
+        self.map.update_map = upd
+        acc = orig_run(self)
+        del self.map.update_map
+        records.append(dict(pre=pre, counts=snap["counts"], weights=snap["weights"],
+                            neval=self.strat.strat_counts.to(torch.int64).clone(), JF=self.strat.JF.clone(),
+                            JF2=self.strat.JF2.clone(), result=self.results[-1].item(),
+                            sigma2=self.sigma2[-1].item(), x_edges_new=self.map.x_edges.clone(),
+                            dh_new=self.strat.dh.clone()))
+        return acc
+
+    V.VEGAS._run_iteration = run
+    orig_map = V.VEGASMap
+    V.VEGASMap = Map50
+    try:
+        integ = tq.VEGAS()
+        dom = torch.tensor([[0.0, 1.0]] * 6, dtype=torch.float32)
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            val = integ.integrate(f, 6, N=10_000_000, integration_domain=dom, rng=ReplayRNG(0))
+    finally:
+        V.VEGAS._run_iteration = orig_run
+        V.VEGASMap = orig_map
+    arrays = dict(params=f.params_vector().numpy(), value=np.float32(val.item()),
+                  n_strat=np.int64(integ.strat.N_strat), fevals=np.int64(integ._nr_of_fevals),
+                  iterations=np.int64(integ.it))
+    picks = [0, 1, 4, 9]
+    # the reference numbers iterations from 1 and counts self.it up before
+    # _run_iteration
+    arrays["steps"] = np.array([records[i]["pre"]["it"] for i in picks], dtype=np.int64)
+    for i in picks:
+        r, p = records[i], f"it{records[i]['pre']['it']}_"
+        nxt = records[i + 1]["pre"]["starting_N"] if i + 1 < len(records) else r["pre"]["starting_N"]
+        assert int(r["neval"].max()) < 65536
+        arrays.update({
+            p + "starting_N": np.int64(r["pre"]["starting_N"]),
+            p + "next_starting_N": np.int64(nxt),
+            p + "rng_offset": np.int64(r["pre"]["rng_offset"]),
+            p + "x_edges": r["pre"]["x_edges"].numpy(), p + "dx_edges": r["pre"]["dx_edges"].numpy(),
+            p + "dh": r["pre"]["dh"].numpy(),
+            p + "neval": r["neval"].numpy().astype(np.uint16),
+            p + "counts": r["counts"].numpy().astype(np.int32), p + "weights": r["weights"].numpy(),
+            p + "JF": r["JF"].numpy(), p + "JF2": r["JF2"].numpy(),
+            p + "result": np.float32(r["result"]), p + "sigma2": np.float32(r["sigma2"]),
+            p + "x_edges_new": r["x_edges_new"].numpy(), p + "dh_new": r["dh_new"].numpy(),
+        })
+    np.savez_compressed(out_path, **arrays)
+    return out_path
+
+
+def gen_vegas_abort(tq):
+    """The reference's _check_abort_conditions (vegas.py:161-209) on
+    prescribed blocks of five iteration results, with results and variances
+    as 0-d tensors of each dtype: the stop decision and the adapted
+    _starting_N (or the exception int() raises)."""
+    import numpy as np
+    import torch
+
+    rng = np.random.default_rng(5)
+    cases = []
+    for _ in range(60):
+        cases.append(dict(r=list(1.0 + 0.01 * rng.standard_normal(5)),
+                          s=list(np.abs(1e-4 * rng.standard_normal(5)) + 1e-8),
+                          eps_rel=float(rng.choice([0.0, 1e-6, 1e-2, 1.0])),
+                          eps_abs=float(rng.choice([0.0, 1e-3])), it=int(rng.choice([5, 10, 15, 20])),
+                          sN=int(rng.integers(1000, 100000)), inc=int(rng.integers(1000, 50000)),
+                          N=int(rng.choice([10**6, 10**7])), max_it=int(rng.choice([10, 20, 40]))))
+    # rounding-sensitive: results within a few fp32 ulps of each other
+    for _ in range(24):
+        base = float(rng.uniform(0.5, 2.0))
+        cases.append(dict(r=list(base * (1.0 + 3e-7 * rng.standard_normal(5))),
+                          s=list(np.abs(1e-13 * rng.standard_normal(5)) + 1e-15),
+                          eps_rel=float(rng.choice([0.0, 1e-7, 3e-7])), eps_abs=0.0, it=5,
+                          sN=int(rng.integers(1000, 10**6)), inc=int(rng.integers(1000, 10**5)),
+                          N=10**8, max_it=20))
+    base = dict(eps_rel=0.0, eps_abs=0.0, it=5, sN=4000, inc=4000, N=10**6, max_it=20)
+    cases += [
+        dict(base, r=[1.0] * 5, s=[0.0] * 5),                                      # constant integrand
+        dict(base, r=[0.0] * 5, s=[0.0] * 5),                                      # zero integrand
+        dict(base, r=[1.0, 2.0, 1.0, 1.0, 1.0], s=[0.0, 1.0, 1.0, 1.0, 1.0]),      # x / 0 in chi2
+        dict(base, r=[1.0, 1.1, 0.9, 1.0, 1.05], s=[1e-2] * 5, eps_rel=1.0),       # accuracy
+        dict(base, r=[1.0, 5.0, -3.0, 1.0, 2.0], s=[1e-6] * 5),                    # chi2 / 5 > 1
+        dict(base, r=[1.0] * 5, s=[1e-4] * 5, N=30000),                            # budget
+        dict(base, r=[1.0] * 5, s=[1e-4] * 5, it=20, max_it=20),                   # iteration limit
+        dict(base, r=[1e-30, 1.1e-30, 0.9e-30, 1e-30, 1e-30], s=[1e3] * 5),        # err / res overflows fp32
+    ]
+    out = []
+    for dtype in ("float32", "float64"):
+        dt = getattr(torch, dtype)
+        for c in cases:
+            v = tq.VEGAS()
+            v.backend, v.dtype = "torch", dt
+            v.it = c["it"]
+            v.results = [torch.tensor(x, dtype=dt) for x in c["r"]]
+            v.sigma2 = [torch.tensor(x, dtype=dt) for x in c["s"]]
+            v._eps_rel, v._eps_abs = c["eps_rel"], c["eps_abs"]
+            v._starting_N, v._N_increment, v.N = c["sN"], c["inc"], c["N"]
+            v._max_iterations = c["max_it"]
+            v._nr_of_fevals = 777 + 1000 * c["it"] * (c["it"] + 1) // 2
+            try:
+                stop = bool(v._check_abort_conditions())
+                err = None
+            except (OverflowError, ValueError) as e:
+                stop, err = None, type(e).__name__
+            out.append(dict(c, dtype=dtype, fevals=v._nr_of_fevals if err is None else 777 + 1000 * c["it"] * (c["it"] + 1) // 2,
+                            stop=stop, error=err, starting_N=v._starting_N,
+                            r=[float(x).hex() for x in c["r"]], s=[float(x).hex() for x in c["s"]]))
+    return out
+
+
 def gen_vegas_special(tq):
     """Zero and constant integrands (reference vegas_test.py:159-184) on
     the Philox draws."""
@@ -346,33 +485,47 @@ def gen_grads(tq):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    tq = _import_reference(ref_root)
+    import argparse
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("ref_root", nargs="?", default="/root/reference")
+    ap.add_argument("--only", default="", help="comma list of parts to regenerate: "
+                    "grid, vegas, c2_steps, abort (default: all)")
+    args = ap.parse_args()
+    only = set(filter(None, args.only.split(",")))
+    tq = _import_reference(args.ref_root)
     import torch
 
     torch.set_num_threads(4)
-    data = {
-        "reference_version": tq.__version__,
-        "torch": torch.__version__,
-        "grid": gen_grid(tq),
-        "multidim": gen_multidim(tq),
-        "linspace": gen_linspace(),
-        "mc": gen_mc(tq),
-        "grads": gen_grads(tq),
-    }
-    with open(HERE / "grid_mc_golden.json", "w") as fh:
-        json.dump(data, fh, indent=0)
-    print("wrote", HERE / "grid_mc_golden.json", len(data["grid"]), "grid cases")
-    vdata = {
-        "reference_version": tq.__version__,
-        "torch": torch.__version__,
-        "steps": gen_vegas_steps(tq),
-        "special": gen_vegas_special(tq),
-        "c2": gen_vegas_c2(tq),
-    }
-    with open(HERE / "vegas_golden.json", "w") as fh:
-        json.dump(vdata, fh, indent=0)
-    print("wrote", HERE / "vegas_golden.json")
+    if not only or "grid" in only:
+        data = {
+            "reference_version": tq.__version__,
+            "torch": torch.__version__,
+            "grid": gen_grid(tq),
+            "multidim": gen_multidim(tq),
+            "linspace": gen_linspace(),
+            "mc": gen_mc(tq),
+            "grads": gen_grads(tq),
+        }
+        with open(HERE / "grid_mc_golden.json", "w") as fh:
+            json.dump(data, fh, indent=0)
+        print("wrote", HERE / "grid_mc_golden.json", len(data["grid"]), "grid cases")
+    vpath = HERE / "vegas_golden.json"
+    if not only or "vegas" in only or "abort" in only:
+        vdata = json.loads(vpath.read_text()) if vpath.exists() else {}
+        vdata["reference_version"] = tq.__version__
+        vdata["torch"] = torch.__version__
+        if not only or "vegas" in only:
+            vdata["steps"] = gen_vegas_steps(tq)
+            vdata["special"] = gen_vegas_special(tq)
+            vdata["c2"] = gen_vegas_c2(tq)
+        if not only or "abort" in only:
+            vdata["abort"] = gen_vegas_abort(tq)
+        with open(vpath, "w") as fh:
+            json.dump(vdata, fh, indent=0)
+        print("wrote", vpath)
+    if not only or "c2_steps" in only:
+        print("wrote", gen_vegas_c2_steps(tq, HERE / "vegas_c2_steps.npz"))
 
 
 if __name__ == "__main__":

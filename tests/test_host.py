@@ -137,24 +137,57 @@ def test_integrand_parameter_vector_cache():
 
 def test_vegas_abort_helpers_follow_tensor_arithmetic():
     """The abort test's sums run left to right from zero (Python's builtin
-    sum of floats is compensated since 3.12) and x / 0 gives IEEE values,
-    as the reference's 0-d tensor arithmetic does."""
+    sum of floats is compensated since 3.12), x / 0 gives IEEE values and
+    the arithmetic is in the state's dtype, as the reference's 0-d tensor
+    arithmetic does."""
     import math
 
-    from torchquad_gb300.integration.vegas import _ieee_div, _sum_lr
+    from torchquad_gb300.integration.vegas import _sum_lr
 
     xs = [1e16, 1.0, -1e16, 1.0]
     assert _sum_lr(xs) == ((1e16 + 1.0) + -1e16) + 1.0
-    assert _ieee_div(1.0, 0.0) == math.inf and _ieee_div(-2.0, 0.0) == -math.inf
-    assert _ieee_div(1.0, -0.0) == -math.inf and math.isnan(_ieee_div(0.0, 0.0))
-    assert _ieee_div(3.0, 2.0) == 1.5
+    for dtype in (torch.float64, torch.float32):
+        v = tq.VEGAS()
+        v.dtype = dtype
+        v.it, v.results, v.sigma2 = 5, [1.0, 2.0, 1.0, 1.0, 1.0], [0.0, 1.0, 1.0, 1.0, 1.0]
+        v._eps_rel = v._eps_abs = 0.0
+        v._starting_N = v._N_increment = 4000
+        v.N, v._max_iterations, v._nr_of_fevals = 10**6, 20, 20000
+        assert v._get_chisq() == math.inf  # (1 - 1.2)^2 / 0
+        assert v._check_abort_conditions() is False and v._starting_N == 8000
+    # fp32 state: the estimate is rounded per operation in fp32
     v = tq.VEGAS()
-    v.it, v.results, v.sigma2 = 5, [1.0, 2.0, 1.0, 1.0, 1.0], [0.0, 1.0, 1.0, 1.0, 1.0]
-    v._eps_rel = v._eps_abs = 0.0
-    v._starting_N = v._N_increment = 4000
-    v.N, v._max_iterations, v._nr_of_fevals = 10**6, 20, 20000
-    assert v._get_chisq() == math.inf  # (1 - 1.2)^2 / 0
-    assert v._check_abort_conditions() is False and v._starting_N == 8000
+    v.dtype = torch.float32
+    v.results, v.sigma2 = [1.0 + 2**-20, 1.0, 1.0, 1.0, 1.0], [3.0] * 5
+    want = np.float32(0)
+    for r in v.results:
+        want = want + np.float32(r) / np.float32(3.0)
+    den = np.float32(0)
+    for _ in range(5):
+        den = den + np.float32(1) / np.float32(3.0)
+    assert v._get_result() == want / den and isinstance(v._get_result(), np.float32)
+
+
+def test_vegas_abort_test_matches_reference_golden():
+    """The host abort test (used by the materialised path and after the
+    fused runs for the estimate) against the reference's
+    _check_abort_conditions on fp32 and fp64 tensors: decision, adapted
+    _starting_N and the exception int() raises for a non-finite value."""
+    from tests import golden as G
+
+    for c in G.load("vegas_golden.json")["abort"]:
+        v = tq.VEGAS()
+        v.dtype = torch.float32 if c["dtype"] == "float32" else torch.float64
+        v.it, v.results, v.sigma2 = c["it"], G.arr(c["r"]).tolist(), G.arr(c["s"]).tolist()
+        v._eps_rel, v._eps_abs = c["eps_rel"], c["eps_abs"]
+        v._starting_N, v._N_increment, v.N = c["sN"], c["inc"], c["N"]
+        v._max_iterations, v._nr_of_fevals = c["max_it"], c["fevals"]
+        if c["error"]:
+            with pytest.raises({"OverflowError": OverflowError, "ValueError": ValueError}[c["error"]]):
+                v._check_abort_conditions()
+            continue
+        assert v._check_abort_conditions() == c["stop"], c
+        assert v._starting_N == c["starting_N"], c
 
 
 def test_host_domain_values():

@@ -152,8 +152,117 @@ def test_materialised_iteration_matches_reference_state(case, cuda):
         _check_step(case, st, dev, dtype, cuda, dev.weights.clone())
 
 
+C2 = G.load_npz("vegas_c2_steps.npz")
+F32 = torch.float32
+
+
+def _c2_device(cuda):
+    dom = torch.tensor([[0.0, 1.0]] * 6, dtype=F32, device=cuda)
+    return VegasDevice(6, F32, 50, int(C2["n_strat"]), cuda, dom, stats_slots=32)
+
+
+def _c2(name, cuda, dtype=F32):
+    return torch.from_numpy(np.ascontiguousarray(C2[name])).to(device=cuda, dtype=dtype)
+
+
+def _floor_nh(dh, n):
+    """get_NH (vegas_stratification.py:92-103) in fp32 on the host."""
+    return np.clip(np.floor((np.asarray(dh, dtype=np.float32) * np.float32(n)).astype(np.float32)), 2, None)
+
+
+@pytest.mark.parametrize("it", [int(i) for i in C2["steps"]])
+def test_plain_vegas_full_size_step_matches_reference(it, cuda):
+    """The plain VEGAS configuration at full size (dim 6, N = 1e7, 50
+    intervals, 6^6 = 46656 cubes, fp32, normal peak sigma 0.05, seed 0),
+    one iteration from the reference's recorded state before iteration `it`
+    on the same Philox draws: evaluations per cube and interval counts bit
+    for bit; cube sums, interval weights, the estimate and the new map to
+    fp32 rounding; and the next get_NH (floor(dh * N) per cube, the only
+    place the next iteration depends on them) exactly."""
+    p = f"it{it}_"
+    f = tq.GaussianPeak.normal(6, 0.5, 0.05)
+    assert np.array_equal(f.params_vector().numpy(), C2["params"])
+    params = f.device_params(cuda)
+    dev = _c2_device(cuda)
+    dev.x_edges.copy_(_c2(p + "x_edges", cuda))
+    dev.dx_edges.copy_(_c2(p + "dx_edges", cuda))
+    dev.dh.copy_(_c2(p + "dh", cuda))
+    dev.rng_offset.fill_(int(C2[p + "rng_offset"]))
+    dev.get_nh(int(C2[p + "starting_N"]), normalize=False)
+    neval = C2[p + "neval"].astype(np.int64)
+    assert np.array_equal(dev.neval.cpu().numpy(), neval)  # bit-exact
+    M = int(neval.sum())
+    dev.set_control(L.TQ_VC_SEED | L.TQ_VC_STREAM, seed=0, sid=0)
+    dev.iterate_fused(f.family, params, True, M)
+    assert np.array_equal(dev.counts.cpu().numpy(), C2[p + "counts"])  # bit-exact
+    assert torch.allclose(dev.weights, _c2(p + "weights", cuda, torch.float64), rtol=2e-5, atol=0)
+    assert torch.allclose(dev.jf, _c2(p + "JF", cuda, torch.float64), rtol=2e-5, atol=1e-35)
+    assert torch.allclose(dev.jf2, _c2(p + "JF2", cuda, torch.float64), rtol=2e-5, atol=1e-35)
+    assert int(dev.rng_offset.item()) == int(C2[p + "rng_offset"]) + tq.RNG.blocks_for(6 * M, F32)
+    dev.finish(0.75, 0)
+    stats = dev.stats[0].cpu()
+    assert abs(float(stats[0]) - float(C2[p + "result"])) <= 2e-5 * abs(float(C2[p + "result"]))
+    assert abs(float(stats[1]) - float(C2[p + "sigma2"])) <= 1e-3 * abs(float(C2[p + "sigma2"]))
+    assert int(stats[2]) == M
+    dev.update_map(0.5)
+    assert float((dev.x_edges - _c2(p + "x_edges_new", cuda)).abs().max()) <= 1e-6
+    n = int(C2[p + "next_starting_N"])
+    dev.get_nh(n, normalize=True)  # normalises dh as update_DH does
+    want = C2[p + "dh_new"]
+    got = dev.dh.cpu().numpy()
+    assert np.max(np.abs(got - want)) <= 5e-5 * np.max(want)
+    nh_ref = _floor_nh(want, n)
+    assert np.array_equal(dev.neval.cpu().numpy(), nh_ref)  # the next iteration's counts, exactly
+    assert np.array_equal(_floor_nh(got, n), nh_ref)
+    nxt = [int(i) for i in C2["steps"]]
+    if it + 1 in nxt:  # the reference's next iteration used exactly these counts
+        assert np.array_equal(nh_ref, C2[f"it{it + 1}_neval"])
+
+
+def test_plain_vegas_full_size_trajectory(cuda):
+    """The GPU's own run of the plain VEGAS configuration against the
+    reference's (both from seed 0 on the same Philox stream): after the
+    warm-up the map agrees to a few fp32 ulps and the RNG offset exactly;
+    iteration 1 has the same evaluations per cube.  Iteration 2's counts come
+    from floor(dh * N) of sums over maps that differ in the last bits (the
+    reference adds interval weights one point at a time in fp32, the kernels
+    per warp in fp32 and across CTAs in fp64), so a cube whose dh * N lies
+    within rounding of an integer can flip by one there; this test lists
+    those flips and requires each to be such a near-tie.  After a flip the
+    points move to other draws and the runs agree statistically
+    (test_plain_vegas_full_size_matches_reference)."""
+    f = tq.GaussianPeak.normal(6, 0.5, 0.05)
+    params = f.device_params(cuda)
+    dev = _c2_device(cuda)
+    dev.set_control(L.TQ_VC_SEED | L.TQ_VC_STREAM, seed=0, sid=0)
+    dev.rng_offset.fill_(0)
+    for _ in range(5):
+        dev.warmup_fused(f.family, params, 80000)
+        dev.update_map(0.5)
+    assert float((dev.x_edges - _c2("it1_x_edges", cuda)).abs().max()) <= 1e-6
+    assert int(dev.rng_offset.item()) == int(C2["it1_rng_offset"])
+    dev.get_nh(400000, normalize=False)
+    assert np.array_equal(dev.neval.cpu().numpy(), C2["it1_neval"].astype(np.int64))
+    dev.iterate_fused(f.family, params, True)
+    assert np.array_equal(dev.counts.cpu().numpy(), C2["it1_counts"])
+    dev.finish(0.75, 0)
+    dev.update_map(0.5)
+    dev.get_nh(400000, normalize=True)
+    got = dev.neval.cpu().numpy()
+    want_dh = C2["it2_dh"].astype(np.float64)
+    flips = np.nonzero(got != C2["it2_neval"].astype(np.int64))[0]
+    assert float(np.max(np.abs(dev.dh.cpu().numpy() - want_dh))) <= 5e-5 * float(want_dh.max())
+    assert len(flips) <= 8, len(flips)
+    for c in flips:
+        x = want_dh[c] * 400000.0
+        assert abs(got[c] - C2["it2_neval"][c]) == 1 and abs(x - round(x)) < 1e-2, (c, x, got[c])
+
+
 def test_plain_vegas_full_size_matches_reference(cuda):
-    """dim 6, N = 1e7, 50 intervals, fp32 normal peak, seed 0."""
+    """dim 6, N = 1e7, 50 intervals, fp32 normal peak, seed 0: the whole
+    integration through the public API (graph-captured device loop) against
+    the reference's run.  The first iteration is identical; the step-wise
+    parity and the trajectory tests above pin the rest."""
     c = VG["c2"]
     f = tq.GaussianPeak.normal(6, 0.5, c["sigma"])
     v = tq.VEGAS()
@@ -163,9 +272,9 @@ def test_plain_vegas_full_size_matches_reference(cuda):
     assert v.it == c["iterations"]
     Ms = [int(m) for m in v._dev.stats[: v.it, 2].cpu()]
     ref_Ms = [it["M"] for it in c["iters"]]
-    # the first iteration starts from identical state: identical cube counts
     assert Ms[0] == ref_Ms[0]
-    assert abs(v._nr_of_fevals - c["fevals"]) <= 2000
+    # after the first floor flip the counts follow other draws: same budget rule
+    assert v._nr_of_fevals <= c["N"] and abs(v._nr_of_fevals - c["fevals"]) <= 0.001 * c["fevals"]
     want = G.f(c["value"])
     assert abs(r.item() - want) <= 5 * v._get_error() + 1e-6
     assert abs(r.item() - 1.0) < 5e-3
@@ -374,61 +483,39 @@ def test_default_interval_count_vegas(cuda):
     assert abs(r.item() - 1.0) < 5 * v._get_error() + 1e-3
 
 
-def _abort_cases():
-    rng = np.random.default_rng(5)
-    cases = []
-    for k in range(60):
-        r = list(1.0 + 0.01 * rng.standard_normal(5))
-        s = list(np.abs(1e-4 * rng.standard_normal(5)) + 1e-8)
-        cases.append(dict(r=r, s=s, eps_rel=float(rng.choice([0.0, 1e-6, 1e-2, 1.0])),
-                          eps_abs=float(rng.choice([0.0, 1e-3])), it=int(rng.choice([5, 10, 15, 20])),
-                          sN=int(rng.integers(1000, 100000)), inc=int(rng.integers(1000, 50000)),
-                          N=int(rng.choice([10**6, 10**7])), max_it=int(rng.choice([10, 20, 40]))))
-    base = dict(eps_rel=0.0, eps_abs=0.0, it=5, sN=4000, inc=4000, N=10**6, max_it=20)
-    cases += [
-        dict(base, r=[1.0] * 5, s=[0.0] * 5),                          # constant integrand
-        dict(base, r=[0.0] * 5, s=[0.0] * 5),                          # zero integrand
-        dict(base, r=[1.0, 2.0, 1.0, 1.0, 1.0], s=[0.0, 1.0, 1.0, 1.0, 1.0]),  # x / 0 in chi2
-        dict(base, r=[1.0, 1.1, 0.9, 1.0, 1.05], s=[1e-2] * 5, eps_rel=1.0),    # accuracy
-        dict(base, r=[1.0, 5.0, -3.0, 1.0, 2.0], s=[1e-6] * 5),        # chi2 / 5 > 1
-        dict(base, r=[1.0] * 5, s=[1e-4] * 5, N=30000),                # budget
-        dict(base, r=[1.0] * 5, s=[1e-4] * 5, it=20, max_it=20),       # iteration limit
-    ]
-    return cases
-
-
-def test_device_abort_test_matches_host_logic(cuda):
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_device_abort_test_matches_reference(dtype, cuda):
     """tq_vegas_abort_test (the every-fifth-iteration test on the device)
-    takes the host _check_abort_conditions' decision and adapted
-    _starting_N, including zero variances and x / 0."""
-    d = VegasDevice(2, torch.float64, 4, 2, cuda, stats_slots=64)
+    against the reference's _check_abort_conditions on tensors of the
+    state's dtype (golden): decision, adapted _starting_N, zero variances,
+    x / 0, and the non-finite int() for which the reference raises (stop
+    codes 5 / 6)."""
+    d = VegasDevice(2, DT[dtype], 4, 2, cuda, stats_slots=64)
     zeros = np.zeros(6)
-    for case in _abort_cases():
+    cases = [c for c in VG["abort"] if c["dtype"] == dtype]
+    assert len(cases) >= 90
+    for case in cases:
         it, warm = case["it"], 777
         pts = np.arange(1, it + 1) * 1000
         d.begin_run(case["sN"], case["N"], case["inc"], case["max_it"], warm, case["eps_rel"],
                     case["eps_abs"], 0, 0, 0, zeros)
         st = torch.zeros((it, 4), dtype=torch.float64)
         st[:, 2] = torch.tensor(pts, dtype=torch.float64)
-        st[it - 5:, 0] = torch.tensor(case["r"], dtype=torch.float64)
-        st[it - 5:, 1] = torch.tensor(case["s"], dtype=torch.float64)
+        st[it - 5:, 0] = torch.tensor(G.arr(case["r"]), dtype=torch.float64)
+        st[it - 5:, 1] = torch.tensor(G.arr(case["s"]), dtype=torch.float64)
         d.stats[:it] = st.to(cuda)
         d.control[1] = it
         d.control[11] = it - 5
         d.abort_test(0)
         d.read_back()
-        v = tq.VEGAS()
-        v.it, v.results, v.sigma2 = it, list(case["r"]), list(case["s"])
-        v._eps_rel, v._eps_abs = case["eps_rel"], case["eps_abs"]
-        v._starting_N, v._N_increment, v.N = case["sN"], case["inc"], case["N"]
-        v._max_iterations = case["max_it"]
-        v._nr_of_fevals = warm + int(pts.sum())
-        stop = v._check_abort_conditions()
         c = d.host_control
-        assert int(c[L.VC_EVALS]) == v._nr_of_fevals
+        assert int(c[L.VC_EVALS]) == case["fevals"] == warm + int(pts.sum())
         assert int(c[L.VC_IT]) == it
-        assert bool(c[L.VC_STOP]) == stop, case
-        assert int(c[L.VC_NEVALS]) == v._starting_N, case
+        if case["error"]:
+            assert int(c[L.VC_STOP]) == {"OverflowError": 5, "ValueError": 6}[case["error"]], case
+            continue
+        assert bool(c[L.VC_STOP]) == case["stop"], case
+        assert int(c[L.VC_NEVALS]) == case["starting_N"], case
 
 
 def test_fused_graph_and_eager_runs_agree(cuda):
@@ -525,3 +612,27 @@ def test_fused_options_match_materialised(opts, cuda):
         rb = b.integrate(lambda x: f(x), 3, N=40000, integration_domain=dom, seed=seed, **opts)
         assert (a.it, a._nr_of_fevals, a._starting_N) == (b.it, b._nr_of_fevals, b._starting_N)
         assert abs(ra.item() - rb.item()) <= 1e-9 * abs(rb.item())
+
+
+def test_integrators_keep_their_own_state(cuda):
+    """Integrators of the same shape share one device plan; each keeps its
+    own map and stratification afterwards (as the reference's instances
+    own theirs), whether it reads them before or after the next run."""
+    f = tq.GaussianPeak.normal(3, 0.5, 0.1)
+    dom = torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float32, device=cuda)
+    a, b, c = tq.VEGAS(), tq.VEGAS(), tq.VEGAS()
+    ra = a.integrate(f, 3, N=200_000, integration_domain=dom, seed=1)
+    xa, dha = a.map.x_edges.clone(), a.strat.dh.clone()
+    rb = b.integrate(f, 3, N=200_000, integration_domain=dom, seed=2)
+    xb, dhb = b.map.x_edges.clone(), b.strat.dh.clone()
+    assert not torch.equal(xa, xb) and ra.item() != rb.item()
+    c.integrate(f, 3, N=200_000, integration_domain=dom, seed=3)
+    assert torch.equal(a.map.x_edges, xa) and torch.equal(a.strat.dh, dha)
+    assert torch.equal(b.map.x_edges, xb) and torch.equal(b.strat.dh, dhb)
+    # d (b's seed) reads its dh only after the next run: still its own,
+    # normalised once (equal to b's up to the order of fp64 atomic adds)
+    d = tq.VEGAS()
+    d.integrate(f, 3, N=200_000, integration_domain=dom, seed=2)
+    a.integrate(f, 3, N=200_000, integration_domain=dom, seed=5)
+    assert torch.allclose(d.map.x_edges, xb, rtol=0, atol=1e-6)
+    assert torch.allclose(d.strat.dh, dhb, rtol=1e-5, atol=0)

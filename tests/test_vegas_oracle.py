@@ -95,6 +95,44 @@ def test_oracle_steps_match_reference(case):
         assert np.max(np.abs(s.dh - want)) <= tol * np.max(want)
 
 
+C2 = G.load_npz("vegas_c2_steps.npz")
+
+
+@pytest.mark.parametrize("it", [int(i) for i in C2["steps"]])
+def test_oracle_c2_steps_match_reference(it):
+    """The plain VEGAS configuration at full size (dim 6, 50 intervals, 6^6
+    cubes, fp32, seed 0): the oracle given the reference's state before
+    iteration `it` reproduces its evaluations per cube and interval counts
+    bit for bit, its sums to fp32 rounding, and the next iteration's
+    evaluations per cube exactly."""
+    dt, p = np.float32, f"it{it}_"
+    fn = lambda x: OI.evaluate(2, C2["params"], x).astype(dt)  # noqa: E731
+    m = OV.Map(50, 6, dt)
+    m.x_edges, m.dx_edges = C2[p + "x_edges"].copy(), C2[p + "dx_edges"].copy()
+    s = OV.Strat(400000, 6, dt)
+    s.dh = C2[p + "dh"].copy()
+    neval = s.get_NH(int(C2[p + "starting_N"]))
+    assert np.array_equal(neval, C2[p + "neval"].astype(np.int64))  # bit-exact
+    M = int(neval.sum())
+    u = OP.ReplayStream(0, 0, int(C2[p + "rng_offset"])).uniform([M, 6], dt)
+    y = s.get_Y(neval, u)
+    jf = (fn(m.get_X(y)) * m.get_Jac(y)).astype(dt)
+    m.accumulate_weight(y, (jf * jf).astype(dt))
+    assert np.array_equal(m.counts, C2[p + "counts"])  # bit-exact
+    assert np.allclose(m.weights, C2[p + "weights"], rtol=2e-6, atol=0)
+    JF, JF2 = s.accumulate_weight(neval, jf)
+    assert np.allclose(JF, C2[p + "JF"], rtol=2e-6, atol=1e-35)
+    assert np.allclose(JF2, C2[p + "JF2"], rtol=2e-6, atol=1e-35)
+    m.update_map()
+    s.update_DH()
+    assert np.max(np.abs(m.x_edges - C2[p + "x_edges_new"])) <= 1e-6
+    want = C2[p + "dh_new"]
+    assert np.max(np.abs(s.dh - want)) <= 5e-5 * np.max(want)
+    n = int(C2[p + "next_starting_N"])  # get_NH of the next iteration (vegas_stratification.py:92-103)
+    nh = np.clip(np.floor((s.dh * dt(n)).astype(dt)), 2, None)
+    assert np.array_equal(nh, np.clip(np.floor((want * dt(n)).astype(dt)), 2, None))
+
+
 def test_oracle_c2_end_to_end_statistically():
     c = VG["c2"]
     params = G.arr(c["params"])
@@ -106,3 +144,27 @@ def test_oracle_c2_end_to_end_statistically():
     assert abs(v.fevals - c["fevals"]) <= 2000
     assert abs(got - want) <= 5 * v.get_error() + 1e-6
     assert abs(got - 1.0) < 5e-3
+
+
+def _abort_vegas(c):
+    v = OV.Vegas()
+    v.dt = np.float32 if c["dtype"] == "float32" else np.float64
+    v.it, v.results, v.sigma2 = c["it"], G.arr(c["r"]).tolist(), G.arr(c["s"]).tolist()
+    v.eps_rel, v.eps_abs = c["eps_rel"], c["eps_abs"]
+    v.starting_N, v.N_increment, v.N, v.max_iterations = c["sN"], c["inc"], c["N"], c["max_it"]
+    v.fevals = c["fevals"]
+    return v
+
+
+def test_oracle_abort_test_matches_reference():
+    """_check_abort_conditions (vegas.py:161-209) on blocks of five results
+    held as fp32 and fp64 tensors in the reference: same decision, same
+    adapted _starting_N, same exception from int()."""
+    for c in VG["abort"]:
+        v = _abort_vegas(c)
+        if c["error"]:
+            with pytest.raises({"OverflowError": OverflowError, "ValueError": ValueError}[c["error"]]):
+                v.check_abort()
+            continue
+        assert v.check_abort() == c["stop"], c
+        assert v.starting_N == c["starting_N"], c

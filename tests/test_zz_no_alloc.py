@@ -5,31 +5,50 @@ a plugin whose host application owns every device allocation, code that
 must not allocate once it runs, or a C caller without an allocator.  Its
 scratch is a static device array shared by every call, so this file is
 collected last and checks, through the C ABI, that two calls in a row give
-the same result as the workspace-taking entry point (tq_grid_fused), within
-the tolerances of the grid-rule parity tests.  It passes alone in a fresh
+the same result as the workspace-taking entry point (tq_grid_fused) and as
+the unmodified reference (its recorded golden values), within the
+tolerances of the grid-rule parity tests.  It passes alone in a fresh
 process (the first call does the per-device set-up) and after the others.
 """
 import pytest
 import torch
 
+from tests import golden as G
 from torchquad_gb300 import _lib as L
 
-pytestmark = pytest.mark.gpu
-
 CASES = [
-    # rule, dtype, dim, n, family, params (c, b, a[dim], u[dim]), domain, rel. tolerance
+    # rule, dtype, dim, n, family, params (c, b, a[dim], u[dim]), domain, rel. tolerance,
+    # name of the reference's recorded value for the same integral (or None)
     (L.TQ_RULE_SIMPSON, torch.float64, 3, 101, L.TQ_FN_EXP_SUM, [1.0, 0.0] + [1.0] * 3 + [0.0] * 3,
-     [[0.0, 1.0]] * 3, 1e-12),
+     [[0.0, 1.0]] * 3, 1e-12, "C1-Simpson-expsum3-101"),
     (L.TQ_RULE_GAUSS, torch.float64, 4, 32, L.TQ_FN_OSCILLATORY,
-     [1.0, 0.37, 1.2, -2.1, 0.7, 2.6] + [0.0] * 4, [[0.0, 1.0]] * 4, 1e-12),
+     [1.0, 0.37, 1.2, -2.1, 0.7, 2.6] + [0.0] * 4, [[0.0, 1.0]] * 4, 1e-12, "C4-GaussLegendre-osc4-32"),
     (L.TQ_RULE_BOOLE, torch.float32, 2, 401, L.TQ_FN_GAUSSIAN, [1.5, 0.0, 2.0, 3.0, 0.3, 0.6],
-     [[-1.0, 1.0], [0.0, 2.0]], 1e-6),
+     [[-1.0, 1.0], [0.0, 2.0]], 1e-6, None),
 ]
 
 
+def _reference_value(name):
+    if name is None:
+        return None
+    (case,) = [c for c in G.load("grid_mc_golden.json")["grid"] if c["name"] == name]
+    return G.f(case["value"])
+
+
+def test_scratch_status_string():
+    # the rejection of a launch larger than the static scratch has its own
+    # status and message (no GPU needed)
+    L.load()
+    assert L.TQ_ERR_SCRATCH == -10
+    msg = L.status_string(L.TQ_ERR_SCRATCH)
+    assert msg != "unknown status" and "scratch" in msg
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("case", CASES, ids=["simpson-f64", "gauss-f64", "boole-f32"])
 def test_noalloc_matches_workspace_entry_point_twice(case, cuda):
-    rule, dtype, dim, n, fam, params, dom, tol = case
+    rule, dtype, dim, n, fam, params, dom, tol, golden = case
+    want = _reference_value(golden)
     lib = L.load()
     stream = torch.cuda.current_stream().cuda_stream
     d = torch.tensor(dom, dtype=dtype, device=cuda)
@@ -59,3 +78,5 @@ def test_noalloc_matches_workspace_entry_point_twice(case, cuda):
         torch.cuda.synchronize()
         a, b = out.item(), ref.item()
         assert abs(a - b) <= tol * max(1.0, abs(b)), (a, b)
+        if want is not None:  # the reference's own value for this integral
+            assert abs(a - want) <= tol * abs(want), (a, want)

@@ -820,16 +820,11 @@ inline size_t map_row_smem(int64_t B, size_t ts) {
   return (((7 * B + 3) * ts + (2 * B + 1) * 4 + 2 * B) + 15) & ~size_t(15);
 }
 
-// The last CTA to arrive (all others have finished reading the weights)
-// resets the weights and counts of the whole map (_reset_weight).  It reads
-// nothing the other CTAs wrote, and their reads of the weights were consumed
-// before they took their tickets, so the ticket needs no fence.
+// The last CTA to arrive resets the weights and counts of the whole map
+// (_reset_weight).  Every CTA read the whole map's weights and counts; the
+// fenced ticket (last_block_of) orders those reads before the reset.
 __device__ void clear_map_by_last(const tq_vegas_state& st, unsigned* ticket, unsigned nrows) {
-  __shared__ bool is_last;
-  __syncthreads();
-  if (threadIdx.x == 0) is_last = atomicAdd(ticket, 1u) == nrows - 1;
-  __syncthreads();
-  if (is_last) {
+  if (last_block_of(ticket, nrows)) {
     const int64_t n = (int64_t)st.dim * st.n_bins;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
       st.weights[i] = 0.0;

@@ -64,26 +64,44 @@ __global__ void vegas_begin_run_kernel(RunArgs a) {
   }
 }
 
-// IEEE quotient (x / 0 is +-inf or NaN, as the reference's tensor arithmetic
-// gives); written out so the compiler's fast paths cannot change it.
-__device__ __forceinline__ double qdiv(double x, double y) { return __ddiv_rn(x, y); }
+// Arithmetic of the abort test in the state's dtype, each operation rounded
+// once to nearest (the reference does it on 0-d tensors of that dtype); the
+// quotients give IEEE results for x / 0 (+-inf or NaN), as tensors do.
+__device__ __forceinline__ float a_add(float x, float y) { return __fadd_rn(x, y); }
+__device__ __forceinline__ double a_add(double x, double y) { return __dadd_rn(x, y); }
+__device__ __forceinline__ float a_sub(float x, float y) { return __fsub_rn(x, y); }
+__device__ __forceinline__ double a_sub(double x, double y) { return __dsub_rn(x, y); }
+__device__ __forceinline__ float a_mul(float x, float y) { return __fmul_rn(x, y); }
+__device__ __forceinline__ double a_mul(double x, double y) { return __dmul_rn(x, y); }
+__device__ __forceinline__ float a_div(float x, float y) { return __fdiv_rn(x, y); }
+__device__ __forceinline__ double a_div(double x, double y) { return __ddiv_rn(x, y); }
+__device__ __forceinline__ float a_sqrt(float x) { return __fsqrt_rn(x); }
+__device__ __forceinline__ double a_sqrt(double x) { return __dsqrt_rn(x); }
+__device__ __forceinline__ float a_cast(double x, float) { return __double2float_rn(x); }
+__device__ __forceinline__ double a_cast(double x, double) { return x; }
 
 // _check_abort_conditions for the block that just ended, in the host code's
-// operation order (every sum left to right from zero), on one warp: lane i
-// < 5 holds result r_i and variance s_i of the block's i-th iteration.  The
-// quotients of the rows are taken by their own lanes at once (the same
-// operations as one thread would do); the sums and the decision are taken
-// by every lane alike.  Returns the stop reason (0: go on) and updates *sN
-// (VEGAS._starting_N).
-__device__ int abort_decision_warp(double r_mine, double s_mine, int64_t it, int64_t evals,
-                                   int64_t N, int64_t n_inc, int64_t max_it, double eps_rel,
-                                   double eps_abs, int64_t* sN) {
+// operation order (every sum left to right from zero), on one warp, in the
+// state's dtype T: lane i < 5 holds result r_i and variance s_i of the
+// block's i-th iteration.  The quotients of the rows are taken by their own
+// lanes at once (the same operations as one thread would do); the sums and
+// the decision are taken by every lane alike.  Python scalars meet the
+// tensors as T (eps_rel, eps_abs, eps_rel + 1e-8, 5.0 and _starting_N are
+// rounded to T first, as torch does with a scalar operand).  Returns the
+// stop reason (0: go on; 5 / 6: int() of an infinite / NaN value, where the
+// reference raises) and updates *sN (VEGAS._starting_N).
+template <typename T>
+__device__ int abort_decision_warp(double r_in, double s_in, int64_t it, int64_t evals, int64_t N,
+                                   int64_t n_inc, int64_t max_it, double eps_rel_d,
+                                   double eps_abs_d, int64_t* sN) {
   const int lane = threadIdx.x & 31;
   const bool row = lane < 5;
-  const unsigned zeros = __ballot_sync(0xffffffffu, row && s_mine == 0.0);
-  const double q_mine = row ? qdiv(r_mine, s_mine) : 0.0;    // r_i / s_i
-  const double inv_mine = row ? qdiv(1.0, s_mine) : 0.0;     // 1 / s_i
-  double r[5], s[5], q[5], inv[5];
+  const T zero = (T)0, one = (T)1, five = (T)5;
+  const T r_mine = a_cast(r_in, zero), s_mine = a_cast(s_in, zero);
+  const unsigned zeros = __ballot_sync(0xffffffffu, row && s_mine == zero);
+  const T q_mine = row ? a_div(r_mine, s_mine) : zero;  // r_i / s_i
+  const T inv_mine = row ? a_div(one, s_mine) : zero;   // 1 / s_i
+  T r[5], s[5], q[5], inv[5];
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
     r[i] = __shfl_sync(0xffffffffu, r_mine, i);
@@ -92,53 +110,56 @@ __device__ int abort_decision_warp(double r_mine, double s_mine, int64_t it, int
     inv[i] = __shfl_sync(0xffffffffu, inv_mine, i);
   }
   // _get_result (EQ 30)
-  double res;
+  T res;
   if (zeros) {
-    double t = 0.0;
-    for (int i = 0; i < 5; ++i) t = __dadd_rn(t, r[i]);
-    res = qdiv(t, 5.0);
+    T t = zero;
+    for (int i = 0; i < 5; ++i) t = a_add(t, r[i]);
+    res = a_div(t, five);
   } else {
-    double num = 0.0, den = 0.0;
+    T num = zero, den = zero;
     for (int i = 0; i < 5; ++i) {
-      num = __dadd_rn(num, q[i]);
-      den = __dadd_rn(den, inv[i]);
+      num = a_add(num, q[i]);
+      den = a_add(den, inv[i]);
     }
-    res = qdiv(num, den);
+    res = a_div(num, den);
   }
-  const double res_abs = fabs(res);
+  const T res_abs = res < zero ? -res : res;
   // _get_error (EQ 31)
-  double isum = 0.0;
+  T isum = zero;
   for (int i = 0; i < 5; ++i)
-    if (s[i] != 0.0) isum = __dadd_rn(isum, inv[i]);
-  const double err = isum == 0.0 ? s[0] : qdiv(1.0, __dsqrt_rn(isum));
+    if (s[i] != zero) isum = a_add(isum, inv[i]);
+  const T err = isum == zero ? s[0] : a_div(one, a_sqrt(isum));
   // _get_chisq (EQ 32): each row's term on its lane, summed in row order
   const bool use = row && r_mine != res;
-  double term = 0.0;
+  T term = zero;
   if (use) {
-    const double d = __dsub_rn(r_mine, res);
-    term = qdiv(__dmul_rn(d, d), s_mine);
+    const T d = a_sub(r_mine, res);
+    term = a_div(a_mul(d, d), s_mine);
   }
   const unsigned used = __ballot_sync(0xffffffffu, use);
-  double chi2 = 0.0;
+  T chi2 = zero;
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
-    const double t = __shfl_sync(0xffffffffu, term, i);
-    if (used >> i & 1u) chi2 = __dadd_rn(chi2, t);
+    const T t = __shfl_sync(0xffffffffu, term, i);
+    if (used >> i & 1u) chi2 = a_add(chi2, t);
   }
-  const double qc = qdiv(chi2, 5.0);
-  if ((err <= __dmul_rn(eps_rel, res_abs) || err <= eps_abs) && qc < 1.0) return 1;
-  if (qc < 1.0) {
-    if (res_abs == 0.0) {
+  const T eps_rel = a_cast(eps_rel_d, zero), eps_abs = a_cast(eps_abs_d, zero);
+  const T qc = a_div(chi2, five);
+  if ((err <= a_mul(eps_rel, res_abs) || err <= eps_abs) && qc < one) return 1;
+  if (qc < one) {
+    if (res_abs == zero) {
       *sN += n_inc;
     } else {
-      const double acc = qdiv(err, res_abs);
-      const double x = __dmul_rn((double)*sN, __dsqrt_rn(qdiv(acc, __dadd_rn(eps_rel, 1e-8))));
-      // int(): truncation toward zero (saturating on the device where the
-      // host would raise for an infinite value)
-      const int64_t t = __double2ll_rz(x);
+      const T acc = a_div(err, res_abs);
+      const T x = a_mul(a_cast((double)*sN, zero), a_sqrt(a_div(acc, a_cast(eps_rel_d + 1e-8, zero))));
+      // int(): truncation toward zero; the reference raises for a value
+      // that is not finite
+      if (isnan(x)) return 6;
+      if (isinf(x)) return 5;
+      const int64_t t = __double2ll_rz((double)x);
       *sN = min(*sN + n_inc, t);
     }
-  } else if (qc > 1.0) {
+  } else if (qc > one) {
     *sN += n_inc;
   }
   if (evals + *sN * 5 > N) return 2;
@@ -148,6 +169,7 @@ __device__ int abort_decision_warp(double r_mine, double s_mine, int64_t it, int
 
 struct AbortArgs {
   int64_t* control;
+  int dtype;
   const double* stats;
   int64_t n_stat_slots;
   cudaGraphConditionalHandle handle;
@@ -176,10 +198,13 @@ __global__ void __launch_bounds__(32) vegas_abort_kernel(AbortArgs a) {
   int stop = 4;  // the statistics slots ran out: nothing valid to test
   int64_t sN = c[kCtlNevals];
   evals += c[kCtlWarm];
-  if (ok)
-    stop = abort_decision_warp(r_mine, s_mine, it, evals, c[kCtlN], c[kCtlNInc], c[kCtlMaxIt],
-                               __longlong_as_double(c[kCtlEpsRel]),
-                               __longlong_as_double(c[kCtlEpsAbs]), &sN);
+  if (ok) {
+    const double er = __longlong_as_double(c[kCtlEpsRel]), ea = __longlong_as_double(c[kCtlEpsAbs]);
+    stop = a.dtype == TQ_F32 ? abort_decision_warp<float>(r_mine, s_mine, it, evals, c[kCtlN], c[kCtlNInc],
+                                                          c[kCtlMaxIt], er, ea, &sN)
+                             : abort_decision_warp<double>(r_mine, s_mine, it, evals, c[kCtlN],
+                                                           c[kCtlNInc], c[kCtlMaxIt], er, ea, &sN);
+  }
   if (lane != 0) return;
   if (ok) {
     c[kCtlEvals] = evals;
@@ -218,6 +243,7 @@ extern "C" int tq_vegas_abort_test(const tq_vegas_state* st, uint64_t cond_handl
   if (!st || !st->control || !st->stats || st->n_stat_slots < 1) return TQ_ERR_ARG;
   AbortArgs a;
   a.control = st->control;
+  a.dtype = st->dtype;
   a.stats = st->stats;
   a.n_stat_slots = st->n_stat_slots;
   a.handle = (cudaGraphConditionalHandle)cond_handle;

@@ -58,6 +58,19 @@ class VegasDevice:
         L.check(L.lib().tq_vegas_init(self.ref, L.stream_handle()), "tq_vegas_init")
         L.count_launches(1)
 
+    def clone_state(self):
+        """A new state of the same shape holding a copy of this one's arrays
+        (map, weights, cube sums and counts, dh, statistics, RNG offset,
+        domain, parameters): device copies on the current stream."""
+        c = VegasDevice(self.dim, self.dtype, self.n_bins, self.n_strat, self.device, self.domain,
+                        stats_slots=self.stats.shape[0])
+        for name in ("x_edges", "dx_edges", "weights", "counts", "dh", "jf", "jf2", "neval",
+                     "cube_start", "scalars", "params", "_rb"):
+            getattr(c, name).copy_(getattr(self, name))
+        c._rb_host.copy_(self._rb_host)
+        c.dh_pending = self.dh_pending
+        return c
+
     def _fill_struct(self):
         s = self.struct
         s.dim = self.dim

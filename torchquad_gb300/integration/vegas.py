@@ -19,7 +19,9 @@ from __future__ import annotations
 import ctypes
 import math
 import warnings
+import weakref
 
+import numpy as np
 import torch
 
 from .. import _lib as L
@@ -56,6 +58,7 @@ class _FusedPlan:
         self.use_grid_improve, self.use_warmup, self.ns = use_grid_improve, use_warmup, ns
         self.uses = 0
         self.graph = None
+        self.owner = None  # weak reference to the VEGAS whose results the state holds
         self._side = torch.cuda.Stream(device=dev.device)
         self._fork, self._join = torch.cuda.Event(), torch.cuda.Event()
 
@@ -149,21 +152,11 @@ class _FusedPlan:
                 return
 
 
-def _sum_lr(xs):
-    t = 0.0
+def _sum_lr(xs, zero=0.0):
+    t = zero
     for x in xs:
         t = t + x
     return t
-
-
-def _ieee_div(a, b):
-    """a / b with IEEE results for b == 0 (inf or nan, as the reference's
-    tensor arithmetic gives) instead of Python's ZeroDivisionError."""
-    if b != 0.0 or b != b:
-        return a / b
-    if a != a or a == 0.0:
-        return math.nan
-    return math.copysign(math.inf, a) * math.copysign(1.0, b)
 
 
 # Set [True] to run the captured sequences as individual launches (for
@@ -274,6 +267,13 @@ class VEGAS(BaseIntegrator):
         _starting_N) and the RNG offset."""
         rng = self.rng
         dev = plan.dev
+        # The plan's state is shared by every VEGAS of this shape; the VEGAS
+        # that used it last gets its own copy before it is overwritten, so its
+        # map and stratification stay its own (as in the reference).
+        prev = plan.owner() if plan.owner is not None else None
+        if prev is not None and prev is not self and prev._dev is dev:
+            prev._detach_state()
+        plan.owner = weakref.ref(self)
         if domain_values is None:
             dev.set_domain(domain)
         warm_evals = 5 * plan.ns if use_warmup else 0
@@ -284,8 +284,13 @@ class VEGAS(BaseIntegrator):
         self.alpha = ALPHA
         plan.run()
         c = dev.host_control
-        if int(c[L.VC_STOP]) == 4:
+        stop = int(c[L.VC_STOP])
+        if stop == 4:
             raise RuntimeError("VEGAS ran out of statistics slots")
+        if stop == 5:  # int() of an infinite value in the abort test (vegas.py:186-189)
+            raise OverflowError("cannot convert float infinity to integer")
+        if stop == 6:
+            raise ValueError("cannot convert float NaN to integer")
         self.it = it = int(c[L.VC_IT])
         self._starting_N = int(c[L.VC_NEVALS])
         self._nr_of_fevals = int(c[L.VC_EVALS])
@@ -297,7 +302,15 @@ class VEGAS(BaseIntegrator):
         # update_DH leaves dh normalised; done on first access
         # (VEGASStratification.dh)
         dev.dh_pending = True
-        return torch.full((), self._get_result(), dtype=self.dtype, device=dev.device)
+        return torch.full((), float(self._get_result()), dtype=self.dtype, device=dev.device)
+
+    def _detach_state(self):
+        """Move this integrator's map and stratification onto a private copy
+        of the shared plan state."""
+        snap = self._dev.clone_state()
+        self._dev = snap
+        self.map._dev = snap
+        self.strat._dev = snap
 
     # ----------------------------------------------------- materialised
     def _integrate_materialised(self, domain, use_warmup):
@@ -362,27 +375,43 @@ class VEGAS(BaseIntegrator):
         return acc
 
     # ------------------------------------------------- shared host logic
+    # The reference keeps results and variances as 0-d tensors of the
+    # state's dtype, so the abort test (vegas.py:161-209) and the estimate
+    # (:318-362) are computed in that dtype: here as numpy scalars of it
+    # (np.float32 / np.float64, every operation rounded once), with Python
+    # scalar operands rounded to the dtype first, as torch does.  Sums run
+    # left to right from zero, as the reference's sums of tensors do (Python's
+    # builtin sum of floats is compensated since 3.12).  x / 0 gives inf or
+    # NaN, as tensors do.  tq_vegas_abort_test does the same on the device.
+    def _scalar(self):
+        return np.float32 if self.dtype == torch.float32 else np.float64
+
+    def _differentiable(self):
+        return any(isinstance(r, torch.Tensor) for r in self.results)
+
     def _check_abort_conditions(self):
         """Every fifth iteration: stop on accuracy, adapt the evaluations per
         iteration, stop on budget/iterations (vegas.py:161-209)."""
         if self.it % 5 > 0:
             return False
-        res_abs = abs(float(self._get_result()))
-        err = self._get_error()
-        chi2 = self._get_chisq()
-        if (err <= self._eps_rel * res_abs or err <= self._eps_abs) and chi2 / 5.0 < 1.0:
-            return True
-        if chi2 / 5.0 < 1.0:
-            if res_abs == 0.0:
+        S = self._scalar()
+        with np.errstate(all="ignore"):
+            res_abs = abs(S(float(self._get_result())))
+            err = S(self._get_error())
+            chi2 = S(self._get_chisq())
+            q = chi2 / S(5.0)
+            if (err <= S(self._eps_rel) * res_abs or err <= S(self._eps_abs)) and q < 1.0:
+                return True
+            if q < 1.0:
+                if res_abs == 0.0:
+                    self._starting_N += self._N_increment
+                else:
+                    acc = err / res_abs
+                    x = S(self._starting_N) * np.sqrt(acc / S(self._eps_rel + 1e-8))
+                    # int() of an infinite / NaN value raises, as in the reference
+                    self._starting_N = min(self._starting_N + self._N_increment, int(x))
+            elif q > 1.0:
                 self._starting_N += self._N_increment
-            else:
-                acc = err / res_abs
-                self._starting_N = min(
-                    self._starting_N + self._N_increment,
-                    int(self._starting_N * math.sqrt(acc / (self._eps_rel + 1e-8))),
-                )
-        elif chi2 / 5.0 > 1.0:
-            self._starting_N += self._N_increment
         if self._nr_of_fevals + self._starting_N * 5 > self.N:
             return True
         if self.it + 5 > self._max_iterations:
@@ -391,29 +420,42 @@ class VEGAS(BaseIntegrator):
         self.sigma2 = []
         return False
 
-    # The sums below run left to right from zero, as the reference's sums of
-    # 0-d tensors do (Python's builtin sum of floats is compensated since
-    # 3.12); tq_vegas_abort_test takes them the same way on the device.
     def _get_result(self):
         """Inverse-variance weighted mean of the iteration results (EQ 30)."""
-        if any(s == 0.0 for s in self.sigma2):
-            return _sum_lr(self.results) / len(self.results)
-        num = _sum_lr(r / s for r, s in zip(self.results, self.sigma2))
-        den = _sum_lr(1.0 / s for s in self.sigma2)
-        return num / den
+        if self._differentiable():  # torch expressions carry the gradient
+            if any(s == 0.0 for s in self.sigma2):
+                return _sum_lr(self.results) / len(self.results)
+            num = _sum_lr(r / s for r, s in zip(self.results, self.sigma2))
+            den = _sum_lr(1.0 / s for s in self.sigma2)
+            return num / den
+        S = self._scalar()
+        rs = [S(float(r)) for r in self.results]
+        ss = [S(float(s)) for s in self.sigma2]
+        with np.errstate(all="ignore"):
+            if any(s == 0.0 for s in ss):
+                return _sum_lr(rs, S(0)) / S(len(rs))
+            num = _sum_lr((r / s for r, s in zip(rs, ss)), S(0))
+            den = _sum_lr((S(1) / s for s in ss), S(0))
+            return num / den
 
     def _get_error(self):
         """Error estimate from the variances (EQ 31)."""
-        res = _sum_lr(1.0 / s for s in self.sigma2 if s != 0.0)
-        return self.sigma2[0] if res == 0 else 1.0 / math.sqrt(res)
+        S = self._scalar()
+        ss = [S(float(s)) for s in self.sigma2]
+        with np.errstate(all="ignore"):
+            res = _sum_lr((S(1) / s for s in ss if s != 0.0), S(0))
+            return ss[0] if res == 0 else S(1) / np.sqrt(res)
 
     def _get_chisq(self):
         """Chi square of the iteration results (EQ 32)."""
-        I_final = float(self._get_result())
-        res = [float(r) for r in self.results]
-        chi2 = 0.0
-        for r, s in zip(res, self.sigma2):
-            if r != I_final:
-                d = r - I_final
-                chi2 += _ieee_div(d * d, s)
+        S = self._scalar()
+        I_final = S(float(self._get_result()))
+        rs = [S(float(r)) for r in self.results]
+        ss = [S(float(s)) for s in self.sigma2]
+        chi2 = S(0)
+        with np.errstate(all="ignore"):
+            for r, s in zip(rs, ss):
+                if r != I_final:
+                    d = r - I_final
+                    chi2 = chi2 + (d * d) / s
         return chi2
