@@ -67,6 +67,7 @@ enum {
  *   TQ_FN_SUM_SIN      f = c * sum_k sin(a_k x_k)
  */
 enum {
+  TQ_FN_PER_DESC = -1, /* batched calls: each descriptor names its own family */
   TQ_FN_EXP_SUM = 1,
   TQ_FN_GAUSSIAN = 2,
   TQ_FN_OSCILLATORY = 3,
@@ -118,18 +119,22 @@ int tq_grid_fused_noalloc(int dtype, int rule, int dim, int64_t n_per_dim,
 
 /* ---- batched grid rules ---------------------------------------------------- */
 
-/* Descriptor of one integral of a batch (48 bytes, int64-aligned). */
+/* Descriptor of one integral of a batch (56 bytes, int64-aligned). */
 typedef struct tq_batch_desc {
   int32_t rule, dim;   /* TQ_RULE_TRAPEZOID..TQ_RULE_GAUSS, 1..TQ_MAX_DIM        */
   int64_t n, total;    /* points per dimension, n^dim                          */
   int64_t par_off;     /* offset of the integral's 2+2*dim parameters in params */
   int64_t dom_off;     /* offset of its [dim][2] domain in domains (dtype)      */
   int64_t gl_off;      /* offset of its n Gauss roots/weights (fp64)           */
+  int32_t family;      /* TQ_FN_* (read when the call's family is TQ_FN_PER_DESC) */
+  int32_t pad;
 } tq_batch_desc;
 
-/* Many tensor-product integrals of one built-in family in one persistent
+/* Many tensor-product integrals of built-in families in one persistent
  * launch (no counterpart in the reference, whose batch is a loop of
- * GridIntegrator.integrate, grid_integrator.py:32-55).  Integral i is cut
+ * GridIntegrator.integrate, grid_integrator.py:32-55).  family is one
+ * TQ_FN_* for every integral, or TQ_FN_PER_DESC to take each descriptor's
+ * (families mixed in one launch).  Integral i is cut
  * into ceil(total_i / tile_points) tiles; tile_start[n_integrals+1] is the
  * exclusive prefix of the tile counts (tile_start[n_integrals] = n_tiles).
  * block (128|256), strip (4|16 nodes per thread) and grid_blocks (0: 8 per
@@ -143,13 +148,14 @@ int tq_batch_grid(int dtype, int64_t n_integrals, const void* descs, const int64
 
 /* Descriptor of one Monte Carlo chunk of a batch (56 bytes). */
 typedef struct tq_mc_desc {
-  int32_t dim, pad;
+  int32_t dim, family;   /* family: TQ_FN_* (read when the call's is TQ_FN_PER_DESC) */
   int64_t first, count;  /* point range [first, first+count) of the stream */
   uint64_t seed, stream_id;
   int64_t par_off, dom_off;
 } tq_mc_desc;
 
-/* One chunk of each of many Monte Carlo integrations of one built-in family
+/* One chunk of each of many Monte Carlo integrations of built-in families
+ * (family: one TQ_FN_* for all, or TQ_FN_PER_DESC for each descriptor's)
  * (no counterpart in the reference; its MonteCarlo.integrate,
  * monte_carlo.py:20-106, does one integral per call).  Request r evaluates
  * points [first, first+count) of its Philox stream (point p uses elements
@@ -177,6 +183,28 @@ int tq_grid_adjoint(int dtype, int rule, int dim, int64_t n_per_dim, const void*
                     const double* params, double* out_value, double* out_grad_domain,
                     double* out_grad_params, void* workspace, size_t workspace_bytes,
                     void* stream);
+
+/* Workspace bytes of tq_batch_grid_adjoint: n_tiles rows of 2 + 4*max_dim
+ * fp64 partial sums. */
+size_t tq_batch_grid_adjoint_workspace_size(int64_t n_tiles, int max_dim);
+
+/* Value and gradient of many tensor-product integrals of built-in families
+ * (dims <= 8) in one persistent launch, the batched form of tq_grid_adjoint
+ * (the reference differentiates each integral separately through torch
+ * autograd over its materialised grid: integration_grid.py:74-88,
+ * utils.py:36-52, gaussian.py:81-84).  descs / tile_start / params /
+ * domains / gl_* as for tq_batch_grid (family per descriptor unless family
+ * >= 0); max_dim: the largest dim of the batch.  Writes, per integral i,
+ * out_value[i] (fp64), out_grad_domain at the integral's dom_off ([dim][2],
+ * fp64: dI/da_k, dI/db_k) and out_grad_params at its par_off (fp64, the
+ * layout of params).  Tiles are summed in tile order: the results do not
+ * depend on the other integrals of the batch. */
+int tq_batch_grid_adjoint(int dtype, int64_t n_integrals, const void* descs,
+                          const int64_t* tile_start, int64_t n_tiles, int64_t tile_points,
+                          const double* params, const void* domains, const double* gl_nodes,
+                          const double* gl_weights, int family, int max_dim, double* out_value,
+                          double* out_grad_domain, double* out_grad_params, void* workspace,
+                          size_t workspace_bytes, void* stream);
 
 /* ---- grid rules: materialised path for arbitrary integrands -------------- */
 

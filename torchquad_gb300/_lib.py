@@ -31,6 +31,7 @@ TQ_F32, TQ_F64 = 0, 1
 TQ_RULE_TRAPEZOID, TQ_RULE_SIMPSON, TQ_RULE_BOOLE, TQ_RULE_GAUSS, TQ_RULE_MC = 0, 1, 2, 3, 4
 
 TQ_FN_EXP_SUM, TQ_FN_GAUSSIAN, TQ_FN_OSCILLATORY, TQ_FN_SUM_SIN = 1, 2, 3, 4
+TQ_FN_PER_DESC = -1  # batched calls: each descriptor's own family
 
 TQ_MAX_DIM = 16
 
@@ -113,6 +114,12 @@ SIGNATURES = {
         c_int,
         [c_int, c_int, c_int, c_int64, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
          c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
+    "tq_batch_grid_adjoint_workspace_size": (c_size_t, [c_int64, c_int]),
+    "tq_batch_grid_adjoint": (
+        c_int,
+        [c_int, c_int64, c_void_p, c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_void_p,
+         c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
     ),
     "tq_batch_grid": (
         c_int,

@@ -11,10 +11,19 @@ weights that the per-call form uses; only the summation order differs.
     b = batch.BatchedGrid(dtype=torch.float64)
     values = b.integrate(integrands, rules, Ns, domains)   # [n] tensor
 
-All integrands of one call are built-in instances of the same family
-(``torchquad_gb300.integrands``); mixed families are split by family.
-The launch shape (threads per CTA, nodes per thread, nodes per tile, CTAs)
-is chosen by a small autotuner that times candidates on the actual batch.
+The integrands are built-in instances (``torchquad_gb300.integrands``) of
+any families: each descriptor carries its family, so a batch that mixes
+families is still one launch.  The launch shape (threads per CTA, nodes per
+thread, nodes per tile, CTAs) is chosen by a small autotuner that times
+candidates on the actual batch.
+
+Gradients: when autograd is on and any integrand parameter or domain tensor
+requires a gradient, ``integrate`` runs the batched adjoint instead
+(``tq_batch_grid_adjoint``: every integral's value and its gradients with
+respect to the domain bounds and the integrand parameters in one pass), and
+the values come back as a differentiable tensor.  The reference
+differentiates each integral on its own through torch autograd over its
+materialised grid (integration_grid.py:74-88, gaussian.py:81-84).
 """
 from __future__ import annotations
 
@@ -38,9 +47,10 @@ RULES = {
 
 DESC_DTYPE = np.dtype(
     [("rule", "<i4"), ("dim", "<i4"), ("n", "<i8"), ("total", "<i8"), ("par_off", "<i8"),
-     ("dom_off", "<i8"), ("gl_off", "<i8")]
+     ("dom_off", "<i8"), ("gl_off", "<i8"), ("family", "<i4"), ("pad", "<i4")]
 )
-assert DESC_DTYPE.itemsize == 48
+assert DESC_DTYPE.itemsize == 56
+FAMILIES = (L.TQ_FN_EXP_SUM, L.TQ_FN_GAUSSIAN, L.TQ_FN_OSCILLATORY, L.TQ_FN_SUM_SIN)
 
 
 def rule_id(r) -> int:
@@ -98,17 +108,25 @@ def _n_for(rid, dim, N):
     return n
 
 
+def _domain_np(d):
+    if isinstance(d, torch.Tensor):
+        d = d.detach().cpu()
+    return np.asarray(d, dtype=np.float64).reshape(-1)
+
+
 def pack(integrands, rules, Ns, domains, dtype, tile_pts):
     """Host side of a batch (numpy only): descriptors, tile prefix, packed
     parameters, domains (in the batch dtype) and Gauss-Legendre tables."""
     m = len(integrands)
     if not (len(rules) == len(Ns) == len(domains) == m) or m == 0:
         raise ValueError("integrands, rules, Ns and domains must have the same non-zero length")
-    family = None
-    for f in integrands:
-        if not isinstance(f, BuiltinIntegrand) or (family is not None and f.family != family):
-            raise ValueError("one batch takes built-in integrands of a single family")
-        family = f.family
+    fams = np.empty(m, dtype=np.int32)
+    for i, f in enumerate(integrands):
+        if not isinstance(f, BuiltinIntegrand) or f.family not in FAMILIES:
+            raise ValueError(f"integral {i}: a batch takes built-in integrands (torchquad_gb300.integrands)")
+        fams[i] = f.family
+    # one family for the whole launch when they agree, else each descriptor's
+    family = int(fams[0]) if (fams == fams[0]).all() else L.TQ_FN_PER_DESC
     rule_cache = {}
     desc = np.zeros(m, dtype=DESC_DTYPE)
     dims = np.fromiter((f.dim for f in integrands), dtype=np.int64, count=m)
@@ -125,7 +143,7 @@ def pack(integrands, rules, Ns, domains, dtype, tile_pts):
                 rule_cache[r] = rid
         rids[i] = rid
         ns[i] = _n_for(rid, int(dims[i]), int(N))
-    dom = np.concatenate([np.asarray(d, dtype=np.float64).reshape(-1) for d in domains])
+    dom = np.concatenate([_domain_np(d) for d in domains])
     if dom.size != 2 * int(dims.sum()):
         raise ValueError("each integration_domain must have dim rows of [low, high]")
     bad = dom[1::2] < dom[0::2]
@@ -154,6 +172,7 @@ def pack(integrands, rules, Ns, domains, dtype, tile_pts):
     desc["par_off"] = np.concatenate([[0], np.cumsum(psize)[:-1]])
     desc["dom_off"] = np.concatenate([[0], np.cumsum(2 * dims)[:-1]])
     desc["gl_off"] = goff
+    desc["family"] = fams
     tiles = (desc["total"] + tile_pts - 1) // tile_pts
     ts = np.zeros(m + 1, dtype=np.int64)
     np.cumsum(tiles, out=ts[1:])
@@ -304,11 +323,86 @@ class BatchedGrid:
         return AUTOTUNER.pick(plan.shape_key, run, L.lib().tq_device_sm_count())
 
     def integrate(self, integrands, rules, Ns, domains):
-        """Values of all integrals, [n] tensor of the batch dtype."""
+        """Values of all integrals, [n] tensor of the batch dtype.  With
+        autograd on and a parameter or domain tensor requiring a gradient,
+        the batched adjoint computes them and the result is differentiable
+        with respect to those tensors."""
+        if torch.is_grad_enabled() and _needs_grad(integrands, domains):
+            return self.integrate_with_grad(integrands, rules, Ns, domains)
         plan = self.plan(integrands, rules, Ns, domains)
         shape = self.tuned_shape(plan)
         self.last_shape = shape
         return self.run(self.retile(plan, shape[2]), shape)
+
+    # ---------------------------------------------------------- gradients
+    def adjoint(self, plan, max_dim=None):
+        """(values [n] fp64, grad_domains [sum 2*dim] fp64, grad_params
+        [len(params)] fp64) of a plan: one tq_batch_grid_adjoint."""
+        max_dim = int(max_dim or plan.desc_np["dim"].max())
+        if max_dim > 8:
+            raise ValueError("batched gradients support dim <= 8")
+        dev = plan.descs.device
+        vals = torch.empty((plan.n_int,), dtype=torch.float64, device=dev)
+        gdom = torch.zeros((plan.domains.numel(),), dtype=torch.float64, device=dev)
+        gpar = torch.zeros((plan.params.numel(),), dtype=torch.float64, device=dev)
+        nbytes = L.lib().tq_batch_grid_adjoint_workspace_size(plan.n_tiles, max_dim)
+        ws = L.workspace.get(nbytes, "batch_adjoint")
+        L.check(
+            L.lib().tq_batch_grid_adjoint(
+                L.dtype_code(self.dtype), plan.n_int, plan.descs.data_ptr(), plan.tile_start.data_ptr(),
+                plan.n_tiles, plan.tile_pts, plan.params.data_ptr(), plan.domains.data_ptr(),
+                plan.gl_nodes.data_ptr(), plan.gl_weights.data_ptr(), plan.family, max_dim, vals.data_ptr(),
+                gdom.data_ptr(), gpar.data_ptr(), ws.data_ptr(), ws.numel(), L.stream_handle(),
+            ),
+            "tq_batch_grid_adjoint",
+        )
+        L.count_launches(2)
+        return vals, gdom, gpar
+
+    def integrate_with_grad(self, integrands, rules, Ns, domains, tile_points=65536):
+        """integrate() with gradients: the values as a tensor whose backward
+        gives every integrand parameter tensor (c, b, a, u) and every domain
+        tensor that requires a gradient its gradient."""
+        plan = self.plan(integrands, rules, Ns, domains, tile_points=tile_points)
+        dev = plan.descs.device
+        # the packed parameters and domains as differentiable functions of the
+        # user's tensors (torch.cat routes the gradients back to each of them)
+        par_t = torch.cat([torch.cat([f.c.reshape(1), f.b.reshape(1), f.a.reshape(-1), f.u.reshape(-1)])
+                           .to(torch.float64) for f in integrands])
+        dom_t = torch.cat([d.reshape(-1).to(torch.float64) if isinstance(d, torch.Tensor)
+                           else torch.as_tensor(_domain_np(d), dtype=torch.float64) for d in domains])
+        return _BatchedAdjointFn.apply(par_t, dom_t, self, plan).to(self.dtype)
+
+
+def _needs_grad(integrands, domains):
+    return any(isinstance(f, BuiltinIntegrand) and f.requires_grad() for f in integrands) or any(
+        isinstance(d, torch.Tensor) and d.requires_grad for d in domains)
+
+
+class _BatchedAdjointFn(torch.autograd.Function):
+    """Forward: the batched adjoint kernel (values and all gradients in one
+    pass); backward: each integral's gradients scaled by its output's."""
+
+    @staticmethod
+    def forward(ctx, par_t, dom_t, bg, plan):
+        vals, gdom, gpar = bg.adjoint(plan)
+        d = plan.desc_np
+        dev = vals.device
+        psize = np.diff(np.append(d["par_off"], plan.params.numel()))
+        ctx.owner_par = torch.from_numpy(np.repeat(np.arange(plan.n_int), psize)).to(dev)
+        ctx.owner_dom = torch.from_numpy(np.repeat(np.arange(plan.n_int), 2 * d["dim"])).to(dev)
+        ctx.par_meta = (par_t.device, par_t.dtype)
+        ctx.dom_meta = (dom_t.device, dom_t.dtype)
+        ctx.save_for_backward(gdom, gpar)
+        return vals
+
+    @staticmethod
+    def backward(ctx, gout):
+        gdom, gpar = ctx.saved_tensors
+        g = gout.detach().to(torch.float64)
+        g_par = (gpar * g[ctx.owner_par]).to(*ctx.par_meta)
+        g_dom = (gdom * g[ctx.owner_dom]).to(*ctx.dom_meta)
+        return g_par, g_dom, None, None
 
 
 def integrate_batch(integrands, rules, Ns, domains, dtype=torch.float64, autotune=True):

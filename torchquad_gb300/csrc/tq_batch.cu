@@ -25,7 +25,10 @@ struct BatchDesc {
   int64_t par_off;  // into params (fp64, 2 + 2*dim values)
   int64_t dom_off;  // into domains (dtype, 2*dim values)
   int64_t gl_off;   // into gl_nodes / gl_weights (Gauss only)
+  int32_t family;   // TQ_FN_* of this integral (used when the launch's family is TQ_FN_PER_DESC)
+  int32_t pad;
 };
+static_assert(sizeof(BatchDesc) == sizeof(tq_batch_desc), "BatchDesc layout");
 
 struct BatchArgs {
   const BatchDesc* desc;
@@ -39,7 +42,89 @@ struct BatchArgs {
   Acc* partials;  // [n_tiles]
 };
 
+// Sum of one tile of the integral described by d (geometry g, family fam
+// and rstride set up in shared memory by the caller); valid in thread 0.
 template <typename T, int FAM, int P>
+__device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t tile, int64_t tile0,
+                             const Geo<T>& g, const Family<T>& fam, const uint64_t* rstride,
+                             InnerTab* tab) {
+  const int dim = d.dim, rule = d.rule, last = dim - 1;
+  const int64_t n = d.n;
+  const int n32 = (int)n;
+  const bool gl = rule == TQ_RULE_GAUSS;
+  const double* gln = a.gl_nodes + d.gl_off;
+  const double* glw = a.gl_weights + d.gl_off;
+  const int64_t begin = (tile - tile0) * a.tile_pts;
+  const int64_t end = min(d.total, begin + a.tile_pts);
+  const double wlast = g.wscale[last];
+  const T a_l = g.a[last], b_l = g.b[last], st_l = g.step[last];
+  const int half = n32 / 2;
+  // fp64: last-dimension tables of this tile's integral (one
+  // outer-function evaluation per row)
+  bool use_tab = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if (dim >= 2 && n <= kTabMax) use_tab = build_inner_tab<FAM>(*tab, g, fam, last, n32, gl, rule, gln, glw);
+  }
+  Acc acc{0.0, 0.0};
+  for (int64_t base = begin + (int64_t)threadIdx.x * P; base < end; base += (int64_t)blockDim.x * P) {
+    uint64_t row = (uint64_t)base / (uint64_t)n;
+    int jl = (int)(base - (int64_t)row * n);
+    int64_t left = min((int64_t)P, end - base);
+    while (left > 0) {
+      T s_outer = T(0);
+      double w_outer = 1.0;
+      for (int k = 0; k < dim - 1; ++k) {
+        const int64_t digit = (int64_t)((row / rstride[k]) % (uint64_t)n);
+        const T x = gl ? (T)__dadd_rn(__dmul_rn(g.half[k], __ldg(gln + digit)), g.mid[k])
+                       : linspace_node<T>(g.a[k], g.b[k], g.step[k], n, digit);
+        const T t = fam_term<FAM, T>(fam, k, x);
+        s_outer = (k == 0) ? t : s_outer + t;
+        w_outer *= g.wscale[k] * (gl ? __ldg(glw + digit) : (double)nc_int(rule, digit, n));
+      }
+      const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
+      T sum = T(0), comp = T(0);
+      bool tabbed = false;
+      if constexpr (std::is_same<T, double>::value) {
+        if (use_tab) {
+          const RowFactor rf = row_factor<FAM>(fam, s_outer);
+          if (rf.ok) {
+            for (int j = jl; j < seg_end; ++j) {
+              const double y = tab->w[j] * tab_value<FAM>(rf, tab->t1[j], tab->t2[j]) - comp;
+              const double tt = sum + y;
+              comp = (tt - sum) - y;
+              sum = tt;
+            }
+            tabbed = true;
+          }
+        }
+      }
+      for (int j = tabbed ? seg_end : jl; j < seg_end; ++j) {
+        T x;
+        if (gl)
+          x = (T)__dadd_rn(__dmul_rn(g.half[last], __ldg(gln + j)), g.mid[last]);
+        else
+          x = (j < half) ? fma(st_l, (T)j, a_l) : fma(-st_l, (T)(n32 - 1 - j), b_l);
+        const T f = fam_outer<FAM, T>(fam, s_outer + fam_term<FAM, T>(fam, last, x));
+        const T wj = gl ? (T)__ldg(glw + j) : (T)nc_int(rule, j, n);
+        // Kahan in the working type within the segment
+        const T y = wj * f - comp;
+        const T tt = sum + y;
+        comp = (tt - sum) - y;
+        sum = tt;
+      }
+      acc_add(acc, ((double)sum - (double)comp) * (w_outer * wlast));
+      left -= seg_end - jl;
+      jl = 0;
+      ++row;
+    }
+  }
+  return block_reduce<256>(acc);
+}
+
+// Persistent launch over the flat tile list.  The family of a tile's
+// integral is the launch's (a.family >= 0) or its descriptor's, so one
+// launch can mix families; the switch is uniform across a CTA.
+template <typename T, int P>
 __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
   __shared__ Geo<T> g;
   __shared__ Family<T> fam;
@@ -62,7 +147,7 @@ __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
       d = a.desc[lo];
       tile0 = a.tile_start[lo];
       geo_setup<T, T>(g, d.rule, d.dim, d.n, (const T*)a.domains + d.dom_off);
-      load_family<T>(fam, a.family, d.dim, a.params + d.par_off);
+      load_family<T>(fam, a.family >= 0 ? a.family : d.family, d.dim, a.params + d.par_off);
       uint64_t st = 1;
       for (int k = d.dim - 2; k >= 0; --k) {
         rstride[k] = st;
@@ -70,79 +155,23 @@ __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
       }
     }
     __syncthreads();
-    const int dim = d.dim, rule = d.rule, last = dim - 1;
-    const int64_t n = d.n;
-    const int n32 = (int)n;
-    const bool gl = rule == TQ_RULE_GAUSS;
-    const double* gln = a.gl_nodes + d.gl_off;
-    const double* glw = a.gl_weights + d.gl_off;
-    const int64_t begin = (tile - tile0) * a.tile_pts;
-    const int64_t end = min(d.total, begin + a.tile_pts);
-    const double wlast = g.wscale[last];
-    const T a_l = g.a[last], b_l = g.b[last], st_l = g.step[last];
-    const int half = n32 / 2;
-    // fp64: last-dimension tables of this tile's integral (one
-    // outer-function evaluation per row)
-    bool use_tab = false;
-    if constexpr (std::is_same<T, double>::value) {
-      if (dim >= 2 && n <= kTabMax)
-        use_tab = build_inner_tab<FAM>(*tab, g, fam, last, n32, gl, rule, gln, glw);
+    Acc acc{CUDART_NAN, 0.0};  // an unknown family (rejected on the host) gives NaN
+    switch (fam.id) {
+      case TQ_FN_EXP_SUM:
+        acc = grid_tile_sum<T, TQ_FN_EXP_SUM, P>(a, d, tile, tile0, g, fam, rstride, tab);
+        break;
+      case TQ_FN_GAUSSIAN:
+        acc = grid_tile_sum<T, TQ_FN_GAUSSIAN, P>(a, d, tile, tile0, g, fam, rstride, tab);
+        break;
+      case TQ_FN_OSCILLATORY:
+        acc = grid_tile_sum<T, TQ_FN_OSCILLATORY, P>(a, d, tile, tile0, g, fam, rstride, tab);
+        break;
+      case TQ_FN_SUM_SIN:
+        acc = grid_tile_sum<T, TQ_FN_SUM_SIN, P>(a, d, tile, tile0, g, fam, rstride, tab);
+        break;
+      default:
+        break;
     }
-    Acc acc{0.0, 0.0};
-    for (int64_t base = begin + (int64_t)threadIdx.x * P; base < end;
-         base += (int64_t)blockDim.x * P) {
-      uint64_t row = (uint64_t)base / (uint64_t)n;
-      int jl = (int)(base - (int64_t)row * n);
-      int64_t left = min((int64_t)P, end - base);
-      while (left > 0) {
-        T s_outer = T(0);
-        double w_outer = 1.0;
-        for (int k = 0; k < dim - 1; ++k) {
-          const int64_t digit = (int64_t)((row / rstride[k]) % (uint64_t)n);
-          const T x = gl ? (T)__dadd_rn(__dmul_rn(g.half[k], __ldg(gln + digit)), g.mid[k])
-                         : linspace_node<T>(g.a[k], g.b[k], g.step[k], n, digit);
-          const T t = fam_term<FAM, T>(fam, k, x);
-          s_outer = (k == 0) ? t : s_outer + t;
-          w_outer *= g.wscale[k] * (gl ? __ldg(glw + digit) : (double)nc_int(rule, digit, n));
-        }
-        const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
-        T sum = T(0), comp = T(0);
-        bool tabbed = false;
-        if constexpr (std::is_same<T, double>::value) {
-          if (use_tab) {
-            const RowFactor rf = row_factor<FAM>(fam, s_outer);
-            if (rf.ok) {
-              for (int j = jl; j < seg_end; ++j) {
-                const double y = tab->w[j] * tab_value<FAM>(rf, tab->t1[j], tab->t2[j]) - comp;
-                const double tt = sum + y;
-                comp = (tt - sum) - y;
-                sum = tt;
-              }
-              tabbed = true;
-            }
-          }
-        }
-        for (int j = tabbed ? seg_end : jl; j < seg_end; ++j) {
-          T x;
-          if (gl)
-            x = (T)__dadd_rn(__dmul_rn(g.half[last], __ldg(gln + j)), g.mid[last]);
-          else
-            x = (j < half) ? fma(st_l, (T)j, a_l) : fma(-st_l, (T)(n32 - 1 - j), b_l);
-          const T f = fam_outer<FAM, T>(fam, s_outer + fam_term<FAM, T>(fam, last, x));
-          const T wj = gl ? (T)__ldg(glw + j) : (T)nc_int(rule, j, n);
-          // Kahan in the working type within the segment
-          const T y = wj * f - comp;
-          const T tt = sum + y;
-          comp = (tt - sum) - y;
-          sum = tt;
-        }
-        acc_add(acc, ((double)sum - (double)comp) * (w_outer * wlast));
-        left -= seg_end - jl;
-        jl = 0;
-        ++row;
-      }
-    }
-    acc = block_reduce<256>(acc);
     if (threadIdx.x == 0) a.partials[tile] = acc;
     __syncthreads();
   }
@@ -183,6 +212,7 @@ extern "C" int tq_batch_grid(int dtype, int64_t n_integrals, const void* descs,
       !domains || !out || !workspace)
     return TQ_ERR_ARG;
   if (block != 128 && block != 256) return TQ_ERR_ARG;
+  if (family != TQ_FN_PER_DESC && (family < TQ_FN_EXP_SUM || family > TQ_FN_SUM_SIN)) return TQ_ERR_FAMILY;
   if (strip != 4 && strip != 16) return TQ_ERR_ARG;
   if (workspace_bytes < (size_t)n_tiles * sizeof(Acc)) return TQ_ERR_WORKSPACE;
   BatchArgs a;
@@ -200,16 +230,14 @@ extern "C" int tq_batch_grid(int dtype, int64_t n_integrals, const void* descs,
   int64_t grid = grid_blocks > 0 ? grid_blocks : (int64_t)sm_count() * 8;
   if (grid > n_tiles) grid = n_tiles;
   cudaStream_t s = (cudaStream_t)stream;
-#define TQ_BATCH(T, PV) batch_grid_kernel<T, FAM, PV><<<(unsigned)grid, block, 0, s>>>(a)
-  TQ_DISPATCH_FAMILY(family, FAM, {
-    if (dtype == TQ_F64) {
-      if (strip == 4) TQ_BATCH(double, 4);
-      else TQ_BATCH(double, 16);
-    } else {
-      if (strip == 4) TQ_BATCH(float, 4);
-      else TQ_BATCH(float, 16);
-    }
-  });
+#define TQ_BATCH(T, PV) batch_grid_kernel<T, PV><<<(unsigned)grid, block, 0, s>>>(a)
+  if (dtype == TQ_F64) {
+    if (strip == 4) TQ_BATCH(double, 4);
+    else TQ_BATCH(double, 16);
+  } else {
+    if (strip == 4) TQ_BATCH(float, 4);
+    else TQ_BATCH(float, 16);
+  }
 #undef TQ_BATCH
   int e = launch_status();
   if (e != TQ_OK) return e;
@@ -231,7 +259,7 @@ extern "C" int tq_batch_grid(int dtype, int64_t n_integrals, const void* descs,
 namespace tq {
 
 struct McDesc {
-  int32_t dim, pad;
+  int32_t dim, family;  // family: TQ_FN_* of this request (launch family TQ_FN_PER_DESC)
   int64_t first, count;  // point range of this chunk
   uint64_t seed, sid;
   int64_t par_off, dom_off;
@@ -247,13 +275,45 @@ struct BatchMcArgs {
   Acc* partials;  // [n_tiles][2]
 };
 
+// Sums f and f^2 over one tile of the chunk described by d; valid in thread 0.
 template <typename T, int FAM>
+__device__ void mc_tile_sums(const McDesc& d, int64_t begin, int64_t end, const Family<T>& fam,
+                             const T* lo, const T* wid, Acc& s1, Acc& s2) {
+  constexpr int PB = Uniform<T>::per_block;
+  const int dim = d.dim;
+  for (int64_t q = begin + threadIdx.x; q < end; q += blockDim.x) {
+    const uint64_t p = (uint64_t)(d.first + q);
+    const uint64_t e0 = p * (uint64_t)dim;
+    const uint64_t blk0 = e0 / PB;
+    const int lane0 = (int)(e0 % PB);
+    int cur = -1;
+    uint4 r = make_uint4(0, 0, 0, 0);
+    T s = T(0);
+    for (int k = 0; k < dim; ++k) {
+      const int le = lane0 + k, bi = le / PB;
+      if (bi != cur) {
+        r = philox_block(d.seed, d.sid, blk0 + (uint64_t)bi);
+        cur = bi;
+      }
+      const T u = Uniform<T>::from(r, le - bi * PB);
+      const T x = u * wid[k] + lo[k];
+      const T g = fam_term<FAM, T>(fam, k, x);
+      s = (k == 0) ? g : s + g;
+    }
+    const double f = (double)fam_outer<FAM, T>(fam, s);
+    acc_add(s1, f);
+    acc_add(s2, f * f);
+  }
+  s1 = block_reduce<256>(s1);
+  s2 = block_reduce<256>(s2);
+}
+
+template <typename T>
 __global__ void __launch_bounds__(256) batch_mc_kernel(BatchMcArgs a) {
   __shared__ Family<T> fam;
   __shared__ T lo[kMaxDim], wid[kMaxDim];
   __shared__ McDesc d;
   __shared__ int64_t tile0;
-  constexpr int PB = Uniform<T>::per_block;
   for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
     if (threadIdx.x == 0) {
       int64_t l = 0, h = a.n_req;
@@ -264,7 +324,7 @@ __global__ void __launch_bounds__(256) batch_mc_kernel(BatchMcArgs a) {
       }
       d = a.desc[l];
       tile0 = a.tile_start[l];
-      load_family<T>(fam, a.family, d.dim, a.params + d.par_off);
+      load_family<T>(fam, a.family >= 0 ? a.family : d.family, d.dim, a.params + d.par_off);
       const T* dom = (const T*)a.domains + d.dom_off;
       for (int k = 0; k < d.dim; ++k) {
         lo[k] = dom[2 * k];
@@ -272,35 +332,26 @@ __global__ void __launch_bounds__(256) batch_mc_kernel(BatchMcArgs a) {
       }
     }
     __syncthreads();
-    const int dim = d.dim;
     const int64_t begin = (tile - tile0) * a.tile_pts;
     const int64_t end = min(d.count, begin + a.tile_pts);
     Acc s1{0.0, 0.0}, s2{0.0, 0.0};
-    for (int64_t q = begin + threadIdx.x; q < end; q += blockDim.x) {
-      const uint64_t p = (uint64_t)(d.first + q);
-      const uint64_t e0 = p * (uint64_t)dim;
-      const uint64_t blk0 = e0 / PB;
-      const int lane0 = (int)(e0 % PB);
-      int cur = -1;
-      uint4 r = make_uint4(0, 0, 0, 0);
-      T s = T(0);
-      for (int k = 0; k < dim; ++k) {
-        const int le = lane0 + k, bi = le / PB;
-        if (bi != cur) {
-          r = philox_block(d.seed, d.sid, blk0 + (uint64_t)bi);
-          cur = bi;
-        }
-        const T u = Uniform<T>::from(r, le - bi * PB);
-        const T x = u * wid[k] + lo[k];
-        const T g = fam_term<FAM, T>(fam, k, x);
-        s = (k == 0) ? g : s + g;
-      }
-      const double f = (double)fam_outer<FAM, T>(fam, s);
-      acc_add(s1, f);
-      acc_add(s2, f * f);
+    switch (fam.id) {
+      case TQ_FN_EXP_SUM:
+        mc_tile_sums<T, TQ_FN_EXP_SUM>(d, begin, end, fam, lo, wid, s1, s2);
+        break;
+      case TQ_FN_GAUSSIAN:
+        mc_tile_sums<T, TQ_FN_GAUSSIAN>(d, begin, end, fam, lo, wid, s1, s2);
+        break;
+      case TQ_FN_OSCILLATORY:
+        mc_tile_sums<T, TQ_FN_OSCILLATORY>(d, begin, end, fam, lo, wid, s1, s2);
+        break;
+      case TQ_FN_SUM_SIN:
+        mc_tile_sums<T, TQ_FN_SUM_SIN>(d, begin, end, fam, lo, wid, s1, s2);
+        break;
+      default:
+        s1.s = CUDART_NAN;
+        break;
     }
-    s1 = block_reduce<256>(s1);
-    s2 = block_reduce<256>(s2);
     if (threadIdx.x == 0) {
       a.partials[2 * tile] = s1;
       a.partials[2 * tile + 1] = s2;
@@ -347,6 +398,7 @@ extern "C" int tq_batch_mc(int dtype, int64_t n_requests, const void* descs,
       !domains || !acc || !workspace)
     return TQ_ERR_ARG;
   if (workspace_bytes < (size_t)n_tiles * 2 * sizeof(Acc)) return TQ_ERR_WORKSPACE;
+  if (family != TQ_FN_PER_DESC && (family < TQ_FN_EXP_SUM || family > TQ_FN_SUM_SIN)) return TQ_ERR_FAMILY;
   BatchMcArgs a;
   a.desc = (const McDesc*)descs;
   a.tile_start = tile_start;
@@ -360,12 +412,10 @@ extern "C" int tq_batch_mc(int dtype, int64_t n_requests, const void* descs,
   int64_t grid = (int64_t)sm_count() * 8;
   if (grid > n_tiles) grid = n_tiles;
   cudaStream_t s = (cudaStream_t)stream;
-  TQ_DISPATCH_FAMILY(family, FAM, {
-    if (dtype == TQ_F64)
-      batch_mc_kernel<double, FAM><<<(unsigned)grid, 256, 0, s>>>(a);
-    else
-      batch_mc_kernel<float, FAM><<<(unsigned)grid, 256, 0, s>>>(a);
-  });
+  if (dtype == TQ_F64)
+    batch_mc_kernel<double><<<(unsigned)grid, 256, 0, s>>>(a);
+  else
+    batch_mc_kernel<float><<<(unsigned)grid, 256, 0, s>>>(a);
   int e = launch_status();
   if (e != TQ_OK) return e;
   batch_mc_finalize_kernel<<<(unsigned)((n_requests * 32 + 255) / 256), 256, 0, s>>>(

@@ -1,6 +1,7 @@
 // Adjoint of the fused tensor-product rules: the integral and its gradient
 // with respect to the domain bounds and the integrand parameters, in one
-// pass over the grid (reverse mode of I = sum_i W_i f(x_i; theta)).
+// pass over the grid (reverse mode of I = sum_i W_i f(x_i; theta)); for one
+// integral (tq_grid_adjoint) and for a batch of many (tq_batch_grid_adjoint).
 //
 // The reference differentiates through torch autograd over the materialised
 // [n^d, d] graph (integration_grid.py:74-88 requires_grad branch,
@@ -16,50 +17,292 @@
 // Outer-dimension factors g_k', dg_k/da_k, t_k are constant along a grid
 // row, so a row segment only accumulates sum W F, sum W F' and the
 // last-dimension terms; the outer terms are folded in once per segment.
+//
+// fp64 grids of at most kAdjTab nodes per dimension take every node's F and
+// F' from a per-row factor and a last-dimension table (the identities of the
+// forward kernels' row tables: exp(s + t) = exp(s) exp(t), cos(p + t) =
+// cos p cos t - sin p sin t, sin(p + t) = sin p cos t + cos p sin t), so the
+// outer function is evaluated once per row instead of once per node; every
+// node's value is still formed and weighted.
+
+#include <type_traits>
 
 #include "tq_grid_common.cuh"
 
 namespace tq {
 
-template <int FAM, typename T>
-__device__ __forceinline__ void fam_outer_d(const Family<T>& f, T s, T& F, T& Fp) {
-  if (FAM == TQ_FN_EXP_SUM) {
-    F = exp(s + f.b);
-    Fp = F;
-  } else if (FAM == TQ_FN_GAUSSIAN) {
-    F = exp(-s);
-    Fp = -F;
-  } else if (FAM == TQ_FN_OSCILLATORY) {
-    T sn, cs;
-    sincos((T)(2.0 * CUDART_PI) * f.b + s, &sn, &cs);
-    F = cs;
-    Fp = -sn;
-  } else {
-    F = s;
-    Fp = (T)1;
+constexpr int kAdjTab = 256;  // last-dimension nodes the adjoint's table holds
+constexpr int kAdjP = 16;     // consecutive nodes per thread and strip
+
+struct AdjTab {
+  double w[kAdjTab];   // unscaled 1-D weight
+  double t[kAdjTab];   // unit node
+  double T1[kAdjTab];  // exp(+-t) | cos t | sin(a x)
+  double T2[kAdjTab];  // sin t (oscillatory)
+  double gp[kAdjTab], ga[kAdjTab], gu[kAdjTab];
+};
+
+// Everything a thread needs to walk the nodes of one integral.
+template <typename T, bool GL, int DM>
+struct AdjCtx {
+  const Geo<T>* g;
+  const Family<T>* fam;
+  const uint64_t* rstride;
+  int dim, rule;
+  int64_t n;
+  const double* gln;
+  const double* glw;
+  AdjTab* tab;
+  bool use_tab;
+};
+
+template <int DM>
+struct AdjAcc {
+  double F, Fp, Sx[DM], St[DM], Pa[DM], Pu[DM];
+  __device__ void zero() {
+    F = Fp = 0.0;
+#pragma unroll
+    for (int k = 0; k < DM; ++k) Sx[k] = St[k] = Pa[k] = Pu[k] = 0.0;
   }
+  // accumulator i of 2 + 4 * dim (F, F', then Sx, St, Pa, Pu by dimension)
+  __device__ double at(int i, int dim) const {
+    if (i == 0) return F;
+    if (i == 1) return Fp;
+    const int q = (i - 2) / dim, k = (i - 2) - q * dim;
+    double v = 0.0;
+#pragma unroll
+    for (int kk = 0; kk < DM; ++kk)
+      if (kk == k) v = q == 0 ? Sx[kk] : q == 1 ? St[kk] : q == 2 ? Pa[kk] : Pu[kk];
+    return v;
+  }
+};
+
+// Sums every accumulator i < 2 + 4*dim over the CTA and stores the sums at
+// out[i * out_stride] (fixed trees: warp shuffles, then warp order).  sh:
+// kBlock/32 rows of 2 + 4*DM doubles.  Contains a barrier; ends with one.
+template <int DM>
+__device__ void adj_block_store(const AdjAcc<DM>& acc, int dim, double (*sh)[2 + 4 * DM], double* out,
+                                int64_t out_stride) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nacc = 2 + 4 * dim;
+  for (int i = 0; i < nacc; ++i) {
+    double v = acc.at(i, dim);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp][i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nacc) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w][threadIdx.x];
+    out[threadIdx.x * out_stride] = t;
+  }
+  __syncthreads();
 }
 
-// g_k'(x), dg_k/da_k, dg_k/du_k
-template <int FAM, typename T>
-__device__ __forceinline__ void fam_term_d(const Family<T>& f, int k, T x, T& gp, T& ga, T& gu) {
-  if (FAM == TQ_FN_GAUSSIAN) {
-    const T dd = x - f.u[k];
-    gp = (T)2 * f.a[k] * dd;
-    ga = dd * dd;
-    gu = -(T)2 * f.a[k] * dd;
+// Row factors of the table path: F = p*T1 (exp families), p*T1 - q*T2
+// (oscillatory), p + T1 (sum of sines).
+struct AdjRow {
+  double p, q;
+  bool ok;
+};
+template <int FAM>
+__device__ __forceinline__ AdjRow adj_row(const Family<double>& f, double s) {
+  AdjRow r;
+  r.q = 0.0;
+  r.ok = true;
+  if (FAM == TQ_FN_OSCILLATORY) {
+    sincos(2.0 * CUDART_PI * f.b + s, &r.q, &r.p);
   } else if (FAM == TQ_FN_SUM_SIN) {
-    const T cs = cos(f.a[k] * x);
-    gp = f.a[k] * cs;
-    ga = x * cs;
-    gu = (T)0;
+    r.p = s;
   } else {
-    gp = f.a[k];
-    ga = x;
-    gu = (T)0;
+    r.p = exp(FAM == TQ_FN_GAUSSIAN ? -s : s + f.b);
+    r.ok = normal_factor(r.p);
+  }
+  return r;
+}
+template <int FAM>
+__device__ __forceinline__ void adj_value(const AdjRow& r, double t1, double t2, double& F, double& Fp) {
+  if (FAM == TQ_FN_OSCILLATORY) {
+    F = fma(r.p, t1, -(r.q * t2));    // cos(p + t)
+    Fp = -fma(r.q, t1, r.p * t2);     // -sin(p + t)
+  } else if (FAM == TQ_FN_SUM_SIN) {
+    F = r.p + t1;
+    Fp = 1.0;
+  } else {
+    F = r.p * t1;
+    Fp = FAM == TQ_FN_GAUSSIAN ? -F : F;
   }
 }
 
+// Builds the last-dimension table (all threads of the CTA; ends with a
+// barrier); returns whether every entry is usable.
+template <typename T, bool GL, int FAM, int DM>
+__device__ bool adj_build_tab(const AdjCtx<T, GL, DM>& c) {
+  const int last = c.dim - 1, n32 = (int)c.n;
+  const T ustep = (T)1 / (T)(c.n - 1);
+  int bad = 0;
+  for (int j = threadIdx.x; j < n32; j += blockDim.x) {
+    const T x = node_at<T, GL>(*c.g, last, c.n, j, c.gln);
+    c.tab->w[j] = GL ? __ldg(c.glw + j) : (double)nc_int(c.rule, j, c.n);
+    c.tab->t[j] = GL ? (double)(T)((__ldg(c.gln + j) + 1.0) * 0.5)
+                     : (double)linspace_node<T>((T)0, (T)1, ustep, c.n, j);
+    T gp, ga, gu;
+    fam_term_d<FAM, T>(*c.fam, last, x, gp, ga, gu);
+    c.tab->gp[j] = (double)gp;
+    c.tab->ga[j] = (double)ga;
+    c.tab->gu[j] = (double)gu;
+    const double tv = (double)fam_term<FAM, T>(*c.fam, last, x);
+    if (FAM == TQ_FN_OSCILLATORY) {
+      double sn, cs;
+      sincos(tv, &sn, &cs);
+      c.tab->T1[j] = cs;
+      c.tab->T2[j] = sn;
+    } else if (FAM == TQ_FN_SUM_SIN) {
+      c.tab->T1[j] = tv;
+      c.tab->T2[j] = 0.0;
+    } else {
+      const double e = exp(FAM == TQ_FN_GAUSSIAN ? -tv : tv);
+      c.tab->T1[j] = e;
+      c.tab->T2[j] = 0.0;
+      bad |= !normal_factor(e);
+    }
+  }
+  return !__syncthreads_or(bad);
+}
+
+// Adds the nodes [first, end) visited in strips of kAdjP starting at
+// first, first + step, ... (flat indices, last dimension fastest).
+template <typename T, bool GL, int FAM, int DM>
+__device__ void adj_accumulate(const AdjCtx<T, GL, DM>& c, int64_t first, int64_t end, int64_t step,
+                               AdjAcc<DM>& acc) {
+  const Geo<T>& g = *c.g;
+  const Family<T>& fam = *c.fam;
+  const int dim = c.dim, last = dim - 1;
+  const int64_t n = c.n;
+  const int n32 = (int)n;
+  const double wlast = g.wscale[last];
+  const T ustep = (T)1 / (T)(n - 1);
+  auto unit = [&](int64_t j) -> T {
+    if (GL) return (T)((__ldg(c.gln + j) + 1.0) * 0.5);
+    return linspace_node<T>((T)0, (T)1, ustep, n, j);
+  };
+  auto wunit = [&](int64_t j) -> double { return GL ? __ldg(c.glw + j) : (double)nc_int(c.rule, j, n); };
+  for (int64_t base = first; base < end; base += step) {
+    uint64_t row = (uint64_t)base / (uint64_t)n;
+    int jl = (int)(base - (int64_t)row * n);
+    int64_t left = min((int64_t)kAdjP, end - base);
+    while (left > 0) {
+      // outer-dimension state of this row: the separable sum and the weight
+      // now, the per-dimension derivative factors after the segment (fewer
+      // live registers across the node loop)
+      T s_outer = T(0);
+      double w_outer = 1.0;
+#pragma unroll
+      for (int k = 0; k < DM; ++k) {
+        if (k < dim - 1) {
+          const int64_t digit = (int64_t)((row / c.rstride[k]) % (uint64_t)n);
+          const T x = node_at<T, GL>(g, k, n, digit, c.gln);
+          const T tv = fam_term<FAM, T>(fam, k, x);
+          s_outer = (k == 0) ? tv : s_outer + tv;
+          w_outer *= g.wscale[k] * wunit(digit);
+        }
+      }
+      const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
+      double sF = 0.0, sFp = 0.0, sX = 0.0, sT = 0.0, sA = 0.0, sU = 0.0;
+      bool tabbed = false;
+      if constexpr (std::is_same<T, double>::value) {
+        if (c.use_tab) {
+          const AdjRow rf = adj_row<FAM>(fam, s_outer);
+          if (rf.ok) {
+            const AdjTab& tb = *c.tab;
+            for (int j = jl; j < seg_end; ++j) {
+              double F, Fp;
+              adj_value<FAM>(rf, tb.T1[j], tb.T2[j], F, Fp);
+              const double W = tb.w[j];
+              const double wfp = W * Fp;
+              sF += W * F;
+              sFp += wfp;
+              sX += wfp * tb.gp[j];
+              sT += wfp * tb.gp[j] * tb.t[j];
+              sA += wfp * tb.ga[j];
+              sU += wfp * tb.gu[j];
+            }
+            tabbed = true;
+          }
+        }
+      }
+      if (!tabbed) {
+        for (int j = jl; j < seg_end; ++j) {
+          const T x = node_at<T, GL>(g, last, n, j, c.gln);
+          T F, Fp, gp, ga, gu;
+          fam_outer_d<FAM, T>(fam, s_outer + fam_term<FAM, T>(fam, last, x), F, Fp);
+          fam_term_d<FAM, T>(fam, last, x, gp, ga, gu);
+          const double W = wunit(j);
+          const double wfp = W * (double)Fp;
+          sF += W * (double)F;
+          sFp += wfp;
+          sX += wfp * (double)gp;
+          sT += wfp * (double)gp * (double)unit(j);
+          sA += wfp * (double)ga;
+          sU += wfp * (double)gu;
+        }
+      }
+      const double sc = w_outer * wlast;
+      acc.F += sc * sF;
+      acc.Fp += sc * sFp;
+      const double fo = sc * sFp;
+#pragma unroll
+      for (int k = 0; k < DM; ++k) {
+        if (k < dim - 1) {
+          const int64_t digit = (int64_t)((row / c.rstride[k]) % (uint64_t)n);
+          const T x = node_at<T, GL>(g, k, n, digit, c.gln);
+          T gp_o, ga_o, gu_o;
+          fam_term_d<FAM, T>(fam, k, x, gp_o, ga_o, gu_o);
+          const T t_o = unit(digit);
+          acc.Sx[k] += fo * (double)gp_o;
+          acc.St[k] += fo * (double)gp_o * (double)t_o;
+          acc.Pa[k] += fo * (double)ga_o;
+          acc.Pu[k] += fo * (double)gu_o;
+        } else if (k == last) {
+          acc.Sx[k] += sc * sX;
+          acc.St[k] += sc * sT;
+          acc.Pa[k] += sc * sA;
+          acc.Pu[k] += sc * sU;
+        }
+      }
+      left -= seg_end - jl;
+      jl = 0;
+      ++row;
+    }
+  }
+}
+
+// The integral and its gradients from the reduced accumulators tot[2+4*dim]
+// (one thread).
+template <typename D>
+__device__ void adj_outputs(const double* tot, int family, double c, const D* dom, int dim,
+                            double* out_value, double* out_gdom, double* out_gpar) {
+  const double I = c * tot[0];
+  *out_value = I;
+  for (int k = 0; k < dim; ++k) {
+    const double L = (double)dom[2 * k + 1] - (double)dom[2 * k];
+    const double sx = c * tot[2 + k], st = c * tot[2 + dim + k];
+    out_gdom[2 * k] = -I / L + (sx - st);
+    out_gdom[2 * k + 1] = I / L + st;
+    out_gpar[2 + k] = c * tot[2 + 2 * dim + k];
+    out_gpar[2 + dim + k] = c * tot[2 + 3 * dim + k];
+  }
+  out_gpar[0] = tot[0];
+  if (family == TQ_FN_EXP_SUM)
+    out_gpar[1] = c * tot[0];
+  else if (family == TQ_FN_OSCILLATORY)
+    out_gpar[1] = 2.0 * CUDART_PI * c * tot[1];
+  else
+    out_gpar[1] = 0.0;
+}
+
+// ----------------------------------------------------------- one integral
 struct GradArgs {
   int rule, dim, family;
   int64_t n, total;
@@ -74,28 +317,13 @@ struct GradArgs {
   double* out_gpar;  // [2 + 2*dim]
 };
 
-__device__ __forceinline__ double block_sum_tree(double v, double* sh) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if (lane == 0) sh[warp] = v;
-  __syncthreads();
-  double t = 0.0;
-  if (warp == 0) {
-    t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-  }
-  return t;
-}
-
 template <typename T, typename D, bool GL, int FAM, int DM>
 __global__ void __launch_bounds__(kBlock) grid_adjoint_kernel(GradArgs args) {
   __shared__ Geo<T> g;
   __shared__ Family<T> fam;
   __shared__ uint64_t rstride[kMaxDim];
-  __shared__ double sh[kBlock / 32];
+  __shared__ double sh[kBlock / 32][2 + 4 * DM];
+  __shared__ AdjTab tab;
   if (threadIdx.x == 0) {
     geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
     load_family<T>(fam, args.family, args.dim, args.params);
@@ -106,109 +334,19 @@ __global__ void __launch_bounds__(kBlock) grid_adjoint_kernel(GradArgs args) {
     }
   }
   __syncthreads();
-  const int dim = args.dim, last = dim - 1, rule = args.rule;
-  const int64_t n = args.n, total = args.total;
-  const int n32 = (int)n;
-  const double wlast = g.wscale[last];
-  const T ustep = (T)1 / (T)(n - 1);
-
-  // unit node t in [0,1] of index j in a dimension (see header comment)
-  auto unit = [&](int j) -> T {
-    if (GL) return (T)((__ldg(args.gl_nodes + j) + 1.0) * 0.5);
-    return linspace_node<T>((T)0, (T)1, ustep, n, j);
-  };
-  auto node = [&](int k, int64_t j) -> T { return node_at<T, GL>(g, k, n, j, args.gl_nodes); };
-  auto wunit = [&](int64_t j) -> double {
-    return GL ? __ldg(args.gl_weights + j) : (double)nc_int(rule, j, n);
-  };
-
-  double accF = 0.0, accFp = 0.0;
-  double Sx[DM], St[DM], Pa[DM], Pu[DM];
-#pragma unroll
-  for (int k = 0; k < DM; ++k) Sx[k] = St[k] = Pa[k] = Pu[k] = 0.0;
-
-  constexpr int P = 16;
+  AdjCtx<T, GL, DM> c{&g, &fam, rstride, args.dim, args.rule, args.n, args.gl_nodes, args.gl_weights, &tab,
+                      false};
+  if (std::is_same<T, double>::value && args.dim >= 2 && args.n <= kAdjTab)
+    c.use_tab = adj_build_tab<T, GL, FAM, DM>(c);
+  AdjAcc<DM> acc;
+  acc.zero();
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * P; base < total;
-       base += nthreads * P) {
-    uint64_t row = (uint64_t)base / (uint64_t)n;
-    int jl = (int)(base - (int64_t)row * n);
-    int64_t left = min((int64_t)P, total - base);
-    while (left > 0) {
-      // outer-dimension state of this row
-      T s_outer = T(0);
-      double w_outer = 1.0;
-      T gp_o[DM], ga_o[DM], gu_o[DM], t_o[DM];
-#pragma unroll
-      for (int k = 0; k < DM; ++k) gp_o[k] = ga_o[k] = gu_o[k] = t_o[k] = T(0);
-#pragma unroll
-      for (int k = 0; k < DM; ++k) {
-        if (k < dim - 1) {
-          const int64_t digit = (int64_t)((row / rstride[k]) % (uint64_t)n);
-          const T x = node(k, digit);
-          const T tv = fam_term<FAM, T>(fam, k, x);
-          s_outer = (k == 0) ? tv : s_outer + tv;
-          w_outer *= g.wscale[k] * wunit(digit);
-          fam_term_d<FAM, T>(fam, k, x, gp_o[k], ga_o[k], gu_o[k]);
-          t_o[k] = unit((int)digit);
-        }
-      }
-      const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
-      double sF = 0.0, sFp = 0.0, sX = 0.0, sT = 0.0, sA = 0.0, sU = 0.0;
-      for (int j = jl; j < seg_end; ++j) {
-        const T x = node(last, j);
-        T F, Fp, gp, ga, gu;
-        fam_outer_d<FAM, T>(fam, s_outer + fam_term<FAM, T>(fam, last, x), F, Fp);
-        fam_term_d<FAM, T>(fam, last, x, gp, ga, gu);
-        const double W = wunit(j);
-        const double wfp = W * (double)Fp;
-        sF += W * (double)F;
-        sFp += wfp;
-        sX += wfp * (double)gp;
-        sT += wfp * (double)gp * (double)unit(j);
-        sA += wfp * (double)ga;
-        sU += wfp * (double)gu;
-      }
-      const double sc = w_outer * wlast;
-      accF += sc * sF;
-      accFp += sc * sFp;
-      const double fo = sc * sFp;
-#pragma unroll
-      for (int k = 0; k < DM; ++k) {
-        if (k < dim - 1) {
-          Sx[k] += fo * (double)gp_o[k];
-          St[k] += fo * (double)gp_o[k] * (double)t_o[k];
-          Pa[k] += fo * (double)ga_o[k];
-          Pu[k] += fo * (double)gu_o[k];
-        } else if (k == last) {
-          Sx[k] += sc * sX;
-          St[k] += sc * sT;
-          Pa[k] += sc * sA;
-          Pu[k] += sc * sU;
-        }
-      }
-      left -= seg_end - jl;
-      jl = 0;
-      ++row;
-    }
-  }
+  adj_accumulate<T, GL, FAM, DM>(c, ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kAdjP, args.total,
+                                 nthreads * kAdjP, acc);
 
-  // per-CTA sums, one accumulator at a time: nacc = 2 + 4 * dim
-  const int nacc = 2 + 4 * dim;
-  auto acc_at = [&](int i) -> double {
-    if (i == 0) return accF;
-    if (i == 1) return accFp;
-    const int q = (i - 2) / dim, k = (i - 2) - q * dim;
-    double v = 0.0;
-#pragma unroll
-    for (int kk = 0; kk < DM; ++kk)
-      if (kk == k) v = q == 0 ? Sx[kk] : q == 1 ? St[kk] : q == 2 ? Pa[kk] : Pu[kk];
-    return v;
-  };
-  for (int i = 0; i < nacc; ++i) {
-    const double t = block_sum_tree(acc_at(i), sh);
-    if (threadIdx.x == 0) args.partials[(int64_t)blockIdx.x * nacc + i] = t;
-  }
+  // per-CTA sums of the nacc = 2 + 4 * dim accumulators
+  const int dim = args.dim, nacc = 2 + 4 * dim;
+  adj_block_store<DM>(acc, dim, sh, args.partials + (int64_t)blockIdx.x * nacc, 1);
   if (last_block_arrives(args.ticket)) {
     // each warp reduces accumulators over the CTAs (strided, compensated,
     // fixed merge order)
@@ -223,27 +361,142 @@ __global__ void __launch_bounds__(kBlock) grid_adjoint_kernel(GradArgs args) {
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      const double c = (double)fam.c;
-      const double I = c * tot[0];
-      *args.out_value = I;
-      const D* dom = (const D*)args.domain;
-      for (int k = 0; k < dim; ++k) {
-        const double L = (double)dom[2 * k + 1] - (double)dom[2 * k];
-        const double sx = c * tot[2 + k], st = c * tot[2 + dim + k];
-        args.out_gdom[2 * k] = -I / L + (sx - st);
-        args.out_gdom[2 * k + 1] = I / L + st;
-        args.out_gpar[2 + k] = c * tot[2 + 2 * dim + k];
-        args.out_gpar[2 + dim + k] = c * tot[2 + 3 * dim + k];
-      }
-      args.out_gpar[0] = tot[0];
-      if (FAM == TQ_FN_EXP_SUM)
-        args.out_gpar[1] = c * tot[0];
-      else if (FAM == TQ_FN_OSCILLATORY)
-        args.out_gpar[1] = 2.0 * CUDART_PI * c * tot[1];
-      else
-        args.out_gpar[1] = 0.0;
+      adj_outputs<D>(tot, FAM, (double)fam.c, (const D*)args.domain, dim, args.out_value, args.out_gdom,
+                     args.out_gpar);
       *args.ticket = 0u;
     }
+  }
+}
+
+// ---------------------------------------------------------- many integrals
+// Tiles of tile_pts consecutive nodes of one integral (the tq_batch_grid
+// layout); each tile's 2 + 4*dim sums go to its row of partials, and a
+// second kernel reduces every integral's rows in tile order.
+struct BatchGradArgs {
+  const tq_batch_desc* desc;
+  const int64_t* tile_start;
+  int64_t n_int, n_tiles, tile_pts;
+  const double* params;
+  const void* domains;
+  const double* gl_nodes;
+  const double* gl_weights;
+  int family;
+  int stride;        // partial sums per tile row: 2 + 4 * DM
+  double* partials;  // [n_tiles][stride]
+};
+
+template <typename T, typename D, bool GL, int FAM, int DM>
+__device__ void batch_adj_tile(const BatchGradArgs& a, const tq_batch_desc& d, int64_t tile, int64_t tile0,
+                               const Geo<T>& g, const Family<T>& fam, const uint64_t* rstride, AdjTab* tab,
+                               double (*sh)[2 + 4 * DM]) {
+  AdjCtx<T, GL, DM> c{&g, &fam, rstride, d.dim, d.rule, d.n, a.gl_nodes + d.gl_off, a.gl_weights + d.gl_off,
+                      tab, false};
+  if (std::is_same<T, double>::value && d.dim >= 2 && d.n <= kAdjTab)
+    c.use_tab = adj_build_tab<T, GL, FAM, DM>(c);
+  const int64_t begin = (tile - tile0) * a.tile_pts;
+  const int64_t end = min(d.total, begin + a.tile_pts);
+  AdjAcc<DM> acc;
+  acc.zero();
+  adj_accumulate<T, GL, FAM, DM>(c, begin + (int64_t)threadIdx.x * kAdjP, end,
+                                 (int64_t)blockDim.x * kAdjP, acc);
+  adj_block_store<DM>(acc, d.dim, sh, a.partials + tile * a.stride, 1);
+}
+
+// Tile body of one (node type, rule kind) for the tile's family.
+template <typename T, typename D, bool GL, int DM>
+__device__ void batch_adj_dispatch(const BatchGradArgs& a, const tq_batch_desc& d, int64_t tile, int64_t tile0,
+                                   const Geo<T>& g, const Family<T>& fam, const uint64_t* rstride, AdjTab* tab,
+                                   double (*sh)[2 + 4 * DM]) {
+  switch (fam.id) {
+    case TQ_FN_EXP_SUM:
+      batch_adj_tile<T, D, GL, TQ_FN_EXP_SUM, DM>(a, d, tile, tile0, g, fam, rstride, tab, sh);
+      break;
+    case TQ_FN_GAUSSIAN:
+      batch_adj_tile<T, D, GL, TQ_FN_GAUSSIAN, DM>(a, d, tile, tile0, g, fam, rstride, tab, sh);
+      break;
+    case TQ_FN_OSCILLATORY:
+      batch_adj_tile<T, D, GL, TQ_FN_OSCILLATORY, DM>(a, d, tile, tile0, g, fam, rstride, tab, sh);
+      break;
+    default:
+      batch_adj_tile<T, D, GL, TQ_FN_SUM_SIN, DM>(a, d, tile, tile0, g, fam, rstride, tab, sh);
+      break;
+  }
+}
+
+// Gauss integrals and fp64 batches work in fp64; fp32 Newton-Cotes
+// integrals in fp32 (the node arithmetic of tq_grid_adjoint).
+template <typename D, int DM>
+__global__ void __launch_bounds__(kBlock) batch_adjoint_kernel(BatchGradArgs a) {
+  __shared__ Geo<double> g64;
+  __shared__ Family<double> fam64;
+  __shared__ Geo<float> g32;
+  __shared__ Family<float> fam32;
+  __shared__ uint64_t rstride[kMaxDim];
+  __shared__ double sh[kBlock / 32][2 + 4 * DM];
+  __shared__ AdjTab tab;
+  __shared__ tq_batch_desc d;
+  __shared__ int64_t tile0;
+  constexpr bool kF32 = std::is_same<D, float>::value;
+  for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+    if (threadIdx.x == 0) {
+      int64_t lo = 0, hi = a.n_int;  // largest i with tile_start[i] <= tile
+      while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (a.tile_start[mid] <= tile) lo = mid;
+        else hi = mid;
+      }
+      d = a.desc[lo];
+      tile0 = a.tile_start[lo];
+      const int fid = a.family >= 0 ? a.family : d.family;
+      const D* dom = (const D*)a.domains + d.dom_off;
+      if (kF32 && d.rule != TQ_RULE_GAUSS) {
+        geo_setup<float, D>(g32, d.rule, d.dim, d.n, dom);
+        load_family<float>(fam32, fid, d.dim, a.params + d.par_off);
+      } else {
+        geo_setup<double, D>(g64, d.rule, d.dim, d.n, dom);
+        load_family<double>(fam64, fid, d.dim, a.params + d.par_off);
+      }
+      uint64_t st = 1;
+      for (int k = d.dim - 2; k >= 0; --k) {
+        rstride[k] = st;
+        st *= (uint64_t)d.n;
+      }
+    }
+    __syncthreads();
+    if (d.rule == TQ_RULE_GAUSS)
+      batch_adj_dispatch<double, D, true, DM>(a, d, tile, tile0, g64, fam64, rstride, &tab, sh);
+    else if (kF32)
+      batch_adj_dispatch<float, D, false, DM>(a, d, tile, tile0, g32, fam32, rstride, &tab, sh);
+    else
+      batch_adj_dispatch<double, D, false, DM>(a, d, tile, tile0, g64, fam64, rstride, &tab, sh);
+    __syncthreads();
+  }
+}
+
+// One warp per integral: compensated sums of its tile rows in tile order,
+// then the value and gradients.
+template <typename D>
+__global__ void batch_adjoint_finalize_kernel(BatchGradArgs a, double* out_value, double* out_gdom,
+                                              double* out_gpar) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  __shared__ double tot[kBlock / 32][2 + 4 * 8];
+  if (w >= a.n_int) return;
+  const tq_batch_desc d = a.desc[w];
+  const int nacc = 2 + 4 * d.dim;
+  const int64_t t0 = a.tile_start[w], t1 = a.tile_start[w + 1];
+  for (int i = 0; i < nacc; ++i) {
+    Acc s{0.0, 0.0};
+    for (int64_t t = t0 + lane; t < t1; t += 32) acc_add(s, a.partials[t * a.stride + i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc_merge(s, acc_shfl_down(s, o));
+    if (lane == 0) tot[wib][i] = s.s + s.c;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    const int fid = a.family >= 0 ? a.family : d.family;
+    adj_outputs<D>(tot[wib], fid, a.params[d.par_off], (const D*)a.domains + d.dom_off, d.dim, out_value + w,
+                   out_gdom + d.dom_off, out_gpar + d.par_off);
   }
 }
 
@@ -252,9 +505,16 @@ __global__ void __launch_bounds__(kBlock) grid_adjoint_kernel(GradArgs args) {
 using namespace tq;
 
 static int64_t adj_blocks(int64_t total) {
-  const int64_t need = (total + (int64_t)kBlock * 16 - 1) / ((int64_t)kBlock * 16);
+  const int64_t need = (total + (int64_t)kBlock * kAdjP - 1) / ((int64_t)kBlock * kAdjP);
   const int64_t cap = (int64_t)sm_count() * 4;
   return need < 1 ? 1 : (need < cap ? need : cap);
+}
+
+static bool valid_nc(int rule, int64_t n) {
+  if (rule < TQ_RULE_TRAPEZOID || rule > TQ_RULE_GAUSS || n < 2) return false;
+  if (rule == TQ_RULE_SIMPSON && (n < 3 || !(n & 1))) return false;
+  if (rule == TQ_RULE_BOOLE && (n < 5 || (n - 1) % 4)) return false;
+  return true;
 }
 
 extern "C" size_t tq_grid_adjoint_workspace_size(int dim, int64_t total_points) {
@@ -268,10 +528,7 @@ extern "C" int tq_grid_adjoint(int dtype, int rule, int dim, int64_t n_per_dim, 
                                void* stream) {
   if (!valid_dtype(dtype)) return TQ_ERR_DTYPE;
   if (dim < 1 || dim > 8) return TQ_ERR_DIM;
-  if (rule < TQ_RULE_TRAPEZOID || rule > TQ_RULE_GAUSS) return TQ_ERR_RULE;
-  if ((rule == TQ_RULE_SIMPSON && (n_per_dim < 3 || !(n_per_dim & 1))) ||
-      (rule == TQ_RULE_BOOLE && (n_per_dim < 5 || (n_per_dim - 1) % 4)) || n_per_dim < 2)
-    return TQ_ERR_RULE;
+  if (!valid_nc(rule, n_per_dim)) return TQ_ERR_RULE;
   if (!domain || !params || !out_value || !out_grad_domain || !out_grad_params || !workspace)
     return TQ_ERR_ARG;
   if (rule == TQ_RULE_GAUSS && (!gl_nodes || !gl_weights)) return TQ_ERR_ARG;
@@ -317,5 +574,59 @@ extern "C" int tq_grid_adjoint(int dtype, int rule, int dim, int64_t n_per_dim, 
     }
   });
 #undef TQ_ADJ
+  return launch_status();
+}
+
+extern "C" size_t tq_batch_grid_adjoint_workspace_size(int64_t n_tiles, int max_dim) {
+  if (n_tiles < 1 || max_dim < 1 || max_dim > 8) return 0;
+  const int dm = max_dim <= 4 ? 4 : 8;
+  return (size_t)n_tiles * (2 + 4 * (size_t)dm) * sizeof(double);
+}
+
+extern "C" int tq_batch_grid_adjoint(int dtype, int64_t n_integrals, const void* descs,
+                                     const int64_t* tile_start, int64_t n_tiles, int64_t tile_points,
+                                     const double* params, const void* domains, const double* gl_nodes,
+                                     const double* gl_weights, int family, int max_dim, double* out_value,
+                                     double* out_grad_domain, double* out_grad_params, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+  if (!valid_dtype(dtype)) return TQ_ERR_DTYPE;
+  if (max_dim < 1 || max_dim > 8) return TQ_ERR_DIM;
+  if (family != TQ_FN_PER_DESC && (family < TQ_FN_EXP_SUM || family > TQ_FN_SUM_SIN)) return TQ_ERR_FAMILY;
+  if (n_integrals < 1 || n_tiles < 1 || tile_points < 1 || !descs || !tile_start || !params || !domains ||
+      !out_value || !out_grad_domain || !out_grad_params || !workspace)
+    return TQ_ERR_ARG;
+  const size_t need = tq_batch_grid_adjoint_workspace_size(n_tiles, max_dim);
+  if (workspace_bytes < need) return TQ_ERR_WORKSPACE;
+  BatchGradArgs a;
+  a.desc = (const tq_batch_desc*)descs;
+  a.tile_start = tile_start;
+  a.n_int = n_integrals;
+  a.n_tiles = n_tiles;
+  a.tile_pts = tile_points;
+  a.params = params;
+  a.domains = domains;
+  a.gl_nodes = gl_nodes ? gl_nodes : params;  // unused unless an integral is Gauss
+  a.gl_weights = gl_weights ? gl_weights : params;
+  a.family = family;
+  a.stride = 2 + 4 * (max_dim <= 4 ? 4 : 8);
+  a.partials = (double*)workspace;
+  int64_t grid = (int64_t)sm_count() * 4;
+  if (grid > n_tiles) grid = n_tiles;
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned g = (unsigned)grid;
+  if (dtype == TQ_F64) {
+    if (max_dim <= 4) batch_adjoint_kernel<double, 4><<<g, kBlock, 0, s>>>(a);
+    else batch_adjoint_kernel<double, 8><<<g, kBlock, 0, s>>>(a);
+  } else {
+    if (max_dim <= 4) batch_adjoint_kernel<float, 4><<<g, kBlock, 0, s>>>(a);
+    else batch_adjoint_kernel<float, 8><<<g, kBlock, 0, s>>>(a);
+  }
+  int e = launch_status();
+  if (e != TQ_OK) return e;
+  const unsigned fb = (unsigned)((n_integrals * 32 + kBlock - 1) / kBlock);
+  if (dtype == TQ_F64)
+    batch_adjoint_finalize_kernel<double><<<fb, kBlock, 0, s>>>(a, out_value, out_grad_domain, out_grad_params);
+  else
+    batch_adjoint_finalize_kernel<float><<<fb, kBlock, 0, s>>>(a, out_value, out_grad_domain, out_grad_params);
   return launch_status();
 }

@@ -170,4 +170,63 @@ __device__ __forceinline__ double tab_value(const RowFactor& f, double t1, doubl
   return f.r1 * t1;
 }
 
+// ------------------------------------------------ adjoint of the families
+// F(s) and F'(s) of the outer function, without the factor c.
+template <int FAM, typename T>
+__device__ __forceinline__ void fam_outer_d(const Family<T>& f, T s, T& F, T& Fp) {
+  if (FAM == TQ_FN_EXP_SUM) {
+    F = exp(s + f.b);
+    Fp = F;
+  } else if (FAM == TQ_FN_GAUSSIAN) {
+    F = exp(-s);
+    Fp = -F;
+  } else if (FAM == TQ_FN_OSCILLATORY) {
+    T sn, cs;
+    sincos((T)(2.0 * CUDART_PI) * f.b + s, &sn, &cs);
+    F = cs;
+    Fp = -sn;
+  } else {
+    F = s;
+    Fp = (T)1;
+  }
+}
+
+// g_k'(x), dg_k/da_k, dg_k/du_k
+template <int FAM, typename T>
+__device__ __forceinline__ void fam_term_d(const Family<T>& f, int k, T x, T& gp, T& ga, T& gu) {
+  if (FAM == TQ_FN_GAUSSIAN) {
+    const T dd = x - f.u[k];
+    gp = (T)2 * f.a[k] * dd;
+    ga = dd * dd;
+    gu = -(T)2 * f.a[k] * dd;
+  } else if (FAM == TQ_FN_SUM_SIN) {
+    const T cs = cos(f.a[k] * x);
+    gp = f.a[k] * cs;
+    ga = x * cs;
+    gu = (T)0;
+  } else {
+    gp = f.a[k];
+    ga = x;
+    gu = (T)0;
+  }
+}
+
+// Sum of v over the CTA (fixed tree); valid in warp 0, lane 0.  sh: 32
+// doubles of shared memory.
+__device__ __forceinline__ double block_sum_tree(double v, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  return t;
+}
+
 }  // namespace tq

@@ -135,6 +135,18 @@ class BuiltinIntegrand:
     def __repr__(self):
         return f"{type(self).__name__}(dim={self.dim})"
 
+    def exact(self, domain) -> float:
+        """The integral over the box domain [[lo, hi]] * dim in closed form
+        (fp64 on the host): the reference value accuracy is reported
+        against."""
+        raise NotImplementedError
+
+    def _box(self, domain):
+        d = np.asarray(domain.detach().cpu() if isinstance(domain, torch.Tensor) else domain,
+                       dtype=np.float64).reshape(self.dim, 2)
+        p = self.params_numpy()
+        return d[:, 0], d[:, 1], float(p[0]), float(p[1]), p[2:2 + self.dim], p[2 + self.dim:]
+
 
 class ExpSum(BuiltinIntegrand):
     """f(x) = c * exp(sum_k a_k x_k + b)."""
@@ -146,6 +158,13 @@ class ExpSum(BuiltinIntegrand):
 
     def _outer(self, s, c, b):
         return c * torch.exp(s + b)
+
+    def exact(self, domain):
+        lo, hi, c, b, a, _ = self._box(domain)
+        v = c * math.exp(b)
+        for k in range(self.dim):
+            v *= (hi[k] - lo[k]) if a[k] == 0.0 else (math.exp(a[k] * hi[k]) - math.exp(a[k] * lo[k])) / a[k]
+        return v
 
 
 class GaussianPeak(BuiltinIntegrand):
@@ -173,6 +192,14 @@ class GaussianPeak(BuiltinIntegrand):
     def _outer(self, s, c, b):
         return c * torch.exp(-s)
 
+    def exact(self, domain):
+        lo, hi, c, _, a, u = self._box(domain)
+        v = c
+        for k in range(self.dim):
+            r = math.sqrt(a[k])
+            v *= math.sqrt(math.pi / a[k]) / 2.0 * (math.erf(r * (hi[k] - u[k])) - math.erf(r * (lo[k] - u[k])))
+        return v
+
 
 class Oscillatory(BuiltinIntegrand):
     """f(x) = c * cos(2 pi b + sum_k a_k x_k)   (b plays the role of u)."""
@@ -184,6 +211,19 @@ class Oscillatory(BuiltinIntegrand):
 
     def _outer(self, s, c, b):
         return c * torch.cos((2.0 * math.pi) * b + s)
+
+    def exact(self, domain):
+        # Re[c e^{i 2 pi b} prod_k (e^{i a_k hi_k} - e^{i a_k lo_k}) / (i a_k)]
+        lo, hi, c, b, a, _ = self._box(domain)
+        z = complex(math.cos(2.0 * math.pi * b), math.sin(2.0 * math.pi * b))
+        for k in range(self.dim):
+            if a[k] == 0.0:
+                z *= hi[k] - lo[k]
+            else:
+                e1 = complex(math.cos(a[k] * hi[k]), math.sin(a[k] * hi[k]))
+                e0 = complex(math.cos(a[k] * lo[k]), math.sin(a[k] * lo[k]))
+                z *= (e1 - e0) / complex(0.0, a[k])
+        return c * z.real
 
 
 class SumSin(BuiltinIntegrand):
@@ -199,6 +239,16 @@ class SumSin(BuiltinIntegrand):
 
     def _outer(self, s, c, b):
         return c * s
+
+    def exact(self, domain):
+        lo, hi, c, _, a, _ = self._box(domain)
+        vol = float(np.prod(hi - lo))
+        v = 0.0
+        for k in range(self.dim):
+            w = hi[k] - lo[k]
+            ik = w if a[k] == 0.0 else (math.cos(a[k] * lo[k]) - math.cos(a[k] * hi[k])) / a[k]
+            v += ik * vol / w if w != 0.0 else 0.0
+        return c * v
 
 
 __all__ = ["BuiltinIntegrand", "ExpSum", "GaussianPeak", "Oscillatory", "SumSin"]

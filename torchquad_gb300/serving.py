@@ -7,11 +7,11 @@ time.  A scheduler thread
   request's device-memory footprint (VEGAS maps and strata dominate) fits
   the HBM budget, and releases both when the request completes;
 * launches all newly admitted Simpson requests as one batched grid launch
-  (``tq_batch_grid``);
+  per dtype (``tq_batch_grid``; integrand families mixed in one launch);
 * advances every active Monte Carlo request by one chunk of its own Philox
   stream per tick (chunks double from ``mc_chunk`` to ``mc_chunk_max``), all
-  of them in one launch (``tq_batch_mc``), stopping a request at its N or
-  its target relative error;
+  of them in one launch per dtype (``tq_batch_mc``), stopping a request at
+  its N or, with ``mc_early_stop``, at its target relative error;
 * runs each VEGAS request on its own stream with its map and stratification
   resident on the device, one block of five iterations at a time (the
   reference's abort test, vegas.py:161-209, decides after each block), so
@@ -43,7 +43,7 @@ from .integrands import BuiltinIntegrand
 from .integration._vegas_state import VegasDevice, n_strat_for
 from .integration.vegas import ALPHA, BETA, VEGAS, _graphs_enabled
 
-MC_DESC = np.dtype([("dim", "<i4"), ("pad", "<i4"), ("first", "<i8"), ("count", "<i8"), ("seed", "<u8"),
+MC_DESC = np.dtype([("dim", "<i4"), ("family", "<i4"), ("first", "<i8"), ("count", "<i8"), ("seed", "<u8"),
                     ("sid", "<u8"), ("par_off", "<i8"), ("dom_off", "<i8")])
 assert MC_DESC.itemsize == 56
 
@@ -109,6 +109,7 @@ class _VegasSession:
         dt = req.dtype
         v = VEGAS()
         v._dim = req.dim
+        v.dtype = dt
         v._max_iterations = 20
         v._eps_rel, v._eps_abs = req.eps_rel, 0.0
         v.use_grid_improve = True
@@ -191,7 +192,7 @@ class IntegrationServer:
 
     def __init__(self, hbm_budget_bytes=None, max_active=64, mc_chunk=1 << 21, mc_chunk_max=1 << 25,
                  mc_tile=1 << 16,
-                 grid_tile=1 << 15, device=None, streams=8):
+                 grid_tile=1 << 15, device=None, streams=8, mc_early_stop=True):
         self.device = device or L.require_cuda()
         if hbm_budget_bytes is None:
             free, _ = torch.cuda.mem_get_info(self.device)
@@ -201,6 +202,9 @@ class IntegrationServer:
         self.max_active = int(max_active)
         self.mc_chunk, self.mc_tile, self.grid_tile = int(mc_chunk), int(mc_tile), int(grid_tile)
         self.mc_chunk_max = max(int(mc_chunk_max), self.mc_chunk)
+        # stop a Monte Carlo request at its target relative error (True) or
+        # always run it to N, as MonteCarlo.integrate does (False)
+        self.mc_early_stop = bool(mc_early_stop)
         self._ids = itertools.count()
         self._pending = deque()
         self._lock = threading.Lock()
@@ -342,8 +346,8 @@ class IntegrationServer:
     def _launch_grid(self, reqs):
         groups = {}
         for r in reqs:
-            groups.setdefault((r.dtype, r.integrand.family), []).append(r)
-        for (dt, _), rs in groups.items():
+            groups.setdefault(r.dtype, []).append(r)
+        for dt, rs in groups.items():
             bg = BatchedGrid(dtype=dt, autotune=False, tile_points=self.grid_tile)
             with torch.cuda.stream(self._grid_stream):
                 plan = bg.plan([r.integrand for r in rs], ["simpson"] * len(rs), [r.N for r in rs],
@@ -379,10 +383,10 @@ class IntegrationServer:
         groups = {}
         for st in self._mc:
             r = st["req"]
-            groups.setdefault((r.dtype, r.integrand.family), []).append(st)
+            groups.setdefault(r.dtype, []).append(st)
         inflight = []
         with torch.cuda.stream(self._mc_stream):
-            for (dt, fam), sts in groups.items():
+            for dt, sts in groups.items():
                 m = len(sts)
                 desc = np.zeros(m, dtype=MC_DESC)
                 par, dom = [], []
@@ -393,7 +397,7 @@ class IntegrationServer:
                     # few ticks for large N, fine steps for the target-error test
                     cnt = min(st["next_chunk"], r.N - st["done_pts"])
                     st["next_chunk"] = min(2 * st["next_chunk"], self.mc_chunk_max)
-                    desc[i] = (r.dim, 0, st["done_pts"], cnt, r.seed, 0, po, do)
+                    desc[i] = (r.dim, r.integrand.family, st["done_pts"], cnt, r.seed, 0, po, do)
                     st["chunk"] = cnt
                     pv = r.integrand.params_numpy()
                     par.append(pv)
@@ -411,7 +415,7 @@ class IntegrationServer:
                 acc = torch.zeros((m, 4), dtype=torch.float64, device=self.device)
                 ws = torch.empty((int(ts[-1]) * 32,), dtype=torch.uint8, device=self.device)
                 L.check(L.lib().tq_batch_mc(L.dtype_code(dt), m, d_desc.data_ptr(), d_ts.data_ptr(), int(ts[-1]),
-                                            self.mc_tile, d_par.data_ptr(), d_dom.data_ptr(), fam,
+                                            self.mc_tile, d_par.data_ptr(), d_dom.data_ptr(), L.TQ_FN_PER_DESC,
                                             acc.data_ptr(), ws.data_ptr(), ws.numel(), L.stream_handle()),
                         "tq_batch_mc")
                 L.count_launches(2)
@@ -455,7 +459,8 @@ class IntegrationServer:
                     r.result = vol * m1
                     r.error = vol * math.sqrt(max(m2 - m1 * m1, 0.0) / n)
                     r.evals = n
-                    if n >= r.N or (r.eps_rel > 0 and n >= 65536 and r.error <= r.eps_rel * abs(r.result)):
+                    if n >= r.N or (self.mc_early_stop and r.eps_rel > 0 and n >= 65536
+                                    and r.error <= r.eps_rel * abs(r.result)):
                         finished.append(st)
             for st in finished:
                 self._mc.remove(st)
