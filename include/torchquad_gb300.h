@@ -479,6 +479,10 @@ int tq_vegas_accumulate(const tq_vegas_state* st, const void* y, const void* val
 int tq_fp32_fma_probe(int64_t iters, int blocks_per_sm, float* out, double* flops,
                       void* stream);
 
+/* The same with fp64 fused multiply-adds: the FP64-pipe peak the fp64 grid
+ * kernels are measured against (out: one double). */
+int tq_fp64_fma_probe(int64_t iters, int blocks_per_sm, double* out, double* flops, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

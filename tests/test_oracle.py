@@ -83,3 +83,29 @@ def test_adjust_n_matches_reference_rules():
     assert OG.adjust_N(OG.BOOLE, 3, 1000) == 9**3
     assert OG.adjust_N(OG.SIMPSON, 2, 4) == 9
     assert OG.adjust_N(OG.BOOLE, 1, 4) == 5
+
+
+def test_oracle_gradients_match_reference_autograd():
+    """The numpy gradient of the discrete rules (oracle/grad.py) against the
+    reference's torch autograd recorded in the golden fixtures (fp64
+    cases)."""
+    from oracle import grad as OGR
+
+    fams = {"ExpSum": 1, "GaussianPeak": 2, "Oscillatory": 3, "SumSin": 4}
+    rules = {"Trapezoid": 0, "Simpson": 1, "Boole": 2, "GaussLegendre": 3}
+    cases = [c for c in G.load("grid_mc_golden.json")["grads"] if c["dtype"] == "float64"]
+    assert len(cases) >= 4
+    for c in cases:
+        d = c["dim"]
+        p = c["params"]
+        a = np.broadcast_to(np.asarray(p["a"], dtype=np.float64), (d,))
+        u = np.broadcast_to(np.asarray(p.get("u", 0.0), dtype=np.float64), (d,))
+        params = np.concatenate([[p.get("c", 1.0), p.get("b", 0.0)], a, u])
+        n = int(round(c["N"] ** (1.0 / d)))
+        I, gdom, gpar = OGR.value_and_grad(fams[c["family"]], params, rules[c["rule"]], d, n, c["domain"])
+        want = G.f(c["value"])
+        assert abs(I - want) <= 1e-12 * max(1.0, abs(want)), c["name"]
+        assert np.allclose(gdom.ravel(), G.arr(c["grad_domain"]), rtol=1e-10, atol=1e-12), c["name"]
+        names = {"c": [0], "b": [1], "a": list(range(2, 2 + d)), "u": list(range(2 + d, 2 + 2 * d))}
+        for k, hs in c["grads"].items():
+            assert np.allclose(gpar[names[k]], G.arr(hs), rtol=1e-10, atol=1e-12), (c["name"], k)

@@ -171,6 +171,7 @@ SIGNATURES = {
     "tq_vegas_accumulate": (
         c_int, [_VS, c_void_p, c_void_p, c_int64, c_int, c_int, c_void_p, c_size_t, c_void_p]),
     "tq_fp32_fma_probe": (c_int, [c_int64, c_int, c_void_p, c_void_p, c_void_p]),
+    "tq_fp64_fma_probe": (c_int, [c_int64, c_int, c_void_p, c_void_p, c_void_p]),
     "tq_mc_fused": (
         c_int,
         [c_int, c_int, c_int64, c_void_p, c_int, c_void_p, c_uint64, c_uint64, c_uint64,

@@ -234,6 +234,92 @@ __global__ void __launch_bounds__(kBlock) grid_points_kernel(PointsArgs args) {
   }
 }
 
+// Tiled variant (HBM-write bound): a CTA builds a tile of consecutive
+// points in shared memory (one thread per point; digits by multiply-high
+// division by n; node values from a per-CTA table of every dimension's
+// nodes), then one thread hands the tile to the bulk-copy engine
+// (cp.async.bulk shared -> global), so the stores are full-line writes
+// issued without per-thread store instructions.  Two tile buffers alternate;
+// a buffer is rewritten only after its previous copy has been read out
+// (cp.async.bulk.wait_group.read 1).  Needs a 16-byte aligned output.
+constexpr int kPtsTileBytes = 24 * 1024;  // per buffer (two buffers per CTA)
+constexpr int kPtsTab = 2048;             // node-table entries (dim * n) a CTA keeps
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+template <typename T, typename D, bool GL>
+__global__ void __launch_bounds__(kBlock) grid_points_tiled_kernel(PointsArgs args, int tile_pts,
+                                                                   int64_t n_tiles) {
+  extern __shared__ __align__(128) unsigned char pts_smem[];
+  __shared__ Geo<T> g;
+  __shared__ FastDiv fd_n;
+  __shared__ T nodes[kPtsTab];  // nodes[k * n + j], when dim * n fits
+  if (threadIdx.x == 0) {
+    geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
+    fd_n = make_fastdiv((uint32_t)args.n);
+  }
+  __syncthreads();
+  const int dim = args.dim;
+  const uint64_t n = (uint64_t)args.n;
+  const int n32 = (int)args.n;
+  // the nodes of every dimension once per CTA (no per-point node arithmetic)
+  const bool tab = (int64_t)dim * args.n <= kPtsTab;
+  if (tab)
+    for (int e = threadIdx.x; e < dim * n32; e += blockDim.x)
+      nodes[e] = node_at<T, GL>(g, e / n32, (int64_t)n, (int64_t)(e % n32), args.gl_nodes);
+  // point indices below 2^32 (all but huge grids): 32-bit digits
+  const bool small = (uint64_t)(args.start + args.count) <= 0xffffffffull;
+  int buf = 0;
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    T* sm = (T*)(pts_smem + (size_t)buf * kPtsTileBytes);
+    const int64_t p0 = tile * (int64_t)tile_pts;  // local point index
+    const int np = (int)min((int64_t)tile_pts, args.count - p0);
+    if (threadIdx.x == 0) {
+      // the copy that last read this buffer (two tiles ago) must be done
+      asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < np; p += blockDim.x) {
+      const uint64_t idx = (uint64_t)(args.start + p0 + p);
+      T* row = sm + (size_t)p * dim;
+      if (small && tab) {
+        uint32_t r = (uint32_t)idx;
+        for (int k = dim - 1; k >= 0; --k) {
+          const uint32_t q = fdiv(r, fd_n);
+          row[k] = nodes[k * n32 + (int)(r - q * fd_n.d)];
+          r = q;
+        }
+      } else {
+        uint64_t r = idx;
+        for (int k = dim - 1; k >= 0; --k) {
+          const uint64_t q = r / n;
+          row[k] = node_at<T, GL>(g, k, (int64_t)n, (int64_t)(r - q * n), args.gl_nodes);
+          r = q;
+        }
+      }
+    }
+    // generic-proxy writes of the tile -> visible to the bulk copy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    const size_t bytes = (size_t)np * dim * sizeof(T);
+    const size_t bulk = bytes & ~(size_t)15;
+    unsigned char* dst = (unsigned char*)args.points + (size_t)p0 * dim * sizeof(T);
+    if (threadIdx.x == 0 && bulk > 0) {
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+                   "r"(smem_u32(sm)), "r"((uint32_t)bulk)
+                   : "memory");
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    }
+    // a tail of 4, 8 or 12 bytes (only in the last tile) by plain stores
+    for (size_t b = bulk + threadIdx.x * sizeof(T); b < bytes; b += blockDim.x * sizeof(T))
+      *(T*)(dst + b) = *(const T*)((const unsigned char*)sm + b);
+    buf ^= 1;
+  }
+  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
 struct WeightsArgs {
   int rule, dim;
   int64_t n, start, count;
@@ -338,6 +424,224 @@ __global__ void __launch_bounds__(kBlock) weighted_sum_kernel(WsumArgs args) {
     }
     if (threadIdx.x == 0) *args.ticket = 0u;
   }
+}
+
+// Weighted sum of one integrand component (n_values == 1, the common case).
+// Along a grid row every node shares its outer weight, so the kernels
+// accumulate sum_j W_j f_j with the unscaled last-dimension weights W_j
+// (fp64 values: one fused multiply-add per node; fp32 values: a compensated
+// fp32 sum on the FP32 pipe) and fold the row's outer weight in once per row
+// segment.  On GB300 an fp64 warp instruction holds a sub-partition's FP64
+// unit for about 64 cycles, so fp64 sums are bound by the FP64 pipe near
+// 0.75 of HBM bandwidth; fp32 sums by HBM.
+template <typename F>
+struct RowAcc;
+template <>
+struct RowAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double w, double v) { s = fma(w, v, s); }
+  __device__ __forceinline__ double value() const { return s; }
+  __device__ __forceinline__ void reset() { s = 0.0; }
+};
+template <>
+struct RowAcc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float w, float v) {
+    const float y = __fmaf_rn(w, v, -c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+  __device__ __forceinline__ void reset() { s = c = 0.f; }
+};
+
+template <typename F, int V>
+__device__ __forceinline__ void load_vec(const F* __restrict__ p, F* v) {
+  if constexpr (sizeof(F) == 8) {
+    const double2 q = __ldg((const double2*)p);
+    v[0] = q.x;
+    v[1] = q.y;
+  } else {
+    const float4 q = __ldg((const float4*)p);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+  }
+}
+
+// Last-CTA reduction of the per-CTA partials into the running sum acc[0..1].
+__device__ __forceinline__ void wsum_finish(const WsumArgs& args, Acc acc) {
+  acc = block_reduce<kBlock>(acc);
+  if (threadIdx.x == 0) args.partials[blockIdx.x] = acc;
+  if (last_block_arrives(args.ticket)) {
+    Acc t{0.0, 0.0};
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc_merge(t, args.partials[i]);
+    t = block_reduce<kBlock>(t);
+    if (threadIdx.x == 0) {
+      Acc run{args.acc[0], args.acc[1]};
+      acc_merge(run, t);
+      args.acc[0] = run.s;
+      args.acc[1] = run.c;
+      *args.ticket = 0u;
+    }
+  }
+}
+
+// Short rows (n < 32): a thread walks strips of P consecutive nodes, read as
+// 16-byte vectors when aligned, with the weights from a shared-memory table.
+constexpr int kWTab = 4096;  // last-dimension weights a CTA keeps
+
+template <typename T, typename D, bool GL, typename F, int P>
+__global__ void __launch_bounds__(kBlock) weighted_sum1_kernel(WsumArgs args) {
+  __shared__ Geo<T> g;
+  __shared__ FastDiv fd_n;
+  __shared__ F wt[kWTab];
+  if (threadIdx.x == 0) {
+    geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
+    fd_n = make_fastdiv((uint32_t)args.n);
+  }
+  const int dim = args.dim, rule = args.rule, last = dim - 1;
+  const int64_t n = args.n;
+  const int n32 = (int)n;
+  const bool tab = n <= kWTab;
+  if (tab)
+    for (int j = threadIdx.x; j < n32; j += blockDim.x) wt[j] = (F)wunit_at<GL>(rule, n, j, args.gl_weights);
+  __syncthreads();
+  const F* __restrict__ f = (const F*)args.f;
+  constexpr int V = 16 / sizeof(F);  // values per 16-byte load
+  const bool vec = (((uintptr_t)f) & 15) == 0;
+  const bool small = (uint64_t)(args.start + args.count) <= 0xffffffffull;
+  const double wlast = g.wscale[last];
+  auto outer_w = [&](uint64_t row) -> double {
+    double w = wlast;
+    if (small) {
+      uint32_t r = (uint32_t)row;
+      for (int k = last - 1; k >= 0; --k) {
+        const uint32_t q = fdiv(r, fd_n);
+        w *= g.wscale[k] * wunit_at<GL>(rule, n, (int64_t)(r - q * fd_n.d), args.gl_weights);
+        r = q;
+      }
+    } else {
+      uint64_t r = row;
+      for (int k = last - 1; k >= 0; --k) {
+        const uint64_t q = r / (uint64_t)n;
+        w *= g.wscale[k] * wunit_at<GL>(rule, n, (int64_t)(r - q * (uint64_t)n), args.gl_weights);
+        r = q;
+      }
+    }
+    return w;
+  };
+  Acc acc{0.0, 0.0};
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * P; base < args.count;
+       base += nthreads * P) {
+    const int cnt = (int)min((int64_t)P, args.count - base);
+    const uint64_t node0 = (uint64_t)(args.start + base);
+    uint64_t row;
+    int j;
+    if (small) {
+      const uint32_t q = fdiv((uint32_t)node0, fd_n);
+      row = q;
+      j = (int)((uint32_t)node0 - q * fd_n.d);
+    } else {
+      row = node0 / (uint64_t)n;
+      j = (int)(node0 - row * (uint64_t)n);
+    }
+    double w_outer = outer_w(row);
+    RowAcc<F> ra;
+#pragma unroll
+    for (int i0 = 0; i0 < P; i0 += V) {
+      F v[V];
+      if (vec && i0 + V <= cnt) {
+        load_vec<F, V>(f + base + i0, v);
+      } else {
+#pragma unroll
+        for (int q = 0; q < V; ++q) v[q] = i0 + q < cnt ? __ldg(f + base + i0 + q) : (F)0;
+      }
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        if (i0 + q < cnt) {
+          ra.add(tab ? wt[j] : (F)wunit_at<GL>(rule, n, j, args.gl_weights), v[q]);
+          if (++j == n32 && i0 + q + 1 < cnt) {  // the strip enters the next row
+            acc_add(acc, ra.value() * w_outer);
+            ra.reset();
+            j = 0;
+            w_outer = outer_w(++row);
+          }
+        }
+      }
+    }
+    acc_add(acc, ra.value() * w_outer);
+  }
+  wsum_finish(args, acc);
+}
+
+// Rows of at least 32 nodes: a warp takes whole grid rows, its lanes read
+// the row with coalesced loads and accumulate W_j f_j, and each lane folds
+// the row's outer weight in once per row (products of per-dimension weight
+// tables in shared memory).  Rows cut by the chunk's start or end are
+// summed over their part in the chunk.
+constexpr int kRowTab = 2048;  // entries of each weight table
+
+template <typename T, typename D, bool GL, typename F>
+__global__ void __launch_bounds__(kBlock) weighted_sum_rows_kernel(WsumArgs args) {
+  __shared__ Geo<T> g;
+  __shared__ FastDiv fd_n;
+  __shared__ F wl[kRowTab];       // unscaled last-dimension weights
+  __shared__ double wo[kRowTab];  // wo[k*n + j] = wscale_k * W_k(j), outer dimensions k
+  if (threadIdx.x == 0) {
+    geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
+    fd_n = make_fastdiv((uint32_t)args.n);
+  }
+  __syncthreads();
+  const int dim = args.dim, rule = args.rule, last = dim - 1;
+  const int64_t n = args.n;
+  const int n32 = (int)n;
+  for (int j = threadIdx.x; j < n32; j += blockDim.x) wl[j] = (F)wunit_at<GL>(rule, n, j, args.gl_weights);
+  for (int e = threadIdx.x; e < last * n32; e += blockDim.x) {
+    const int k = e / n32;
+    wo[e] = g.wscale[k] * wunit_at<GL>(rule, n, e - k * n32, args.gl_weights);
+  }
+  __syncthreads();
+  const F* __restrict__ f = (const F*)args.f;
+  const int lane = threadIdx.x & 31;
+  const int64_t end = args.start + args.count;
+  const uint64_t row_begin = (uint64_t)args.start / (uint64_t)n;
+  const uint64_t row_end = ((uint64_t)end + (uint64_t)n - 1) / (uint64_t)n;
+  const bool small = (uint64_t)end <= 0xffffffffull;
+  const double wlast = g.wscale[last];
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  double lane_acc = 0.0;
+  for (uint64_t r = row_begin + (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < row_end;
+       r += (uint64_t)nwarps) {
+    double w = wlast;
+    if (small) {
+      uint32_t q = (uint32_t)r;
+      for (int k = last - 1; k >= 0; --k) {
+        const uint32_t q2 = fdiv(q, fd_n);
+        w *= wo[k * n32 + (int)(q - q2 * fd_n.d)];
+        q = q2;
+      }
+    } else {
+      uint64_t q = r;
+      for (int k = last - 1; k >= 0; --k) {
+        const uint64_t q2 = q / (uint64_t)n;
+        w *= wo[k * n32 + (int)(q - q2 * (uint64_t)n)];
+        q = q2;
+      }
+    }
+    const int64_t r0 = (int64_t)r * n;
+    const int j0 = (int)max((int64_t)0, args.start - r0);
+    const int j1 = (int)min(n, end - r0);
+    const F* fr = f + (r0 - args.start);
+    RowAcc<F> ra;
+#pragma unroll 4
+    for (int j = j0 + lane; j < j1; j += 32) ra.add(wl[j], __ldg(fr + j));
+    lane_acc += ra.value() * w;
+  }
+  wsum_finish(args, Acc{lane_acc, 0.0});
 }
 
 template <typename D>
@@ -484,6 +788,33 @@ extern "C" int tq_grid_points(int dtype, int rule, int dim, int64_t n_per_dim,
   if (count == 0) return TQ_OK;
   PointsArgs a{rule, dim, n_per_dim, start, count, domain, gl_nodes, points};
   cudaStream_t s = (cudaStream_t)stream;
+  const size_t tsize = (rule == TQ_RULE_GAUSS || dtype == TQ_F64) ? 8 : 4;
+  // tiles of a multiple of 16 points that fill a 24 KiB buffer
+  const int tile_pts = (int)((kPtsTileBytes / (tsize * (size_t)dim)) & ~(size_t)15);
+  if ((((uintptr_t)points) & 15) == 0 && tile_pts >= 16) {
+    const int64_t n_tiles = (count + tile_pts - 1) / tile_pts;
+    const int64_t cap = (int64_t)sm_count() * 4;
+    const dim3 grid((unsigned)(n_tiles < cap ? n_tiles : cap));
+    const size_t smem = 2 * (size_t)kPtsTileBytes;
+#define TQ_PTS_TILED(T, D, GLB)                                                                     \
+  {                                                                                                 \
+    auto k = grid_points_tiled_kernel<T, D, GLB>;                                                   \
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e != cudaSuccess) return set_cuda_error(e);                                                 \
+    k<<<grid, kBlock, smem, s>>>(a, tile_pts, n_tiles);                                             \
+  }
+    if (rule == TQ_RULE_GAUSS) {
+      if (dtype == TQ_F64) TQ_PTS_TILED(double, double, true)
+      else TQ_PTS_TILED(double, float, true)
+    } else if (dtype == TQ_F64) {
+      TQ_PTS_TILED(double, double, false)
+    } else {
+      TQ_PTS_TILED(float, float, false)
+    }
+#undef TQ_PTS_TILED
+    return launch_status();
+  }
+  // unaligned output: one thread per element
   const dim3 grid((unsigned)stream_blocks(count * dim));
   if (rule == TQ_RULE_GAUSS) {
     if (dtype == TQ_F64)
@@ -527,6 +858,7 @@ extern "C" int tq_grid_weights(int dtype, int rule, int dim, int64_t n_per_dim,
 }
 
 static constexpr int kStripW = 8;
+static constexpr int kStripW1 = 32;  // nodes per strip of the short-row weighted sum
 
 static int64_t wsum_blocks_x(int64_t count) {
   const int64_t need = (count + (int64_t)kBlock * kStripW - 1) / ((int64_t)kBlock * kStripW);
@@ -576,11 +908,29 @@ extern "C" int tq_weighted_sum(int dtype, int rule, int dim, int64_t n_per_dim,
   cudaStream_t s = (cudaStream_t)stream;
   const dim3 grid((unsigned)gx, (unsigned)gy);
   const bool gl = rule == TQ_RULE_GAUSS;
-#define TQ_WSUM(T, D, GLB)                                                             \
-  if (f_dtype == TQ_F64)                                                               \
-    weighted_sum_kernel<T, D, GLB, double, kStripW><<<grid, kBlock, 0, s>>>(a);        \
-  else                                                                                 \
-    weighted_sum_kernel<T, D, GLB, float, kStripW><<<grid, kBlock, 0, s>>>(a);
+  // one component of a grid rule: the row kernels (row weights, coalesced
+  // or vector loads); Monte Carlo and vector integrands: the general one
+  const bool scalar = n_values == 1 && rule != TQ_RULE_MC;
+  const bool rows = scalar && n_per_dim >= 32 && n_per_dim <= kRowTab && (dim - 1) * n_per_dim <= kRowTab;
+  int64_t g1 = (count + (int64_t)kBlock * kStripW1 - 1) / ((int64_t)kBlock * kStripW1);
+  g1 = g1 < 1 ? 1 : (g1 < gx ? g1 : gx);  // the workspace holds gx partials
+  const dim3 grid1((unsigned)g1);
+#define TQ_WSUM(T, D, GLB)                                                                   \
+  if (rows) {                                                                                \
+    if (f_dtype == TQ_F64)                                                                   \
+      weighted_sum_rows_kernel<T, D, GLB, double><<<grid, kBlock, 0, s>>>(a);                \
+    else                                                                                     \
+      weighted_sum_rows_kernel<T, D, GLB, float><<<grid, kBlock, 0, s>>>(a);                 \
+  } else if (scalar) {                                                                       \
+    if (f_dtype == TQ_F64)                                                                   \
+      weighted_sum1_kernel<T, D, GLB, double, kStripW1><<<grid1, kBlock, 0, s>>>(a);         \
+    else                                                                                     \
+      weighted_sum1_kernel<T, D, GLB, float, kStripW1><<<grid1, kBlock, 0, s>>>(a);          \
+  } else if (f_dtype == TQ_F64) {                                                            \
+    weighted_sum_kernel<T, D, GLB, double, kStripW><<<grid, kBlock, 0, s>>>(a);              \
+  } else {                                                                                   \
+    weighted_sum_kernel<T, D, GLB, float, kStripW><<<grid, kBlock, 0, s>>>(a);               \
+  }
   if (gl) {
     if (dtype == TQ_F64) {
       TQ_WSUM(double, double, true)
