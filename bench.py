@@ -79,6 +79,85 @@ def _dist_env():
     return ws, rank, local
 
 
+# ------------------------------------------------------------ helpers
+HBM_FALLBACK_GBS = 6800.0
+
+
+def hbm_peak():
+    """(GB/s, source): the measured copy bandwidth of the GB300s
+    (MEASURED_PEAKS.json next to this file), else the fallback figure."""
+    try:
+        with open(ROOT / "MEASURED_PEAKS.json") as fh:
+            v = float(json.load(fh)["hbm_gbs"])
+        return v, "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "of fallback (6.8 TB/s)"
+
+
+def fp_peaks(L, torch):
+    """FP32 and FP64 FMA peaks (TFLOP/s) measured in this run by the probe
+    kernels (best of three launches)."""
+    out = {}
+    for name, dt, fn in (("fp32", torch.float32, "tq_fp32_fma_probe"), ("fp64", torch.float64, "tq_fp64_fma_probe")):
+        buf = torch.zeros(1, dtype=dt, device="cuda")
+        flops = ctypes.c_double(0.0)
+        best = 0.0
+        iters = 4096 if name == "fp32" else 64
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            L.check(getattr(L.lib(), fn)(iters, 8, buf.data_ptr(), ctypes.byref(flops), L.stream_handle()), fn)
+            e1.record()
+            torch.cuda.synchronize()
+            best = max(best, flops.value / (e0.elapsed_time(e1) / 1000.0) / 1e12)
+        out[name] = best
+    return out
+
+
+def timed_launches(torch, fn, reps, flush=None):
+    """Mean device time (s) of fn over reps launches (CUDA events on the
+    current stream); with flush, L2 is overwritten before every launch and
+    each launch is timed on its own."""
+    fn()
+    torch.cuda.synchronize()
+    if flush is None:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps / 1000.0
+    tot = 0.0
+    for k in range(reps):
+        flush.fill_(k & 0xFF)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1) / 1000.0
+    return tot / reps
+
+
+def cpu_cores_used():
+    return 1
+
+
+def c2_accuracy(results, errors):
+    """Relative error of the timed plain-VEGAS integrations against the
+    analytic integral erf(0.5 / (0.05 sqrt 2))^6 (the normal densities
+    truncated to [0, 1]^6), with VEGAS's own error estimate beside it."""
+    import numpy as np
+
+    exact = math.erf(0.5 / (SIGMA * math.sqrt(2.0))) ** DIM
+    rel = np.abs(np.array(results) - exact) / exact
+    est = np.array(errors) / exact
+    return {"analytic": exact, "rel_err_median": float(np.median(rel)), "rel_err_max": float(np.max(rel)),
+            "frac_within_1e-4": float(np.mean(rel <= 1e-4)), "reported_rel_error_median": float(np.median(est)),
+            "integrations": len(results)}
+
+
 # ------------------------------------------------- batched workload (C3)
 def c3_workload(n=4096, seed=1):
     """4096 independent Gaussian-peak integrals: dims U{1..4}, rule U{trapezoid,
@@ -113,9 +192,35 @@ def c3_workload(n=4096, seed=1):
     return out, exact
 
 
-def measure_batched(tq, dev, reps=5):
+def c3_cpu_baseline(specs, budget_s=6.0):
+    """The oracle port (numpy restatement of the reference's per-call grid
+    rules) over the integrals of the workload in order, until budget_s."""
+    import numpy as np
+
+    from oracle import grid as OG
+    from oracle import integrands as OI
+
+    rid = {"trapezoid": OG.TRAPEZOID, "simpson": OG.SIMPSON, "boole": OG.BOOLE, "gausslegendre": OG.GAUSS}
+    t0 = time.perf_counter()
+    k = 0
+    nodes = 0
+    while k < len(specs) and time.perf_counter() - t0 < budget_s:
+        rule, d, N, dom, a, u = specs[k]
+        params = np.concatenate([[1.0, 0.0], a, u])
+        OG.integrate(lambda x: OI.evaluate(2, params, x), rid[rule], d, N, dom)
+        nodes += OG.n_per_dim(OG.adjust_N(rid[rule], d, N), d) ** d
+        k += 1
+    t = time.perf_counter() - t0
+    return {"integrals_per_s": k / t, "unit": "integrals/s", "cores": cpu_cores_used(), "kind": "port",
+            "sample": f"the first {k} integrals of the workload ({nodes} nodes), numpy restatement of the "
+                      "reference's per-call grid rules, one process"}
+
+
+def measure_batched(tq, dev, L, peaks, reps=5):
     """Batched (one persistent launch) vs plain per-call integration of the
     4096-integral workload, fp32 and fp64; integrals/s and accuracy."""
+    import warnings
+
     import numpy as np
     import torch
     from torchquad_gb300 import batch as B
@@ -136,22 +241,13 @@ def measure_batched(tq, dev, reps=5):
         shape = bg.tuned_shape(plan)
         plan = bg.retile(plan, shape[2])
         vals = bg.run(plan, shape)
+        t_batch = timed_launches(torch, lambda: bg.run(plan, shape), reps)
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            vals = bg.run(plan, shape)
-        e1.record()
-        torch.cuda.synchronize()
-        t_batch = e0.elapsed_time(e1) / reps / 1000.0
         t0 = time.perf_counter()
         v_e2e = bg.integrate(fs, rules, Ns, doms).cpu()
         t_e2e = time.perf_counter() - t0
         vb = vals.double().cpu().numpy()
-        # plain per-call GPU form: one integrate() per integral, domains resident
         dtens = [torch.tensor(dm, dtype=dtype, device=dev) for dm in doms]
-        import warnings
-
         with warnings.catch_warnings():
             warnings.simplefilter("ignore")
             for i in range(64):  # warm-up
@@ -164,69 +260,126 @@ def measure_batched(tq, dev, reps=5):
             t_plain = time.perf_counter() - t0
         vp = np.array([float(x) for x in plain])
         rel = np.abs(vb - exact) / np.abs(exact)
-        out[name] = {
+        d = plan.desc_np
+        rows = int(np.sum(d["total"] // d["n"]))
+        rec = {
             "batched_integrals_per_s": len(specs) / t_batch,
             "batched_ms": t_batch * 1000.0,
             "batched_e2e_integrals_per_s": len(specs) / t_e2e,
             "plain_integrals_per_s": len(specs) / t_plain,
             "speedup_batched_vs_plain": t_plain / t_batch,
             "speedup_batched_e2e_vs_plain": t_plain / t_e2e,
-            "evals_per_s": plan.total_points / t_batch,
-            "total_points": plan.total_points,
+            "nodes_per_s": plan.total_points / t_batch,
+            "total_nodes": plan.total_points,
             "tuned_shape": {"block": shape[0], "strip": shape[1], "tile_points": shape[2], "ctas": shape[3]},
             "frac_within_1e-4_of_analytic": float(np.mean(rel <= 1e-4)),
+            "median_rel_err_vs_analytic": float(np.median(rel)),
             "max_rel_diff_batched_vs_plain": float(np.max(np.abs(vb - vp) / np.maximum(np.abs(vp), 1e-300))),
             "max_rel_diff_e2e_vs_resident": float(np.max(np.abs(v_e2e.double().numpy() - vb) / np.abs(vb))),
         }
+        if dtype == torch.float64:
+            # fp64 grids: the outer function once per grid row, every node a
+            # multiply by its row factor and a compensated add (3 FP64 ops)
+            rec["outer_evals_per_s"] = rows / t_batch
+            ach = 3.0 * plan.total_points / t_batch / 1e12
+            rec["roofline"] = {"bound": "fp64", "achieved": ach, "peak": peaks["fp64"], "unit": "TFLOP/s",
+                               "frac": ach / peaks["fp64"], "ops_per_node": 3,
+                               "peak_source": "FP64 FMA probe measured in this run"}
+        out[name] = rec
+    out["cpu_baseline"] = c3_cpu_baseline(specs)
     return out
 
 
-def sampler_traffic_bytes():
-    """DRAM bytes (read + write) of one fused-sampler launch of this workload,
-    from the committed ncu summary (profiles/), or None without one."""
-    p = Path(__file__).resolve().parent / "profiles" / "vegas_iteration_kernels_d6_N1e7_ncu.md"
-    try:
-        for line in p.read_text().splitlines():
-            if line.startswith("traffic_bytes_per_launch vegas_sample_kernel:"):
-                return int(line.split(":")[1])
-    except OSError:
-        pass
-    return None
-
-
-def measure_grid_cases(tq, dev, reps=20):
-    """The two grid-rule configurations: C1, plain Simpson, dim 3, 101 points
-    per dimension (N = 1,030,301), fp64, exp(x0+x1+x2) on [0,1]^3 against
-    (e-1)^3; C4, GaussLegendre, dim 4, 32 nodes per dimension, fp64,
-    cos(2 pi u + a.x) with u and the domain bounds requiring gradients:
-    forward and forward+backward times, gradients against central
-    differences (h = 1e-6).  Device-resident inputs, CUDA events."""
+def measure_grid_cases(tq, dev, L, peaks, flush, reps=20):
+    """C1: plain Simpson, dim 3, 101 points per dimension (N = 1,030,301),
+    fp64, exp(x0+x1+x2) on [0,1]^3 against (e-1)^3: the API call, the fused
+    kernel alone (C-ABI, CUDA events) with its FP64 roofline, and the
+    materialised path (any torch callable) with the HBM roofline of its two
+    kernels, also at 301^3 nodes.  C4: GaussLegendre, dim 4, 32 nodes per
+    dimension, fp64, cos(2 pi u + a.x) with u and the domain bounds
+    requiring gradients: forward and forward+backward times, gradients
+    against central differences (h = 1e-6), and the batch of 1024 such
+    integrals through the batched adjoint."""
     import numpy as np
     import torch
 
+    lib = L.lib()
+    hbm, hbm_src = hbm_peak()
+
     def timed(fn):
-        fn()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            r = fn()
-        e1.record()
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / reps, r
+        return timed_launches(torch, fn, reps) * 1000.0
 
     out = {}
+    # ---------------------------------------------------------------- C1
     dom = torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float64, device=dev)
     f1 = tq.ExpSum(3)
-    ms, v = timed(lambda: tq.Simpson().integrate(f1, 3, N=1_030_301, integration_domain=dom))
+    v = tq.Simpson().integrate(f1, 3, N=1_030_301, integration_domain=dom)
+    ms = timed(lambda: tq.Simpson().integrate(f1, 3, N=1_030_301, integration_domain=dom))
     exact = (math.e - 1.0) ** 3
     t0 = time.perf_counter()
     v_e2e = tq.Simpson().integrate(f1, 3, N=1_030_301,
                                    integration_domain=torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float64)).item()
     t_e2e = time.perf_counter() - t0
-    out["c1_simpson_d3_fp64"] = {"ms": ms, "evals_per_s": 1_030_301 / (ms / 1000.0), "e2e_ms": t_e2e * 1000.0,
-                                 "rel_err_vs_analytic": abs(v.item() - exact) / exact,
-                                 "e2e_value_matches": v_e2e == v.item()}
+    n, nodes = 101, 101**3
+    params = f1.device_params(dev)
+    res = torch.empty((), dtype=torch.float64, device=dev)
+    ws = torch.zeros(lib.tq_grid_fused_workspace_size(L.TQ_RULE_SIMPSON, 3, n), dtype=torch.uint8, device=dev)
+
+    def fused():
+        L.check(lib.tq_grid_fused(L.TQ_F64, L.TQ_RULE_SIMPSON, 3, n, dom.data_ptr(), None, None, f1.family,
+                                  params.data_ptr(), res.data_ptr(), L.TQ_F64, None, ws.data_ptr(), ws.numel(),
+                                  L.stream_handle()), "tq_grid_fused")
+
+    t_k = timed_launches(torch, fused, 200)
+    ach = 3.0 * nodes / t_k / 1e12
+    c1 = {"api_ms": ms, "kernel_us": t_k * 1e6, "nodes_per_s": nodes / t_k, "outer_evals_per_s": n**2 / t_k,
+          "e2e_ms": t_e2e * 1000.0, "rel_err_vs_analytic": abs(v.item() - exact) / exact,
+          "e2e_value_matches": v_e2e == v.item(),
+          "roofline": {"kernel": "grid_fused_kernel<double,double,SIMPSON,EXP_SUM>", "bound": "fp64",
+                       "achieved": ach, "peak": peaks["fp64"], "unit": "TFLOP/s", "frac": ach / peaks["fp64"],
+                       "ops_per_node": 3, "peak_source": "FP64 FMA probe measured in this run",
+                       "note": "fp64 rows: exp once per grid row; per node a multiply by the row factor, "
+                               "a weight multiply and an add (3 FP64 ops); 1.03M nodes is a few microseconds "
+                               "of work, so launch and reduction latency weigh in"}}
+    # materialised path: an arbitrary torch callable
+    fn = lambda x: torch.exp(x.sum(1))  # noqa: E731
+    c1["materialised_api_ms"] = timed(lambda: tq.Simpson().integrate(fn, 3, N=nodes, integration_domain=dom))
+    mat = {}
+    for tag, nn in (("n101", 101), ("n301", 301)):
+        tot = nn**3
+        pts = torch.empty((tot, 3), dtype=torch.float64, device=dev)
+
+        def gp():
+            L.check(lib.tq_grid_points(L.TQ_F64, L.TQ_RULE_SIMPSON, 3, nn, dom.data_ptr(), None, 0, tot,
+                                       pts.data_ptr(), L.stream_handle()), "tq_grid_points")
+
+        t_p = timed_launches(torch, gp, 10, flush)
+        fv = torch.exp(pts.sum(1))
+        acc = torch.zeros(2, dtype=torch.float64, device=dev)
+        wsw = torch.zeros(lib.tq_weighted_sum_workspace_size(tot, 1), dtype=torch.uint8, device=dev)
+
+        def wsum():
+            L.check(lib.tq_weighted_sum(L.TQ_F64, L.TQ_RULE_SIMPSON, 3, nn, dom.data_ptr(), None, 0, tot,
+                                        fv.data_ptr(), L.TQ_F64, 1, acc.data_ptr(), wsw.data_ptr(), wsw.numel(),
+                                        L.stream_handle()), "tq_weighted_sum")
+
+        t_w = timed_launches(torch, wsum, 10, flush)
+        bp, bw = tot * 3 * 8, tot * 8
+        mat[tag] = {
+            "nodes": tot,
+            "grid_points": {"us": t_p * 1e6, "bytes": bp, "achieved_gbs": bp / t_p / 1e9, "peak_gbs": hbm,
+                            "frac": bp / t_p / 1e9 / hbm, "bytes_per_node": 24},
+            "weighted_sum": {"us": t_w * 1e6, "bytes": bw, "achieved_gbs": bw / t_w / 1e9, "peak_gbs": hbm,
+                             "frac": bw / t_w / 1e9 / hbm, "bytes_per_node": 8,
+                             "fp64_pipe_frac": (tot / t_w / 1e12) * 2.0 / peaks["fp64"]},
+        }
+        del pts, fv
+    mat["peak_source"] = hbm_src
+    mat["l2"] = "flushed (256 MiB write) before every timed launch"
+    c1["materialised"] = mat
+    out["c1_simpson_d3_fp64"] = c1
+
+    # ---------------------------------------------------------------- C4
     a = [1.2, -2.1, 0.7, 2.6]
     u0 = 0.37
 
@@ -236,8 +389,8 @@ def measure_grid_cases(tq, dev, reps=20):
     u = torch.tensor(u0, dtype=torch.float64, device=dev, requires_grad=True)
     d4 = torch.tensor([[0.0, 1.0]] * 4, dtype=torch.float64, device=dev, requires_grad=True)
     with torch.no_grad():
-        ms_f, _ = timed(lambda: fwd(torch.tensor(u0, dtype=torch.float64, device=dev),
-                                    torch.tensor([[0.0, 1.0]] * 4, dtype=torch.float64, device=dev)))
+        ms_f = timed(lambda: fwd(torch.tensor(u0, dtype=torch.float64, device=dev),
+                                 torch.tensor([[0.0, 1.0]] * 4, dtype=torch.float64, device=dev)))
 
     def fb():
         u.grad = None
@@ -246,7 +399,7 @@ def measure_grid_cases(tq, dev, reps=20):
         val.backward()
         return val
 
-    ms_fb, _ = timed(fb)
+    ms_fb = timed(fb)
     g = np.concatenate([[u.grad.item()], d4.grad.double().cpu().numpy().ravel()])
     h = 1e-6
     fd = []
@@ -264,41 +417,141 @@ def measure_grid_cases(tq, dev, reps=20):
             fm = fwd(torch.tensor(um, dtype=torch.float64, device=dev), torch.tensor(dm, device=dev)).item()
             fd.append((fp - fm) / (2 * h))
     fd = np.array(fd)
-    out["c4_gausslegendre_d4_grad_fp64"] = {
-        "forward_ms": ms_f, "forward_backward_ms": ms_fb, "evals_per_s": 32**4 / (ms_f / 1000.0),
-        "max_abs_grad_diff_vs_central_differences": float(np.max(np.abs(g - fd))),
-        "max_abs_grad": float(np.max(np.abs(g)))}
+    c4 = {"forward_ms": ms_f, "forward_backward_ms": ms_fb, "nodes_per_s": 32**4 / (ms_f / 1000.0),
+          "max_abs_grad_diff_vs_central_differences": float(np.max(np.abs(g - fd))),
+          "max_abs_grad": float(np.max(np.abs(g)))}
+    c4["batch_1024"] = measure_c4_batch(tq, dev, peaks)
+    out["c4_gausslegendre_d4_grad_fp64"] = c4
     return out
 
 
-def measure_serving(tq, dev, n=120, rates=(1e2, 1e3, 1e4, 1e5)):
+def measure_c4_batch(tq, dev, peaks, m=1024):
+    """1024 differentiation integrals (GL dim 4, 32 nodes, fp64, random a, u)
+    with gradients: the batched adjoint (device time, and end to end from
+    host parameters through backward) against the per-call form and the
+    numpy port on the host."""
+    import numpy as np
+    import torch
+    from torchquad_gb300 import batch as B
+
+    from oracle import grad as OGR
+
+    rng = np.random.default_rng(4)
+    a = rng.uniform(-3.0, 3.0, (m, 4))
+    us = rng.uniform(0.0, 1.0, m)
+    fs = [tq.Oscillatory(4, a=a[i].tolist(), b=float(us[i])) for i in range(m)]
+    bg = B.BatchedGrid(dtype=torch.float64)
+    plan = bg.plan(fs, ["gausslegendre"] * m, [32**4] * m, [[[0.0, 1.0]] * 4] * m, tile_points=65536)
+    t_dev = timed_launches(torch, lambda: bg.adjoint(plan), 5)
+    vals, gdom, gpar = bg.adjoint(plan)
+
+    def e2e():
+        u = torch.tensor(us, dtype=torch.float64, requires_grad=True)
+        d = torch.tensor([[[0.0, 1.0]] * 4] * m, dtype=torch.float64, requires_grad=True)
+        ff = [tq.Oscillatory(4, a=a[i].tolist(), b=u[i]) for i in range(m)]
+        v = bg.integrate(ff, ["gausslegendre"] * m, [32**4] * m, list(d))
+        v.sum().backward()
+        return float(v.detach().sum()), u.grad, d.grad
+
+    e2e()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e()
+    t_e2e = time.perf_counter() - t0
+    # per-call form: integrate + backward, one integral at a time
+    k = 64
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    diffs = []
+    for i in range(k):
+        ui = torch.tensor(us[i], dtype=torch.float64, device=dev, requires_grad=True)
+        di = torch.tensor([[0.0, 1.0]] * 4, dtype=torch.float64, device=dev, requires_grad=True)
+        vi = tq.GaussLegendre().integrate(tq.Oscillatory(4, a=a[i].tolist(), b=ui), 4, N=32**4, integration_domain=di)
+        vi.backward()
+        diffs.append(abs(vi.item() - vals[i].item()) / max(1.0, abs(vi.item())))
+    torch.cuda.synchronize()
+    t_plain = (time.perf_counter() - t0) / k
+    # host port: value and gradient in numpy (one core), bounded sample
+    t0 = time.perf_counter()
+    j = 0
+    while j < m and time.perf_counter() - t0 < 5.0:
+        OGR.value_and_grad(3, np.concatenate([[1.0, us[j]], a[j], np.zeros(4)]), OGR.GAUSS, 4, 32, [[0.0, 1.0]] * 4)
+        j += 1
+    t_cpu = (time.perf_counter() - t0) / j
+    nodes = m * 32**4
+    ach = 10.0 * nodes / t_dev / 1e12
+    return {
+        "batched_device_ms": t_dev * 1e3, "batched_fwd_bwd_integrals_per_s": m / t_dev,
+        "batched_e2e_ms": t_e2e * 1e3, "batched_e2e_integrals_per_s": m / t_e2e,
+        "plain_fwd_bwd_integrals_per_s": 1.0 / t_plain,
+        "speedup_batched_vs_plain": t_plain * m / t_dev, "speedup_batched_e2e_vs_plain": t_plain * m / t_e2e,
+        "max_rel_diff_batched_vs_plain_sample": float(max(diffs)),
+        "roofline": {"kernel": "batch_adjoint_kernel<double,4>", "bound": "fp64", "achieved": ach,
+                     "peak": peaks["fp64"], "unit": "TFLOP/s", "frac": ach / peaks["fp64"], "ops_per_node": 10,
+                     "peak_source": "FP64 FMA probe measured in this run",
+                     "note": "per node: cos/sin of the angle sum from row factor and table (4 ops), two "
+                             "weight products and four gradient accumulations"},
+        "cpu_baseline": {"integrals_per_s": 1.0 / t_cpu, "unit": "integrals/s (value + gradient)",
+                         "cores": cpu_cores_used(), "kind": "port",
+                         "sample": f"{j} of the integrals, numpy gradient of the discrete rule "
+                                   "(oracle/grad.py), one process"},
+    }
+
+
+def _serving_accuracy(reqs):
+    import numpy as np
+
+    ratios, within = [], []
+    for r in reqs:
+        ex = r.integrand.exact(r.domain)
+        err = abs(r.result - ex) / max(abs(ex), 1e-300)
+        ratios.append(err / r.eps_rel)
+        within.append(err <= r.eps_rel)
+    return {"frac_within_target_rel_err": float(np.mean(within)),
+            "median_rel_err_over_target": float(np.median(ratios)),
+            "p90_rel_err_over_target": float(np.percentile(ratios, 90))}
+
+
+def measure_serving(tq, dev, n=1000, rates=(1e2, 1e3, 1e4, 1e5)):
     """Poisson request streams (MC / VEGAS / Simpson, dims 1-10, N log-uniform
     1e4..1e8, target relative error 1e-3..1e-5, seed 2) through the serving
-    loop: p50/p99 latency and integrals/s per arrival rate, and the same
-    requests through the plain per-call API one after the other."""
+    loop: p50/p99 latency, integrals/s, evaluations and accuracy against the
+    closed-form integral per arrival rate.  Matched work: Monte Carlo runs to
+    its N as MonteCarlo.integrate does (the per-call form has no stopping
+    rule); the early-stop variant, which stops Monte Carlo at its target
+    error, is reported beside it at the highest rate.  The same requests
+    then go through the plain per-call API one after the other."""
     import warnings
 
+    import numpy as np
     import torch
-    from torchquad_gb300.serving import IntegrationRequest, IntegrationServer, poisson_stream
+    from torchquad_gb300.serving import IntegrationServer, poisson_stream
 
     out = {"requests_per_rate": n}
-    for rate in rates:
+
+    def serve(rate, early):
         stream = poisson_stream(n, rate, seed=2)
-        with IntegrationServer(max_active=64) as srv:
+        with IntegrationServer(max_active=64, mc_early_stop=early) as srv:
             t0 = time.perf_counter()
-            futs = []
             for t_arr, req in stream:
                 delay = t0 + t_arr - time.perf_counter()
                 if delay > 0:
                     time.sleep(delay)
-                futs.append(srv.submit(req))
-            srv.drain(timeout=600)
+                srv.submit(req)
+            srv.drain(timeout=900)
             st = srv.stats()
-        out[f"rate_{int(rate)}"] = {k: st[k] for k in ("p50_ms", "p99_ms", "integrals_per_s", "peak_active", "evals")}
+            reqs = list(srv.completed)
+        rec = {k: st[k] for k in ("p50_ms", "p99_ms", "integrals_per_s", "peak_active", "evals")}
+        rec.update(_serving_accuracy(reqs))
+        return rec
+
+    for rate in rates:
+        out[f"rate_{int(rate)}"] = serve(rate, False)
+    out[f"rate_{int(rates[-1])}_mc_early_stop"] = serve(rates[-1], True)
     # plain per-call path, same requests, back to back
     stream = poisson_stream(n, rates[-1], seed=2)
     cls = {"montecarlo": tq.MonteCarlo, "vegas": tq.VEGAS, "simpson": tq.Simpson}
-    lat = []
+    lat, evals, done = [], 0, []
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         torch.cuda.synchronize()
@@ -309,16 +562,58 @@ def measure_serving(tq, dev, n=120, rates=(1e2, 1e3, 1e4, 1e5)):
             kw = {"seed": r.seed} if r.method != "simpson" else {}
             if r.method == "vegas":
                 kw["eps_rel"] = r.eps_rel
-            cls[r.method]().integrate(r.integrand, r.dim, N=r.N, integration_domain=dom, **kw).item()
+            integ = cls[r.method]()
+            r.result = integ.integrate(r.integrand, r.dim, N=r.N, integration_domain=dom, **kw).item()
+            evals += int(integ._nr_of_fevals)
             lat.append(time.perf_counter() - t1)
+            done.append(r)
         t_plain = time.perf_counter() - t0
+    out["plain_per_call"] = {"integrals_per_s": n / t_plain, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                             "p99_ms": float(np.percentile(lat, 99) * 1e3), "evals": evals,
+                             **_serving_accuracy(done)}
+    best = max(v["integrals_per_s"] for k, v in out.items() if k.startswith("rate_") and "early" not in k)
+    out["served_vs_plain_integrals_per_s_matched_work"] = best / (n / t_plain)
+    out["served_early_stop_vs_plain_integrals_per_s"] = (
+        out[f"rate_{int(rates[-1])}_mc_early_stop"]["integrals_per_s"] / (n / t_plain))
+    out["cpu_baseline"] = serving_cpu_baseline(n)
+    return out
+
+
+def serving_cpu_baseline(n, budget_s=8.0, max_n=2_000_000):
+    """The oracle port on the requests of the stream with N <= max_n, in
+    arrival order, until budget_s (Monte Carlo: the same Philox draws;
+    VEGAS and Simpson: the numpy restatements)."""
     import numpy as np
 
-    out["plain_per_call"] = {"integrals_per_s": n / t_plain, "p50_ms": float(np.percentile(lat, 50) * 1e3),
-                             "p99_ms": float(np.percentile(lat, 99) * 1e3)}
-    best = max(v["integrals_per_s"] for k, v in out.items() if k.startswith("rate_"))
-    out["served_vs_plain_integrals_per_s"] = best / (n / t_plain)
-    return out
+    from oracle import grid as OG
+    from oracle import integrands as OI
+    from oracle import mc as OM
+    from oracle import philox as OP
+    from oracle import vegas as OV
+    from torchquad_gb300.serving import poisson_stream
+
+    t0 = time.perf_counter()
+    k = 0
+    for _, r in poisson_stream(n, 1e5, seed=2):
+        if time.perf_counter() - t0 > budget_s:
+            break
+        if r.N > max_n:
+            continue
+        p = r.integrand.params_numpy()
+        fn = lambda x, fam=r.integrand.family, p=p: OI.evaluate(fam, p, x)  # noqa: E731
+        dt = np.float32
+        if r.method == "montecarlo":
+            u = OP.uniform(r.seed, 0, 0, r.N * r.dim, dt).reshape(r.N, r.dim)
+            OM.integrate(fn, r.dim, r.N, r.domain, u)
+        elif r.method == "vegas":
+            OV.Vegas().integrate(fn, r.dim, r.N, r.domain, OP.ReplayStream(r.seed), dt=dt, eps_rel=r.eps_rel)
+        else:
+            OG.integrate(fn, OG.SIMPSON, r.dim, r.N, r.domain, dt=dt)
+        k += 1
+    t = time.perf_counter() - t0
+    return {"integrals_per_s": k / t, "unit": "integrals/s", "cores": cpu_cores_used(), "kind": "port",
+            "sample": f"{k} requests of the stream with N <= {max_n}, in arrival order, numpy restatements "
+                      "of the reference, one process (the larger requests take minutes each on one core)"}
 
 
 # ----------------------------------------------------------- CPU (oracle)
@@ -489,7 +784,7 @@ def run_gpu(args):
 
     # ---- device-resident inputs
     clocks = ClockSampler(os.environ.get("TQ_CLOCKS_CSV", f"/tmp/tq_clocks_{rank}.csv"), local)
-    step_ms, evals = [], 0
+    step_ms, evals, results, errors = [], 0, [], []
     with clocks:
         # keep the GPU under the same load for about a second first, so the
         # 200 ms clock samples cover the load the timed steps run under
@@ -500,7 +795,11 @@ def run_gpu(args):
             k_soak += 1
         barrier()
         launches0 = L.launches[0]
+        v = r = None
         for k in range(args.steps):
+            # a user's loop drops the previous integrator before the next
+            # (one that keeps it alive gets a second pooled device plan)
+            v = r = None
             flush.fill_(k & 0xFF)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
@@ -509,6 +808,8 @@ def run_gpu(args):
             torch.cuda.synchronize()
             step_ms.append(e0.elapsed_time(e1))
             evals += v._nr_of_fevals
+            results.append(r.item())
+            errors.append(float(v._get_error()))
         barrier()
     launches = L.launches[0] - launches0
     t_local = sum(step_ms) / 1000.0
@@ -561,6 +862,7 @@ def run_gpu(args):
     V.FORCE_EAGER[0] = True
     try:
         for k in range(args.steps):
+            v = None
             flush.fill_(k & 0xFF)
             n0 = len(sampler_events)
             v, _ = one(rank_seed(rank, k), domain_dev)
@@ -605,19 +907,9 @@ def run_gpu(args):
         assert math.isfinite(val)
     barrier()
 
-    # ---- FP32 FMA peak (measured in this run)
-    out = torch.zeros(1, dtype=torch.float32, device=dev)
-    flops = ctypes.c_double(0.0)
-    peaks = []
-    for _ in range(3):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        L.check(L.lib().tq_fp32_fma_probe(4096, 8, out.data_ptr(), ctypes.byref(flops), L.stream_handle()),
-                "tq_fp32_fma_probe")
-        e1.record()
-        torch.cuda.synchronize()
-        peaks.append(flops.value / (e0.elapsed_time(e1) / 1000.0) / 1e12)
-    fp32_peak = max(peaks)
+    # ---- FP32 / FP64 FMA peaks (measured in this run)
+    peaks = fp_peaks(L, torch)
+    fp32_peak = peaks["fp32"]
 
     # ---- reduce over ranks
     t_max, e2e_t, tot_evals, tot_e2e = reduce_over_ranks(t_local, sum(e2e_ms) / 1000.0, evals, e2e_evals,
@@ -668,20 +960,23 @@ def run_gpu(args):
             "peak": fp32_peak,
             "unit": "TFLOP/s",
             "frac": achieved / fp32_peak,
-            "traffic": sampler_traffic_bytes(),
+            # one ncu capture of the sampler gives the DRAM bytes of a launch;
+            # that figure is in the committed profile summary, not measured here
+            "traffic": None,
             "peak_source": "FP32 FMA probe kernel measured in this run (MEASURED_PEAKS.json has HBM and bf16 only)",
             "points_per_launch": pts,
             "avg_launch_us": avg_ms * 1000.0,
             "flops_per_point": flops_per_point,
         },
+        "accuracy": c2_accuracy(results, errors),
         "iteration_steps_us": step_us,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "evals_per_step": tot_evals / (args.steps * ws),
     }
     if not args.no_batched:
-        line["grid_cases"] = measure_grid_cases(tq, dev)
-        line["batched"] = measure_batched(tq, dev)
+        line["grid_cases"] = measure_grid_cases(tq, dev, L, peaks, flush)
+        line["batched"] = measure_batched(tq, dev, L, peaks)
     if not args.no_serving:
         line["serving"] = measure_serving(tq, dev)
     if not args.no_cpu_baseline:

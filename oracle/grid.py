@@ -9,8 +9,10 @@ TRAPEZOID, SIMPSON, BOOLE, GAUSS = 0, 1, 2, 3
 
 
 def _fma(x, y, z, dt):
+    """x * y + z rounded once to dt (x, y, z arrays or scalars of dt): the
+    product and sum are formed in extended precision first."""
     ld = np.longdouble
-    return dt(ld(x) * ld(y) + ld(z))
+    return (np.asarray(x, dtype=ld) * np.asarray(y, dtype=ld) + np.asarray(z, dtype=ld)).astype(dt)
 
 
 def linspace(a, b, n, dt):
@@ -19,8 +21,8 @@ def linspace(a, b, n, dt):
     a, b = dt(a), dt(b)
     step = dt((b - a) / dt(n - 1))
     i = np.arange(n)
-    lo = np.array([_fma(step, dt(k), a, dt) for k in i[: n // 2]], dtype=dt)
-    hi = np.array([_fma(-step, dt(n - 1 - k), b, dt) for k in i[n // 2 :]], dtype=dt)
+    lo = _fma(step, i[: n // 2].astype(dt), a, dt)
+    hi = _fma(-step, (n - 1 - i[n // 2:]).astype(dt), b, dt)
     return np.concatenate([lo, hi]).astype(dt)
 
 

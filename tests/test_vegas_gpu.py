@@ -636,3 +636,19 @@ def test_integrators_keep_their_own_state(cuda):
     a.integrate(f, 3, N=200_000, integration_domain=dom, seed=5)
     assert torch.allclose(d.map.x_edges, xb, rtol=0, atol=1e-6)
     assert torch.allclose(d.strat.dh, dhb, rtol=1e-5, atol=0)
+
+
+def test_more_live_integrators_than_pooled_plans(cuda):
+    """Six integrators of one shape alive at once (more than the plans kept
+    per shape): the ones whose plan is handed on get a private copy of
+    their state first, so every one still reads its own map and dh."""
+    f = tq.GaussianPeak.normal(2, 0.5, 0.1)
+    dom = torch.tensor([[0.0, 1.0]] * 2, dtype=torch.float64, device=cuda)
+    vs, snaps = [], []
+    for seed in range(6):
+        v = tq.VEGAS()
+        v.integrate(f, 2, N=50_000, integration_domain=dom, seed=100 + seed)
+        vs.append(v)
+        snaps.append((v.map.x_edges.clone(), v.strat.dh.clone(), list(v.results)))
+    for v, (xe, dh, res) in zip(vs, snaps):
+        assert torch.equal(v.map.x_edges, xe) and torch.equal(v.strat.dh, dh) and v.results == res

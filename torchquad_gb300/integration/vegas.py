@@ -50,8 +50,9 @@ class _FusedPlan:
     the results back once per call.  The first use runs the same launches
     eagerly, with the loop on the host."""
 
-    _cache = {}
-    _MAX = 8
+    _cache = {}  # shape key -> [plans]
+    _MAX = 8  # shape keys kept
+    _PER_KEY = 4  # plans per shape key (integrators of one shape alive at once)
 
     def __init__(self, dev, family, use_grid_improve, use_warmup, ns):
         self.dev, self.family = dev, family
@@ -63,15 +64,36 @@ class _FusedPlan:
         self._fork, self._join = torch.cuda.Event(), torch.cuda.Event()
 
     @classmethod
-    def get(cls, make_dev, shape_key, family, use_grid_improve, use_warmup, ns, max_iterations):
+    def get(cls, make_dev, shape_key, family, use_grid_improve, use_warmup, ns, max_iterations, requester):
+        """A plan of this shape for `requester`: its own from an earlier call,
+        else one no live integrator holds, else a new one (up to _PER_KEY);
+        when all are held, the least recently used one, whose integrator
+        first gets a private copy of its state."""
         key = (*shape_key, family, bool(use_grid_improve), bool(use_warmup), ns, max_iterations)
-        plan = cls._cache.get(key)
-        if plan is None:
-            plan = cls(make_dev(), family, use_grid_improve, use_warmup, ns)
+        plans = cls._cache.get(key)
+        if plans is None:
             if len(cls._cache) >= cls._MAX:
                 cls._cache.pop(next(iter(cls._cache)))
-            cls._cache[key] = plan
-        return plan
+            plans = cls._cache[key] = []
+        free = None
+        for p in plans:
+            owner = p.owner() if p.owner is not None else None
+            if owner is requester:
+                return p
+            if owner is None and free is None:
+                free = p
+        if free is not None:
+            return free
+        if len(plans) < cls._PER_KEY:
+            p = cls(make_dev(), family, use_grid_improve, use_warmup, ns)
+            plans.append(p)
+            return p
+        p = plans.pop(0)  # least recently handed out
+        plans.append(p)
+        owner = p.owner() if p.owner is not None else None
+        if owner is not None and owner._dev is p.dev:
+            owner._detach_state()
+        return p
 
     # launch sequences
     def _warm_seq(self):
@@ -235,7 +257,7 @@ class VEGAS(BaseIntegrator):
                                     stats_slots=max_iterations + 10),
                 (str(device), torch.cuda.current_stream().cuda_stream, dim, self.dtype,
                  N_intervals, n_strat), fn.family,
-                use_grid_improve, use_warmup, ns, max_iterations)
+                use_grid_improve, use_warmup, ns, max_iterations, self)
             self._dev = plan.dev
         else:
             if domain is None:
@@ -267,12 +289,9 @@ class VEGAS(BaseIntegrator):
         _starting_N) and the RNG offset."""
         rng = self.rng
         dev = plan.dev
-        # The plan's state is shared by every VEGAS of this shape; the VEGAS
-        # that used it last gets its own copy before it is overwritten, so its
-        # map and stratification stay its own (as in the reference).
-        prev = plan.owner() if plan.owner is not None else None
-        if prev is not None and prev is not self and prev._dev is dev:
-            prev._detach_state()
+        # The plan's device state now holds this integrator's map and
+        # stratification (as the reference's instances own theirs); no other
+        # live integrator is handed this plan while this one holds it.
         plan.owner = weakref.ref(self)
         if domain_values is None:
             dev.set_domain(domain)
