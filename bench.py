@@ -989,6 +989,74 @@ def run_gpu(args):
     return 0
 
 
+def run_case(name):
+    """One launch of a named kernel workload after one warm-up launch, for
+    profiling a single kernel (ncu -k ... -c 1):
+      c1_fused        fused Simpson, dim 3, 101^3 nodes, fp64, exp(x0+x1+x2)
+      points_n301     tq_grid_points, Simpson, dim 3, 301^3 nodes, fp64
+      wsum_n301       tq_weighted_sum of those 301^3 fp64 values
+      c3_fp64         the 4096-integral batch, fp64, one tq_batch_grid launch
+      c4_batch        1024 differentiation integrals, one tq_batch_grid_adjoint
+      c2              one plain VEGAS integration (dim 6, N = 1e7, 50 intervals),
+                      its kernels launched eagerly"""
+    import torch
+
+    import torchquad_gb300 as tq
+    from torchquad_gb300 import _lib as L
+    from torchquad_gb300 import batch as B
+
+    dev = torch.device("cuda", 0)
+    lib = L.lib()
+    runs = []
+    if name == "c1_fused":
+        dom = torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float64, device=dev)
+        f = tq.ExpSum(3)
+        runs = [lambda: tq.Simpson().integrate(f, 3, N=101**3, integration_domain=dom)]
+    elif name in ("points_n301", "wsum_n301"):
+        dom = torch.tensor([[0.0, 1.0]] * 3, dtype=torch.float64, device=dev)
+        tot = 301**3
+        pts = torch.empty((tot, 3), dtype=torch.float64, device=dev)
+        fv = torch.rand(tot, dtype=torch.float64, device=dev)
+        acc = torch.zeros(2, dtype=torch.float64, device=dev)
+        ws = torch.zeros(lib.tq_weighted_sum_workspace_size(tot, 1), dtype=torch.uint8, device=dev)
+        if name == "points_n301":
+            runs = [lambda: L.check(lib.tq_grid_points(L.TQ_F64, L.TQ_RULE_SIMPSON, 3, 301, dom.data_ptr(), None, 0,
+                                                       tot, pts.data_ptr(), L.stream_handle()), "pts")]
+        else:
+            runs = [lambda: L.check(lib.tq_weighted_sum(L.TQ_F64, L.TQ_RULE_SIMPSON, 3, 301, dom.data_ptr(), None, 0,
+                                                        tot, fv.data_ptr(), L.TQ_F64, 1, acc.data_ptr(),
+                                                        ws.data_ptr(), ws.numel(), L.stream_handle()), "wsum")]
+    elif name == "c3_fp64":
+        specs, _ = c3_workload()
+        fs = [tq.GaussianPeak(d, a=a.tolist(), u=u.tolist()) for (_, d, _, _, a, u) in specs]
+        bg = B.BatchedGrid(dtype=torch.float64, autotune=False, block=128, strip=16, tile_points=32768)
+        plan = bg.plan(fs, [sp[0] for sp in specs], [sp[2] for sp in specs], [sp[3] for sp in specs])
+        runs = [lambda: bg.run(plan)]
+    elif name == "c4_batch":
+        import numpy as np
+
+        rng = np.random.default_rng(4)
+        a, us = rng.uniform(-3.0, 3.0, (1024, 4)), rng.uniform(0.0, 1.0, 1024)
+        fs = [tq.Oscillatory(4, a=a[i].tolist(), b=float(us[i])) for i in range(1024)]
+        bg = B.BatchedGrid(dtype=torch.float64)
+        plan = bg.plan(fs, ["gausslegendre"] * 1024, [32**4] * 1024, [[[0.0, 1.0]] * 4] * 1024, tile_points=65536)
+        runs = [lambda: bg.adjoint(plan)]
+    elif name == "c2":
+        from torchquad_gb300.integration import vegas as V
+
+        f = tq.GaussianPeak.normal(DIM, 0.5, SIGMA)
+        dom = torch.tensor([[0.0, 1.0]] * DIM, dtype=torch.float32, device=dev)
+        V.FORCE_EAGER[0] = True
+        runs = [lambda: tq.VEGAS().integrate(f, DIM, N=N_EVALS, integration_domain=dom, seed=0, n_intervals=N_BINS)]
+    else:
+        raise SystemExit(f"unknown case {name}")
+    for fn in runs * 2:  # warm-up launch, then the profiled one
+        fn()
+    torch.cuda.synchronize()
+    print(json.dumps({"case": name, "ok": True}))
+    return 0
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -999,7 +1067,13 @@ def main():
     p.add_argument("--no-batched", action="store_true", help="skip the batched-vs-plain measurement")
     p.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     p.add_argument("--cpu-seconds", type=float, default=20.0)
+    p.add_argument("--case", default=None, help="run one named kernel workload twice (for ncu), see run_case")
     args = p.parse_args()
+    if args.case:
+        from __graft_entry__ import build
+
+        build()
+        return run_case(args.case)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

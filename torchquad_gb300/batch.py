@@ -405,6 +405,21 @@ class _BatchedAdjointFn(torch.autograd.Function):
         return g_par, g_dom, None, None
 
 
+def integrate_domains(integrand, rule, N, domains, dtype=torch.float64):
+    """One built-in integrand over many domains in one launch: the batched-
+    domain pattern of the reference tutorial's custom Gaussian integrator
+    (a [batch, 2] domain tensor through _resize_roots), here for any rule and
+    dimension.  domains: [batch, dim, 2] (tensor or nested lists); returns
+    [batch] values of dtype (differentiable when the domains or the
+    integrand's parameters require gradients)."""
+    if isinstance(domains, torch.Tensor):
+        doms = list(domains) if domains.dim() == 3 else list(domains.reshape(-1, 1, 2))
+    else:
+        doms = [np.asarray(d, dtype=np.float64).reshape(-1, 2) for d in domains]
+    m = len(doms)
+    return BatchedGrid(dtype=dtype, autotune=False).integrate([integrand] * m, [rule] * m, [N] * m, doms)
+
+
 def integrate_batch(integrands, rules, Ns, domains, dtype=torch.float64, autotune=True):
     """Functional form of BatchedGrid(dtype).integrate(...)."""
     return BatchedGrid(dtype=dtype, autotune=autotune).integrate(integrands, rules, Ns, domains)

@@ -47,7 +47,7 @@ struct BatchArgs {
 template <typename T, int FAM, int P>
 __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t tile, int64_t tile0,
                              const Geo<T>& g, const Family<T>& fam, const uint64_t* rstride,
-                             InnerTab* tab) {
+                             InnerTab* tab, RowTab* rt, FastDiv* fdn) {
   const int dim = d.dim, rule = d.rule, last = dim - 1;
   const int64_t n = d.n;
   const int n32 = (int)n;
@@ -66,6 +66,14 @@ __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t til
     if (dim >= 2 && n <= kTabMax) use_tab = build_inner_tab<FAM>(*tab, g, fam, last, n32, gl, rule, gln, glw);
   }
   Acc acc{0.0, 0.0};
+  if constexpr (std::is_same<T, double>::value) {
+    if (use_tab) {
+      if (threadIdx.x == 0) *fdn = make_fastdiv((uint32_t)n);
+      __syncthreads();
+      acc = tab_rows_sum<FAM>(g, fam, *tab, *rt, dim, rule, gl, n, *fdn, gln, glw, begin, end);
+      return block_reduce<256>(acc);
+    }
+  }
   for (int64_t base = begin + (int64_t)threadIdx.x * P; base < end; base += (int64_t)blockDim.x * P) {
     uint64_t row = (uint64_t)base / (uint64_t)n;
     int jl = (int)(base - (int64_t)row * n);
@@ -132,9 +140,13 @@ __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
   __shared__ BatchDesc d;
   __shared__ int64_t tile0;
   InnerTab* tab = nullptr;
+  RowTab* rt = nullptr;
+  __shared__ FastDiv fdn;
   if constexpr (std::is_same<T, double>::value) {
     __shared__ InnerTab tab_s;
+    __shared__ RowTab rt_s;
     tab = &tab_s;
+    rt = &rt_s;
   }
   for (int64_t tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
     if (threadIdx.x == 0) {
@@ -158,16 +170,16 @@ __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
     Acc acc{CUDART_NAN, 0.0};  // an unknown family (rejected on the host) gives NaN
     switch (fam.id) {
       case TQ_FN_EXP_SUM:
-        acc = grid_tile_sum<T, TQ_FN_EXP_SUM, P>(a, d, tile, tile0, g, fam, rstride, tab);
+        acc = grid_tile_sum<T, TQ_FN_EXP_SUM, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn);
         break;
       case TQ_FN_GAUSSIAN:
-        acc = grid_tile_sum<T, TQ_FN_GAUSSIAN, P>(a, d, tile, tile0, g, fam, rstride, tab);
+        acc = grid_tile_sum<T, TQ_FN_GAUSSIAN, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn);
         break;
       case TQ_FN_OSCILLATORY:
-        acc = grid_tile_sum<T, TQ_FN_OSCILLATORY, P>(a, d, tile, tile0, g, fam, rstride, tab);
+        acc = grid_tile_sum<T, TQ_FN_OSCILLATORY, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn);
         break;
       case TQ_FN_SUM_SIN:
-        acc = grid_tile_sum<T, TQ_FN_SUM_SIN, P>(a, d, tile, tile0, g, fam, rstride, tab);
+        acc = grid_tile_sum<T, TQ_FN_SUM_SIN, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn);
         break;
       default:
         break;

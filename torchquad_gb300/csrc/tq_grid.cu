@@ -134,8 +134,21 @@ __global__ void __launch_bounds__(kBlock, 2) grid_fused_kernel(FusedArgs args) {
   }
 
   Acc acc{0.0, 0.0};
+  bool rows_done = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if (use_tab) {
+      // a contiguous node range per CTA, rows in groups of 32 per warp
+      __shared__ FastDiv fdn;
+      __shared__ RowTab rt;
+      if (threadIdx.x == 0) fdn = make_fastdiv((uint32_t)n);
+      __syncthreads();
+      const int64_t b0 = total * (int64_t)blockIdx.x / gridDim.x, b1 = total * ((int64_t)blockIdx.x + 1) / gridDim.x;
+      if (b1 > b0) acc = tab_rows_sum<FAM>(g, fam, *tab, rt, dim, args.rule, GL, n, fdn, gl_nodes, gl_w, b0, b1);
+      rows_done = true;
+    }
+  }
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * P; base < total;
+  for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * P; base < total && !rows_done;
        base += nthreads * P) {
     uint64_t row;
     int jl;

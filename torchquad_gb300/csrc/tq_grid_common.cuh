@@ -170,6 +170,107 @@ __device__ __forceinline__ double tab_value(const RowFactor& f, double t1, doubl
   return f.r1 * t1;
 }
 
+// Weighted sum over the nodes [begin, end) of an fp64 grid whose last
+// dimension has a usable table.  The CTA first forms the outer state of
+// each grid row in the range (a chunk of up to kRowChunk rows at a time:
+// digits by multiply-high division, separable sum, outer weight and row
+// factor; one outer-function evaluation per row, one thread per row) in
+// shared memory; then its threads walk strips of kTabP consecutive nodes:
+// value = row factor x table entry, one fused multiply-add per node into
+// the row-segment sum, one per row segment into the strip sum, and a
+// compensated add per strip.  Returns the thread's compensated partial.
+constexpr int kRowChunk = 512;
+constexpr int kTabP = 32;
+
+struct RowTab {
+  double p[kRowChunk], q[kRowChunk], w[kRowChunk], s[kRowChunk];
+  int ok[kRowChunk];
+};
+
+template <int FAM>
+__device__ Acc tab_rows_sum(const Geo<double>& g, const Family<double>& fam, const InnerTab& tab, RowTab& rt,
+                            int dim, int rule, bool gl, int64_t n, const FastDiv& fdn,
+                            const double* __restrict__ gl_nodes, const double* __restrict__ gl_w, int64_t begin,
+                            int64_t end) {
+  const int last = dim - 1;
+  const int n32 = (int)n;
+  const int64_t row_first = begin / n, row_last = (end - 1) / n;
+  const bool small = end <= (int64_t)0xffffffffll;
+  const double wlast = g.wscale[last];
+  Acc acc{0.0, 0.0};
+  for (int64_t rc = row_first; rc <= row_last; rc += kRowChunk) {
+    const int nr = (int)min((int64_t)kRowChunk, row_last - rc + 1);
+    __syncthreads();  // the previous chunk's rows are no longer read
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+      double t[kMaxDim], wk[kMaxDim];
+      uint64_t r = (uint64_t)(rc + i);
+      for (int k = last - 1; k >= 0; --k) {
+        uint64_t digit;
+        if (small) {
+          const uint32_t qq = fdiv((uint32_t)r, fdn);
+          digit = (uint32_t)r - qq * fdn.d;
+          r = qq;
+        } else {
+          const uint64_t qq = r / (uint64_t)n;
+          digit = r - qq * (uint64_t)n;
+          r = qq;
+        }
+        const double x = gl ? __dadd_rn(__dmul_rn(g.half[k], __ldg(gl_nodes + digit)), g.mid[k])
+                            : linspace_node<double>(g.a[k], g.b[k], g.step[k], n, (int64_t)digit);
+        t[k] = fam_term<FAM, double>(fam, k, x);
+        wk[k] = g.wscale[k] * (gl ? __ldg(gl_w + digit) : (double)nc_int(rule, (int64_t)digit, n));
+      }
+      double sv = 0.0, wo = 1.0;
+      for (int k = 0; k < last; ++k) {
+        sv = (k == 0) ? t[k] : sv + t[k];
+        wo *= wk[k];
+      }
+      const RowFactor rf = row_factor<FAM>(fam, sv);
+      rt.p[i] = rf.r1;
+      rt.q[i] = rf.r2;
+      rt.ok[i] = rf.ok;
+      rt.s[i] = sv;
+      rt.w[i] = wo * wlast;
+    }
+    __syncthreads();
+    const int64_t c0 = max(begin, rc * n), c1 = min(end, (rc + nr) * n);
+    for (int64_t base = c0 + (int64_t)threadIdx.x * kTabP; base < c1; base += (int64_t)blockDim.x * kTabP) {
+      const int cnt = (int)min((int64_t)kTabP, c1 - base);
+      int ri, j;
+      if (small) {
+        const uint32_t qq = fdiv((uint32_t)base, fdn);
+        ri = (int)((int64_t)qq - rc);
+        j = (int)((uint32_t)base - qq * fdn.d);
+      } else {
+        const int64_t qq = base / n;
+        ri = (int)(qq - rc);
+        j = (int)(base - qq * n);
+      }
+      double seg = 0.0, ga = 0.0;
+      for (int e = 0; e < cnt; ++e) {
+        double v;
+        if (rt.ok[ri]) {
+          v = tab_value<FAM>(RowFactor{rt.p[ri], rt.q[ri], true}, tab.t1[j], tab.t2[j]);
+        } else {  // a row whose factor is not a normal number: the direct formula
+          const double x = gl ? __dadd_rn(__dmul_rn(g.half[last], __ldg(gl_nodes + j)), g.mid[last])
+                              : linspace_node<double>(g.a[last], g.b[last], g.step[last], n, j);
+          v = fam_outer<FAM, double>(fam, rt.s[ri] + fam_term<FAM, double>(fam, last, x));
+        }
+        seg = fma(tab.w[j], v, seg);
+        if (++j == n32) {
+          ga = fma(seg, rt.w[ri], ga);
+          seg = 0.0;
+          j = 0;
+          ++ri;
+        }
+      }
+      if (j != 0) ga = fma(seg, rt.w[ri], ga);
+      acc_add(acc, ga);
+    }
+  }
+  return acc;
+}
+
 // ------------------------------------------------ adjoint of the families
 // F(s) and F'(s) of the outer function, without the factor c.
 template <int FAM, typename T>
