@@ -824,6 +824,8 @@ def run_gpu(args):
     originals = {name: getattr(V.VegasDevice, name) for name in other_events}
 
     def timed_iterate(self, *a, **k):
+        if torch.cuda.is_current_stream_capturing():  # a graph being recorded runs nothing
+            return orig_iter(self, *a, **k)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         orig_iter(self, *a, **k)
@@ -834,6 +836,8 @@ def run_gpu(args):
         fn = originals[name]
 
         def wrapper(self, *a, **k):
+            if torch.cuda.is_current_stream_capturing():
+                return fn(self, *a, **k)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             out = fn(self, *a, **k)

@@ -294,9 +294,9 @@ typedef struct tq_vegas_state {
                          * advance it by the blocks their draws consumed       */
   double* stats;        /* [n_stat_slots][4]: result, sigma2, points, unused   */
   int64_t n_stat_slots; /* rows of stats                                       */
-  int32_t* flags;       /* [4]: [0] map updates skipped (all-zero weights),
+  int32_t* flags;       /* [8]: [0] map updates skipped (all-zero weights),
                          * [1] infinite edges repaired, [2] unrepairable edges,
-                         * [3] a finish found its slot >= n_stat_slots       */
+                         * [3] a finish found its slot >= n_stat_slots      */
   double* scalars;      /* [4]: [0] sum of the unnormalised dh              */
   const void* domain;   /* [d][2] dtype                                        */
   int64_t* control;     /* [16] per-iteration inputs read by the kernels, so
@@ -312,7 +312,9 @@ typedef struct tq_vegas_state {
                          * [10] warm-up evaluations, [11] iterations done,
                          * [12] stop reason (0 go on, 1 accuracy reached,
                          * 2 evaluation budget, 3 iteration limit, 4 out of
-                         * statistics slots), [13] evaluations so far,
+                         * statistics slots, 5 / 6 int() of an infinite / NaN
+                         * value, where the reference raises), [13]
+                         * evaluations so far,
                          * [14] 1 while cube_start is split (see
                          * tq_vegas_get_nh_split)                          */
 } tq_vegas_state;
@@ -377,6 +379,7 @@ int tq_vegas_begin_run(const tq_vegas_state* st, const tq_vegas_run* run, double
  * cudaGraphConditionalHandle of the WHILE node this runs in, set to 0 to
  * stop. */
 int tq_vegas_abort_test(const tq_vegas_state* st, uint64_t cond_handle, void* stream);
+
 
 /* Capture helpers for a device-side loop (CUDA graph conditional nodes).
  * During a stream capture on `stream`, tq_capture_while_begin appends a

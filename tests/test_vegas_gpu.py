@@ -652,3 +652,4 @@ def test_more_live_integrators_than_pooled_plans(cuda):
         snaps.append((v.map.x_edges.clone(), v.strat.dh.clone(), list(v.results)))
     for v, (xe, dh, res) in zip(vs, snaps):
         assert torch.equal(v.map.x_edges, xe) and torch.equal(v.strat.dh, dh) and v.results == res
+

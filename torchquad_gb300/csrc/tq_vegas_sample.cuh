@@ -82,15 +82,15 @@ __device__ __forceinline__ T strat_y(int pos, T u, T nsf) {
 
 // cube_start[c] for c < n_cubes; pre != nullptr: cube_start is split
 // (kCtlSplit) and pre holds the offsets of its kBlock-cube blocks.
-__device__ __forceinline__ int64_t cube_start_at(const int64_t* __restrict__ cs,
-                                                 const int64_t* __restrict__ pre, int64_t c) {
-  return pre ? cs[c] + pre[c / kBlock] : cs[c];
+// Loads through L2 (__ldcg), never the read-only cache: the prefix is
+// rewritten by other kernels between samplings of the same state.
+__device__ __forceinline__ int64_t cube_start_at(const int64_t* cs, const int64_t* pre, int64_t c) {
+  return pre ? __ldcg(cs + c) + __ldcg(pre + c / kBlock) : __ldcg(cs + c);
 }
 
 // Largest c in [0, n) with cube_start[c] <= target; strictly increasing,
 // cube_start[0] = 0.  One warp, 32-ary search with coalesced probes.
-__device__ __forceinline__ int64_t warp_find_cube(const int64_t* __restrict__ cs,
-                                                  const int64_t* __restrict__ pre, int64_t n,
+__device__ __forceinline__ int64_t warp_find_cube(const int64_t* cs, const int64_t* pre, int64_t n,
                                                   int64_t target) {
   const int lane = threadIdx.x & 31;
   int64_t lo = 0, hi = n;
@@ -224,8 +224,10 @@ struct DrawBlocks {
 // D > 0: the dimension is known at compile time (fully unrolled point
 // loops, D interval indices in registers); D = 0: any dimension up to
 // kMaxDim from the state.
+// The sampler as a device body: CTA bid of nblk CTAs taking part (the
+// per-launch kernel below, or one state's share of a batched launch).
 template <typename T, int FAM, bool WARM, int D>
-__global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kernel(SampleArgs a) {
+__device__ void sample_body(const SampleArgs& a, unsigned bid, unsigned nblk) {
   constexpr int KD = D > 0 ? D : kMaxDim;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ Family<T> fam;
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
     }
   }
 
-  const int64_t M = WARM ? a.n_samples : st.cube_start[st.n_cubes];
+  const int64_t M = WARM ? a.n_samples : __ldcg(st.cube_start + st.n_cubes);
   const uint64_t offset = *st.rng_offset;
   const uint64_t seed = (uint64_t)st.control[3], sid = (uint64_t)st.control[4];
   const int64_t ns = st.n_strat;
@@ -276,8 +278,8 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
   // global loads) runs before the barrier, beside the loads of the map and
   // the integrand parameters.
   const int64_t n_tiles = (M + 31) / 32;
-  const int64_t n_warps = (int64_t)gridDim.x * kWarps;
-  const int64_t gw = (int64_t)blockIdx.x * kWarps + warp;
+  const int64_t n_warps = (int64_t)nblk * kWarps;
+  const int64_t gw = (int64_t)bid * kWarps + warp;
   const int64_t t_begin = gw * n_tiles / n_warps, t_end = (gw + 1) * n_tiles / n_warps;
   int64_t c0 = 0;  // cube of the tile's first point
   const int64_t* pre = (!WARM && st.control[kCtlSplit] != 0) ? a.block_pre : nullptr;
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
     if (!WARM) {
       const int64_t cl = c0 + lane;
       csl = cl < st.n_cubes ? cube_start_at(st.cube_start, pre, cl)
-                            : (cl == st.n_cubes ? st.cube_start[cl] : INT64_MAX);
+                            : (cl == st.n_cubes ? __ldcg(st.cube_start + cl) : INT64_MAX);
       // bit p: a cube starts at point j0 + p (cube c0 holds j0, so the
       // starts of cubes c0 + 1.. lie after j0); the slot of point j0 + p
       // (largest l with cube_start[c0 + l] <= j) counts the starts in bits 1..p
@@ -443,10 +445,15 @@ __global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kern
   // The last CTA advances the RNG offset.  It reads nothing the other CTAs
   // wrote (each read the offset before taking its ticket), so no fence.
   __syncthreads();
-  if (threadIdx.x == 0 && atomicAdd(a.ticket, 1u) == gridDim.x - 1) {
+  if (threadIdx.x == 0 && atomicAdd(a.ticket, 1u) == nblk - 1) {
     *st.rng_offset = offset + ((uint64_t)M * d + PB - 1) / PB;
     *a.ticket = 0u;
   }
+}
+
+template <typename T, int FAM, bool WARM, int D>
+__global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_sample_kernel(SampleArgs a) {
+  sample_body<T, FAM, WARM, D>(a, blockIdx.x, gridDim.x);
 }
 
 // fp32 states with 1 <= dim <= 8: the dimension-specialised sampler

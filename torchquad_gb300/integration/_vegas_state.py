@@ -129,11 +129,11 @@ class VegasDevice:
         except TypeError:
             self._domain_src = None
 
-    def begin_run(self, nevals, N, n_inc, max_it, warm_evals, eps_rel, eps_abs, seed, sid, offset,
-                  params, domain_values=None):
-        """Per-call inputs of a device-side run (one launch): control
-        fields, the RNG offset, the integrand parameters (fp64 numpy) and,
-        if given, the domain as host values ([dim][2] floats)."""
+    def fill_run(self, nevals, N, n_inc, max_it, warm_evals, eps_rel, eps_abs, seed, sid, offset,
+                 params, domain_values=None):
+        """The tq_vegas_run struct of a device-side run: control fields, the
+        RNG offset, the integrand parameters (fp64 numpy) and, if given, the
+        domain as host values ([dim][2] floats)."""
         r = self._run
         r.nevals_exp, r.N, r.N_increment = int(nevals), int(N), int(n_inc)
         r.max_iterations, r.warm_evals = int(max_it), int(warm_evals)
@@ -152,6 +152,14 @@ class VegasDevice:
             self._domain_src = None
         else:
             r.n_domain = 0
+        return r
+
+    def begin_run(self, nevals, N, n_inc, max_it, warm_evals, eps_rel, eps_abs, seed, sid, offset,
+                  params, domain_values=None):
+        """Per-call inputs of a device-side run written by one launch (see
+        fill_run)."""
+        r = self.fill_run(nevals, N, n_inc, max_it, warm_evals, eps_rel, eps_abs, seed, sid, offset, params,
+                          domain_values)
         L.check(L.lib().tq_vegas_begin_run(self.ref, ctypes.byref(r), self.params.data_ptr(),
                                            L.stream_handle()), "tq_vegas_begin_run")
         L.count_launches(1)

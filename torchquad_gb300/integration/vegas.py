@@ -297,11 +297,17 @@ class VEGAS(BaseIntegrator):
             dev.set_domain(domain)
         warm_evals = 5 * plan.ns if use_warmup else 0
         dev.dh_pending = False
-        dev.begin_run(self._starting_N, self.N, self._N_increment, self._max_iterations, warm_evals,
-                      self._eps_rel, self._eps_abs, rng.seed, rng.stream_id, rng.offset,
-                      fn.params_numpy(), domain_values)
+        run_args = (self._starting_N, self.N, self._N_increment, self._max_iterations, warm_evals,
+                    self._eps_rel, self._eps_abs, rng.seed, rng.stream_id, rng.offset, fn.params_numpy(),
+                    domain_values)
         self.alpha = ALPHA
+        dev.begin_run(*run_args)
         plan.run()
+        return self._collect_fused(dev, rng)
+
+    def _collect_fused(self, dev, rng):
+        """The reference's attributes from the state's host copy after a
+        fused run, and the result."""
         c = dev.host_control
         stop = int(c[L.VC_STOP])
         if stop == 4:
