@@ -380,6 +380,72 @@ int tq_vegas_begin_run(const tq_vegas_state* st, const tq_vegas_run* run, double
  * stop. */
 int tq_vegas_abort_test(const tq_vegas_state* st, uint64_t cond_handle, void* stream);
 
+/* ---- many VEGAS states per launch (tq_vegas_batch.cu) ---------------------
+ * A batch of resident VEGAS states advanced together: each phase of the
+ * fused integration (the launches a single state's graph makes, see
+ * tq_vegas_begin_run .. tq_vegas_abort_test) is one launch for every state
+ * of the batch, whose CTAs are split among the states in proportion to
+ * their work.  No counterpart in the reference, whose VEGAS.integrate
+ * (vegas.py:100-160) runs one integral per call; each state follows the
+ * reference's algorithm exactly as a single fused run does.  States of a
+ * batch share the dtype; maps have at most 1024 intervals per dimension. */
+enum {
+  TQ_VB_BEGIN = 0,      /* the run inputs (runs[i]) and the state reset      */
+  TQ_VB_WARM = 1,       /* one warm-up sampling pass                         */
+  TQ_VB_MAP = 2,        /* the warm-up map update (one CTA per dimension)    */
+  TQ_VB_NH = 3,         /* get_NH, cube prefix left split                    */
+  TQ_VB_SAMPLE = 4,     /* one stratified sampling iteration                 */
+  TQ_VB_FINISH = 5,     /* end of the iteration, beside the map update       */
+  TQ_VB_ABORT = 6,      /* the abort test after a block of five iterations;
+                         * the last CTA sets the graph condition: 1 while some
+                         * state goes on                                     */
+  TQ_VB_PHASES = 7
+};
+
+/* One state of a batch. */
+typedef struct tq_vegas_item {
+  tq_vegas_state st;        /* the state (its arrays in device memory)        */
+  double* params;           /* [2 + 2 dim] device: the integrand parameters
+                             * the run writes and the samplers read          */
+  void* workspace;          /* tq_vegas_workspace_size(&st) device bytes      */
+  size_t workspace_bytes;
+  int64_t warm_samples;     /* points per warm-up pass (0: no warm-up)        */
+  int64_t expected_points;  /* points of an iteration, sizes its CTA share    */
+  int32_t family;           /* TQ_FN_* (built-in integrand)                   */
+  int32_t use_grid_improve; /* map histogram and map update per iteration     */
+  int32_t use_warmup;       /* five warm-up passes with map updates          */
+  int32_t pad;
+} tq_vegas_item;
+
+/* What the launches of a batch need on the host (filled by
+ * tq_vegas_batch_build). */
+typedef struct tq_vegas_batch_info {
+  int64_t n_items;
+  int32_t dtype;
+  int32_t pad;
+  int64_t ctas[TQ_VB_PHASES]; /* CTAs of each phase's launch                 */
+  int64_t smem[TQ_VB_PHASES]; /* dynamic shared memory of each launch        */
+} tq_vegas_batch_info;
+
+/* Device bytes of the table of the batch items[n_items] (host); 0 if an
+ * item is invalid. */
+size_t tq_vegas_batch_table_size(const tq_vegas_item* items, int64_t n_items);
+
+/* Checks items[n_items] (host), builds the batch's table in `table` (device,
+ * tq_vegas_batch_table_size bytes; copied on `stream`, which is then
+ * synchronised) and fills *info. */
+int tq_vegas_batch_build(const tq_vegas_item* items, int64_t n_items, void* table, size_t table_bytes,
+                         tq_vegas_batch_info* info, void* stream);
+
+/* Runs `phase` for every state of the batch in one launch.  runs[n_items]
+ * (device; TQ_VB_BEGIN only): each state's run inputs, as
+ * tq_vegas_begin_run takes them.  States stopped by their abort test
+ * (control[12] != 0) skip TQ_VB_NH .. TQ_VB_ABORT.  cond_handle (ABORT):
+ * the cudaGraphConditionalHandle of the WHILE node the launch runs in, or 0. */
+int tq_vegas_batch_phase(const tq_vegas_batch_info* info, const void* table, int phase,
+                         const tq_vegas_run* runs, double alpha, double beta, uint64_t cond_handle,
+                         void* stream);
+
 
 /* Capture helpers for a device-side loop (CUDA graph conditional nodes).
  * During a stream capture on `stream`, tq_capture_while_begin appends a
@@ -434,8 +500,9 @@ int tq_vegas_get_nh_split(const tq_vegas_state* st, void* workspace, size_t work
  * (get_X/get_Jac, vegas_map.py:44-74), f = integrand(domain(x)) * volume;
  * accumulates the map weights/counts (if use_grid_improve) and the per-cube
  * sums jf/jf2 (accumulate_weight, vegas_stratification.py:46-70).
- * max_points sizes the launch (an upper bound of cube_start[n_cubes] or 0
- * for a grid that covers any count).  Advances *st->rng_offset. */
+ * max_points sizes the launch: about two 32-point tiles per warp for that
+ * many points, at most one full wave of CTAs (0: one full wave); any count
+ * of points is covered whatever the size.  Advances *st->rng_offset. */
 int tq_vegas_iterate_fused(const tq_vegas_state* st, int family, const double* params,
                            int use_grid_improve, int64_t max_points, void* workspace,
                            size_t workspace_bytes, void* stream);

@@ -653,3 +653,17 @@ def test_more_live_integrators_than_pooled_plans(cuda):
     for v, (xe, dh, res) in zip(vs, snaps):
         assert torch.equal(v.map.x_edges, xe) and torch.equal(v.strat.dh, dh) and v.results == res
 
+
+
+def test_fused_sampler_dynamic_smem_near_default_limit(cuda):
+    """fp32 d=5 with 94 map intervals: the sampler's dynamic shared memory
+    (47.8 KB: map edges plus per-warp histograms) and its static shared
+    memory together pass the 48 KB a launch gets without the opt-in, which
+    is made for it."""
+    f = tq.SumSin(5, a=2.0)
+    dom = torch.tensor([[0.0, 1.0]] * 5, dtype=torch.float32, device=cuda)
+    v = tq.VEGAS()
+    r = v.integrate(f, 5, N=23_672, integration_domain=dom, seed=7)
+    exact = f.exact(dom)
+    assert v.map.N_intervals == 94
+    assert abs(float(r) - exact) < 0.05 * abs(exact)

@@ -90,6 +90,39 @@ class VegasRun(ctypes.Structure):
 # control block fields of the device-side VEGAS loop (tq_vegas_state.control)
 VC_NEVALS, VC_SLOT, VC_IT, VC_STOP, VC_EVALS = 0, 1, 11, 12, 13
 
+# phases of a batch of VEGAS states (tq_vegas_batch_phase)
+VB_BEGIN, VB_WARM, VB_MAP, VB_NH, VB_SAMPLE, VB_FINISH, VB_ABORT = range(7)
+VB_PHASES = 7
+
+
+class VegasItem(ctypes.Structure):
+    """Mirror of ``tq_vegas_item`` (include/torchquad_gb300.h)."""
+
+    _fields_ = [
+        ("st", VegasState),
+        ("params", c_void_p),
+        ("workspace", c_void_p),
+        ("workspace_bytes", c_size_t),
+        ("warm_samples", c_int64),
+        ("expected_points", c_int64),
+        ("family", ctypes.c_int32),
+        ("use_grid_improve", ctypes.c_int32),
+        ("use_warmup", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+
+class VegasBatchInfo(ctypes.Structure):
+    """Mirror of ``tq_vegas_batch_info`` (include/torchquad_gb300.h)."""
+
+    _fields_ = [
+        ("n_items", c_int64),
+        ("dtype", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+        ("ctas", c_int64 * VB_PHASES),
+        ("smem", c_int64 * VB_PHASES),
+    ]
+
 
 _VS = POINTER(VegasState)
 
@@ -156,6 +189,11 @@ SIGNATURES = {
     "tq_vegas_set_control": (c_int, [_VS, c_int, c_int64, c_int64, c_int64, c_uint64, c_uint64, c_void_p]),
     "tq_vegas_begin_run": (c_int, [_VS, POINTER(VegasRun), c_void_p, c_void_p]),
     "tq_vegas_abort_test": (c_int, [_VS, c_uint64, c_void_p]),
+    "tq_vegas_batch_table_size": (c_size_t, [POINTER(VegasItem), c_int64]),
+    "tq_vegas_batch_build": (
+        c_int, [POINTER(VegasItem), c_int64, c_void_p, c_size_t, POINTER(VegasBatchInfo), c_void_p]),
+    "tq_vegas_batch_phase": (
+        c_int, [POINTER(VegasBatchInfo), c_void_p, c_int, c_void_p, c_double, c_double, c_uint64, c_void_p]),
     "tq_capture_while_begin": (c_int, [c_void_p, c_void_p, POINTER(c_uint64)]),
     "tq_capture_while_end": (c_int, [c_void_p]),
     "tq_vegas_warmup_fused": (c_int, [_VS, c_int, c_void_p, c_int64, c_void_p, c_size_t, c_void_p]),
@@ -249,6 +287,20 @@ def require_cuda() -> torch.device:
 
 def stream_handle() -> int:
     return torch.cuda.current_stream().cuda_stream
+
+
+def body_stream(device, avoid=()) -> torch.cuda.Stream:
+    """A stream for the body of a conditional node captured from the current
+    stream.  torch hands out streams from a small per-device pool in turn,
+    so a new stream can be the very stream being captured; another one is
+    taken then (the body must be captured on a stream of its own).  Streams
+    in `avoid` (torch streams) are skipped too."""
+    taken = {torch.cuda.current_stream(device).cuda_stream} | {a.cuda_stream for a in avoid}
+    for _ in range(64):
+        s = torch.cuda.Stream(device=device)
+        if s.cuda_stream not in taken:
+            return s
+    raise RuntimeError("no CUDA stream distinct from the capturing stream")
 
 
 def dtype_code(dtype: torch.dtype) -> int:

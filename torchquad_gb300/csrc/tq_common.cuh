@@ -24,6 +24,18 @@ int launch_status();                // TQ_OK or TQ_ERR_CUDA for the last launch
 int sm_count();                     // SMs of the current device (cached)
 int grid_for(const void* kernel, int block, size_t smem, int64_t work_blocks);
 
+// Opt-in for dynamic shared memory: a launch gets 48 KB of shared memory
+// (static and dynamic together) unless the kernel's attribute allows more,
+// so the attribute is raised whenever the dynamic part alone exceeds 32 KB
+// (the static shared memory of the kernels launched this way stays below
+// 16 KB).
+template <typename K>
+inline int opt_in_smem(K kfn, size_t smem) {
+  if (smem <= 32 * 1024) return TQ_OK;
+  const cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return e == cudaSuccess ? TQ_OK : set_cuda_error(e);
+}
+
 inline bool valid_dtype(int d) { return d == TQ_F32 || d == TQ_F64; }
 inline size_t dtype_size(int d) { return d == TQ_F64 ? 8 : 4; }
 

@@ -733,11 +733,7 @@ static int launch_sample(const tq_vegas_state* st, int family, const double* par
 #define TQ_SAMPLE_LAUNCH(T, WARMB)                                                          \
   {                                                                                         \
     auto kfn = vegas_sample_kernel<T, FAM, WARMB, 0>;                                       \
-    if (smem > 48 * 1024) {                                                                 \
-      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                           (int)smem);                                      \
-      if (e != cudaSuccess) return set_cuda_error(e);                                       \
-    }                                                                                       \
+    { const int orc = opt_in_smem(kfn, smem); if (orc != TQ_OK) return orc; }                   \
     kfn<<<grid, kTile, smem, s>>>(a);                                                       \
   }
   TQ_DISPATCH_FAMILY(family, FAM, {
@@ -810,20 +806,16 @@ static int launch_update_map(const tq_vegas_state* st, double alpha, void* works
 #define TQ_ROWS_LAUNCH(T)                                                                      \
   {                                                                                            \
     auto kfn = vegas_map_rows_kernel<T>;                                                       \
-    if (smem > 48 * 1024) {                                                                    \
-      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
-                                           (int)smem);                                         \
-      if (e != cudaSuccess) return set_cuda_error(e);                                          \
-    }                                                                                          \
+    { const int orc = opt_in_smem(kfn, smem); if (orc != TQ_OK) return orc; }                   \
     kfn<<<st->dim, kRowThreads, smem, s>>>(*st, alpha, smooth_out, ws.t_map);                  \
   }
   if (st->dtype == TQ_F64) {
     TQ_ROWS_LAUNCH(double)
   } else {
     auto kfn = vegas_map_rows_f32_kernel;
-    if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return set_cuda_error(e);
+    {
+      const int orc = opt_in_smem(kfn, smem);
+      if (orc != TQ_OK) return orc;
     }
     kfn<<<st->dim, kRowThreads, smem, s>>>(*st, alpha, smooth_out, ws.t_map);
   }
@@ -909,11 +901,7 @@ extern "C" int tq_vegas_finish_update_map(const tq_vegas_state* st, double beta,
 #define TQ_FINISH_MAP(T)                                                                      \
   {                                                                                           \
     auto kfn = vegas_finish_map_kernel<T>;                                                    \
-    if (smem > 48 * 1024) {                                                                   \
-      cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
-                                           (int)smem);                                        \
-      if (e != cudaSuccess) return set_cuda_error(e);                                         \
-    }                                                                                         \
+    { const int orc = opt_in_smem(kfn, smem); if (orc != TQ_OK) return orc; }                   \
     kfn<<<g, kBlock, smem, s>>>(a, alpha, ws.t_map);                                          \
   }
   if (st->dtype == TQ_F64)

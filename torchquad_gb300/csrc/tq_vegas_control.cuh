@@ -40,9 +40,10 @@ struct RunArgs {
   int dtype;
 };
 
-static __device__ void begin_run_body(const RunArgs& a) {
-  int64_t* c = a.control;
-  const tq_vegas_run& r = a.run;
+// The run inputs r into a state's control block, RNG offset, parameter
+// vector and domain buffer (one thread).
+static __device__ void begin_run_from(const tq_vegas_run& r, int64_t* c, uint64_t* rng_offset,
+                                      double* params_dev, void* domain, int dtype) {
   c[kCtlNevals] = r.nevals_exp;
   c[kCtlSeed] = (int64_t)r.seed;
   c[kCtlStream] = (int64_t)r.stream_id;
@@ -55,14 +56,18 @@ static __device__ void begin_run_body(const RunArgs& a) {
   c[kCtlIt] = 0;
   c[kCtlStop] = 0;
   c[kCtlEvals] = r.warm_evals;
-  *a.rng_offset = r.rng_offset;
-  for (int i = 0; i < r.n_params; ++i) a.params_dev[i] = r.params[i];
+  *rng_offset = r.rng_offset;
+  for (int i = 0; i < r.n_params; ++i) params_dev[i] = r.params[i];
   for (int i = 0; i < r.n_domain; ++i) {
-    if (a.dtype == TQ_F64)
-      ((double*)a.domain)[i] = r.domain[i];
+    if (dtype == TQ_F64)
+      ((double*)domain)[i] = r.domain[i];
     else
-      ((float*)a.domain)[i] = __double2float_rn(r.domain[i]);
+      ((float*)domain)[i] = __double2float_rn(r.domain[i]);
   }
+}
+
+static __device__ void begin_run_body(const RunArgs& a) {
+  begin_run_from(a.run, a.control, a.rng_offset, a.params_dev, a.domain, a.dtype);
 }
 
 // Arithmetic of the abort test in the state's dtype, each operation rounded

@@ -61,6 +61,7 @@ extern "C" int tq_capture_while_begin(void* stream, void* body_stream, uint64_t*
   size_t n_deps = 0;
   cudaError_t e = cudaStreamGetCaptureInfo(s, &status, nullptr, &graph, &deps, &edges, &n_deps);
   if (e != cudaSuccess) return set_cuda_error(e);
+  if (status == cudaStreamCaptureStatusInvalidated) return set_cuda_error(cudaErrorStreamCaptureInvalidated);
   if (status != cudaStreamCaptureStatusActive || !graph) return TQ_ERR_ARG;
   cudaGraphConditionalHandle h;
   e = cudaGraphConditionalHandleCreate(&h, graph, 1u, cudaGraphCondAssignDefault);

@@ -212,6 +212,29 @@ __device__ __forceinline__ void warp_hist_add(H* hw, unsigned* hc, int key, bool
   }
 }
 
+// The integrand inside the sampler with every operation rounded on its own
+// (no FMA contraction), as the reference's separate tensor operations round
+// them: the dimension-specialised and the generic samplers (and the batched
+// one) then compute the same values.
+template <int FAM, typename T>
+__device__ __forceinline__ T vegas_term(const Family<T>& f, int k, T x) {
+  if (FAM == TQ_FN_GAUSSIAN) {
+    const T d = sub_rn(x, f.u[k]);
+    return mul_rn(f.a[k], mul_rn(d, d));
+  } else if (FAM == TQ_FN_SUM_SIN) {
+    return sin(mul_rn(f.a[k], x));
+  } else {
+    return mul_rn(f.a[k], x);
+  }
+}
+template <int FAM, typename T>
+__device__ __forceinline__ T vegas_outer(const Family<T>& f, T s) {
+  if (FAM == TQ_FN_EXP_SUM) return mul_rn(f.c, exp(add_rn(s, f.b)));
+  if (FAM == TQ_FN_GAUSSIAN) return mul_rn(f.c, exp(-s));
+  if (FAM == TQ_FN_OSCILLATORY) return mul_rn(f.c, cos(add_rn(mul_rn((T)(2.0 * CUDART_PI), f.b), s)));
+  return mul_rn(f.c, s);  // TQ_FN_SUM_SIN
+}
+
 // Philox blocks a point's D draws can touch: a point's first draw sits at
 // word (j*D) mod PB of its first block, at most PB - gcd(D, PB).
 __host__ __device__ constexpr int gcd_c(int a, int b) { return b == 0 ? a : gcd_c(b, a % b); }
@@ -376,11 +399,11 @@ __device__ void sample_body(const SampleArgs& a, unsigned bid, unsigned nblk) {
           jac = mul_rn(jac, jf_k);
           // vegas.py:110: fn(x * domain_sizes + domain_starts) * domain_volume
           const T xt = add_rn(mul_rn(x, wid[k]), lo[k]);
-          const T g = fam_term<FAM, T>(fam, k, xt);
-          s = (k == 0) ? g : s + g;
+          const T g = vegas_term<FAM, T>(fam, k, xt);
+          s = (k == 0) ? g : add_rn(s, g);
         }
       }
-      const T f = mul_rn(fam_outer<FAM, T>(fam, s), volume);
+      const T f = mul_rn(vegas_outer<FAM, T>(fam, s), volume);
       const T jfv = mul_rn(f, jac);
       jfd = (H)jfv;
       jf2 = jfd * jfd;

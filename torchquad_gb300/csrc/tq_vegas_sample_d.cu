@@ -9,10 +9,8 @@ namespace tq {
 template <int FAM, bool WARM, int D>
 static int launch_dims(const SampleArgs& a, unsigned grid, size_t smem, cudaStream_t s) {
   auto kfn = vegas_sample_kernel<float, FAM, WARM, D>;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return set_cuda_error(e);
-  }
+  const int rc = opt_in_smem(kfn, smem);
+  if (rc != TQ_OK) return rc;
   kfn<<<grid, kTile, smem, s>>>(a);
   return launch_status();
 }

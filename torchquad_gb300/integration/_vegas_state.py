@@ -22,7 +22,7 @@ def n_strat_for(N_increment, dim):
 
 
 class VegasDevice:
-    def __init__(self, dim, dtype, n_bins, n_strat, device, domain=None, stats_slots=64):
+    def __init__(self, dim, dtype, n_bins, n_strat, device, domain=None, stats_slots=64, readback=None):
         if dim < 1 or dim > L.TQ_MAX_DIM:
             raise ValueError(f"VEGAS kernels support 1 <= dim <= {L.TQ_MAX_DIM}, got {dim}")
         self.dim, self.dtype, self.device = dim, dtype, device
@@ -39,7 +39,10 @@ class VegasDevice:
         self.neval = torch.zeros((self.n_cubes,), dtype=torch.int64, device=device)
         self.cube_start = torch.zeros((self.n_cubes + 1,), dtype=torch.int64, device=device)
         self.scalars = torch.zeros((4,), dtype=torch.float64, device=device)
-        self._alloc_readback(max(1, stats_slots))
+        if readback is not None:  # rows of a batch's shared read-back buffers
+            self._set_readback(*readback)
+        else:
+            self._alloc_readback(max(1, stats_slots))
         self.params = torch.zeros((2 + 2 * dim,), dtype=torch.float64, device=device)
         if domain is None:
             domain = torch.tensor([[0.0, 1.0]] * dim, **f)
@@ -88,16 +91,28 @@ class VegasDevice:
     # padding, stats [slots][4] (fp64).
     _RB_CONTROL, _RB_FLAGS, _RB_OFFSET, _RB_STATS = 0, 16, 20, 24
 
+    @classmethod
+    def readback_words(cls, slots):
+        """int64 words of the read-back buffer of a state with `slots`
+        statistics rows."""
+        return cls._RB_STATS + 4 * slots
+
     def _alloc_readback(self, slots, old=None):
-        buf = torch.zeros((self._RB_STATS + 4 * slots,), dtype=torch.int64, device=self.device)
+        buf = torch.zeros((self.readback_words(slots),), dtype=torch.int64, device=self.device)
         if old is not None:
             buf[: old.numel()] = old
+        self._set_readback(buf, torch.empty(buf.shape, dtype=torch.int64, pin_memory=True))
+
+    def _set_readback(self, buf, host):
+        """Device int64 buffer `buf` and its pinned host copy `host` (same
+        length) hold control, flags, RNG offset and statistics."""
+        slots = (buf.numel() - self._RB_STATS) // 4
         self._rb = buf
         self.control = buf[self._RB_CONTROL:self._RB_FLAGS]
         self.flags = buf[self._RB_FLAGS:self._RB_OFFSET].view(torch.int32)
         self.rng_offset = buf[self._RB_OFFSET:self._RB_OFFSET + 1]
         self.stats = buf[self._RB_STATS:].view(torch.float64).view(slots, 4)
-        self._rb_host = torch.empty(buf.shape, dtype=torch.int64, pin_memory=True)
+        self._rb_host = host
         h = self._rb_host.numpy()
         self.host_control = h[self._RB_CONTROL:self._RB_FLAGS]
         self.host_flags = h[self._RB_FLAGS:self._RB_OFFSET].view("int32")
@@ -191,6 +206,13 @@ class VegasDevice:
         L.check(L.lib().tq_vegas_warmup_fused(self.ref, family, params.data_ptr(), n_samples, p, n,
                                               L.stream_handle()), "tq_vegas_warmup_fused")
         L.count_launches(1)
+
+    def points_hint(self, n_inc):
+        """Points an iteration is sized for (tq_vegas_iterate_fused's
+        max_points): N_increment, at least two per cube.  The single-state
+        graphs and the batched ones size the sampler alike, so a state gets
+        the same CTA split (and the same fp32 partial sums) either way."""
+        return max(int(n_inc), 2 * self.n_cubes)
 
     def iterate_fused(self, family, params, use_grid_improve, max_points=0):
         p, n = self._ws()

@@ -54,9 +54,10 @@ class _FusedPlan:
     _MAX = 8  # shape keys kept
     _PER_KEY = 4  # plans per shape key (integrators of one shape alive at once)
 
-    def __init__(self, dev, family, use_grid_improve, use_warmup, ns):
+    def __init__(self, dev, family, use_grid_improve, use_warmup, ns, n_inc):
         self.dev, self.family = dev, family
         self.use_grid_improve, self.use_warmup, self.ns = use_grid_improve, use_warmup, ns
+        self.points_hint = dev.points_hint(n_inc)
         self.uses = 0
         self.graph = None
         self.owner = None  # weak reference to the VEGAS whose results the state holds
@@ -64,12 +65,12 @@ class _FusedPlan:
         self._fork, self._join = torch.cuda.Event(), torch.cuda.Event()
 
     @classmethod
-    def get(cls, make_dev, shape_key, family, use_grid_improve, use_warmup, ns, max_iterations, requester):
+    def get(cls, make_dev, shape_key, family, use_grid_improve, use_warmup, ns, n_inc, max_iterations, requester):
         """A plan of this shape for `requester`: its own from an earlier call,
         else one no live integrator holds, else a new one (up to _PER_KEY);
         when all are held, the least recently used one, whose integrator
         first gets a private copy of its state."""
-        key = (*shape_key, family, bool(use_grid_improve), bool(use_warmup), ns, max_iterations)
+        key = (*shape_key, family, bool(use_grid_improve), bool(use_warmup), ns, n_inc, max_iterations)
         plans = cls._cache.get(key)
         if plans is None:
             if len(cls._cache) >= cls._MAX:
@@ -85,7 +86,7 @@ class _FusedPlan:
         if free is not None:
             return free
         if len(plans) < cls._PER_KEY:
-            p = cls(make_dev(), family, use_grid_improve, use_warmup, ns)
+            p = cls(make_dev(), family, use_grid_improve, use_warmup, ns, n_inc)
             plans.append(p)
             return p
         p = plans.pop(0)  # least recently handed out
@@ -116,7 +117,7 @@ class _FusedPlan:
             d.get_nh_split()
             if i > 0 and self.use_grid_improve:
                 main.wait_event(join)
-            d.iterate_fused(self.family, d.params, self.use_grid_improve)
+            d.iterate_fused(self.family, d.params, self.use_grid_improve, self.points_hint)
             if self.use_grid_improve:
                 fork.record(main)
                 with torch.cuda.stream(side):
@@ -137,9 +138,12 @@ class _FusedPlan:
     def _capture(self):
         """Records warm-up + WHILE(block, abort test) without running it."""
         g = torch.cuda.CUDAGraph()
-        body = torch.cuda.Stream(device=self.dev.device)
         h = ctypes.c_uint64(0)
         with torch.cuda.graph(g):
+            body = L.body_stream(self.dev.device)
+            if self._side.cuda_stream in (L.stream_handle(), body.cuda_stream):
+                # the map-update stream must be neither capturing stream
+                self._side = L.body_stream(self.dev.device, avoid=(body,))
             self._warm_seq()
             L.check(L.lib().tq_capture_while_begin(L.stream_handle(), body.cuda_stream, ctypes.byref(h)),
                     "tq_capture_while_begin")
@@ -257,7 +261,7 @@ class VEGAS(BaseIntegrator):
                                     stats_slots=max_iterations + 10),
                 (str(device), torch.cuda.current_stream().cuda_stream, dim, self.dtype,
                  N_intervals, n_strat), fn.family,
-                use_grid_improve, use_warmup, ns, max_iterations, self)
+                use_grid_improve, use_warmup, ns, self._N_increment, max_iterations, self)
             self._dev = plan.dev
         else:
             if domain is None:

@@ -169,7 +169,7 @@ class _VegasSession:
         d = self.dev
         for _ in range(5):
             d.get_nh()
-            d.iterate_fused(self.req.integrand.family, self.params, True)
+            d.iterate_fused(self.req.integrand.family, self.params, True, d.points_hint(self.v._N_increment))
             d.finish_update_map(BETA, ALPHA)
 
     def done(self):
