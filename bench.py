@@ -498,6 +498,114 @@ def measure_c4_batch(tq, dev, peaks, m=1024):
     }
 
 
+def vegas_batch_workload(n=1024, seed=5):
+    """C5's VEGAS share at the sizes one batch holds: the first n VEGAS
+    requests of the serving stream (dims 1-10, Gaussian-peak or oscillatory
+    integrands, target relative error 1e-3..1e-5) with N log-uniform in
+    1e4..2.56e5 (maps of at most 1024 intervals), fp32."""
+    from torchquad_gb300.serving import poisson_stream
+
+    reqs = [r for _, r in poisson_stream(4 * n, 1e5, seed=seed, n_range=(1e4, 2.56e5)) if r.method == "vegas"]
+    return reqs[:n]
+
+
+def measure_vegas_batch(tq, dev, n=1024, reps=5, k_plain=128):
+    """Batched VEGAS (torchquad_gb300.vegas_batch) on C5's VEGAS share: every
+    integral keeps its own N, target error and seed; the batch replays one
+    captured graph (one launch per phase for all integrals).  Against the
+    per-call VEGAS().integrate of the same requests (a sample, one after the
+    other) and the numpy port on the host."""
+    import numpy as np
+    import torch
+    from torchquad_gb300 import _lib as L
+    from torchquad_gb300.vegas_batch import VegasBatch
+
+    from oracle import integrands as OI
+    from oracle import philox as OP
+    from oracle import vegas as OV
+
+    reqs = vegas_batch_workload(n)
+    fns = [r.integrand for r in reqs]
+    Ns = [r.N for r in reqs]
+    doms = [r.domain for r in reqs]
+    seeds = [r.seed for r in reqs]
+    eps = [r.eps_rel for r in reqs]
+    vb = VegasBatch(fns, Ns, dtype=torch.float32)
+
+    def call():
+        return vb.integrate(domains=doms, seeds=seeds, eps_rel=eps)
+
+    call()  # eager
+    call()  # captures the graph
+    launches0 = L.launches[0]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        res = call()
+    t_e2e = (time.perf_counter() - t0) / reps
+    launches = (L.launches[0] - launches0) // reps
+    # device time of the graph alone (CUDA events on the replaying stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record()
+    for _ in range(reps):
+        vb.graph.replay()
+    ev[1].record()
+    torch.cuda.synchronize()
+    t_dev = ev[0].elapsed_time(ev[1]) / 1e3 / reps
+    res = call().cpu().numpy().astype(np.float64)
+    evals = int(vb.nr_of_fevals.sum())
+    its = vb.it.copy()
+    exact = np.array([f.exact(d) for f, d in zip(fns, doms)])
+    err = np.abs(res - exact) / np.maximum(np.abs(exact), 1e-300)
+    # per-call form on a sample of the same requests
+    k = min(k_plain, n)
+
+    def per_call(i):
+        v = tq.VEGAS()
+        r = v.integrate(fns[i], fns[i].dim, N=Ns[i], integration_domain=torch.tensor(doms[i], dtype=torch.float32,
+                                                                                     device=dev),
+                        seed=seeds[i], eps_rel=eps[i])
+        return float(r), v._nr_of_fevals
+
+    for i in range(min(8, k)):
+        per_call(i)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain = [per_call(i) for i in range(k)]
+    t_plain = (time.perf_counter() - t0) / k
+    diff = max(abs(plain[i][0] - res[i]) / max(abs(plain[i][0]), 1e-300) for i in range(k))
+    # numpy port on the host, the requests in order, bounded
+    t0 = time.perf_counter()
+    j = 0
+    while j < n and time.perf_counter() - t0 < 8.0:
+        r = reqs[j]
+        p = r.integrand.params_numpy()
+        OV.Vegas().integrate(lambda x, fam=r.integrand.family, p=p: OI.evaluate(fam, p, x), r.dim, r.N, r.domain,
+                             OP.ReplayStream(r.seed), dt=np.float32, eps_rel=r.eps_rel)
+        j += 1
+    t_cpu = (time.perf_counter() - t0) / max(1, j)
+    h2d = n * ctypes.sizeof(L.VegasRun)
+    return {
+        "workload": f"{n} VEGAS requests of the serving stream (seed 5), dims 1-10, N log-uniform "
+                    "1e4..2.56e5, target rel err 1e-3..1e-5, fp32, Gaussian-peak / oscillatory",
+        "integrals": n, "evals": evals, "max_iterations_run": int(its.max()),
+        "batched_device_ms": t_dev * 1e3, "batched_integrals_per_s": n / t_dev,
+        "batched_evals_per_s": evals / t_dev,
+        "e2e": {"ms": t_e2e * 1e3, "integrals_per_s": n / t_e2e, "h2d_bytes_per_call": h2d,
+                "d2h_bytes_per_call": vb._rb.numel() * 8},
+        "gpu_launches_per_call": launches,
+        "plain_per_call_integrals_per_s": 1.0 / t_plain, "plain_sample": k,
+        "speedup_batched_vs_plain": t_plain * n / t_dev, "speedup_batched_e2e_vs_plain": t_plain * n / t_e2e,
+        "max_rel_diff_batched_vs_plain_sample": float(diff),
+        "accuracy": {"median_rel_err": float(np.median(err)),
+                     "frac_within_target_rel_err": float(np.mean(err <= np.asarray(eps))),
+                     "frac_within_1e-3": float(np.mean(err <= 1e-3))},
+        "cpu_baseline": {"integrals_per_s": 1.0 / t_cpu, "unit": "integrals/s", "cores": cpu_cores_used(),
+                         "kind": "port", "sample": f"the first {j} requests, numpy VEGAS restatement "
+                                                  "(oracle/vegas.py), one process"},
+    }
+
+
 def _serving_accuracy(reqs):
     import numpy as np
 
@@ -981,6 +1089,7 @@ def run_gpu(args):
     if not args.no_batched:
         line["grid_cases"] = measure_grid_cases(tq, dev, L, peaks, flush)
         line["batched"] = measure_batched(tq, dev, L, peaks)
+        line["vegas_batch"] = measure_vegas_batch(tq, dev)
     if not args.no_serving:
         line["serving"] = measure_serving(tq, dev)
     if not args.no_cpu_baseline:
@@ -1002,7 +1111,9 @@ def run_case(name):
       c3_fp64         the 4096-integral batch, fp64, one tq_batch_grid launch
       c4_batch        1024 differentiation integrals, one tq_batch_grid_adjoint
       c2              one plain VEGAS integration (dim 6, N = 1e7, 50 intervals),
-                      its kernels launched eagerly"""
+                      its kernels launched eagerly
+      vegas_batch     the 1024-integral VEGAS batch of C5's VEGAS share, its
+                      phases launched eagerly"""
     import torch
 
     import torchquad_gb300 as tq
@@ -1052,6 +1163,14 @@ def run_case(name):
         dom = torch.tensor([[0.0, 1.0]] * DIM, dtype=torch.float32, device=dev)
         V.FORCE_EAGER[0] = True
         runs = [lambda: tq.VEGAS().integrate(f, DIM, N=N_EVALS, integration_domain=dom, seed=0, n_intervals=N_BINS)]
+    elif name == "vegas_batch":
+        from torchquad_gb300.vegas_batch import VegasBatch
+
+        reqs = vegas_batch_workload(1024)
+        vb = VegasBatch([r.integrand for r in reqs], [r.N for r in reqs], dtype=torch.float32)
+        runs = [lambda: vb.integrate(domains=[r.domain for r in reqs], seeds=[r.seed for r in reqs],
+                                     eps_rel=[r.eps_rel for r in reqs])]
+        os.environ["TORCHQUAD_GB300_CUDA_GRAPHS"] = "0"  # eager phases: each launch is seen
     else:
         raise SystemExit(f"unknown case {name}")
     for fn in runs * 2:  # warm-up launch, then the profiled one
