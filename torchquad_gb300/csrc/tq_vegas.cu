@@ -683,6 +683,17 @@ namespace tq {
 int vegas_check_state(const tq_vegas_state* st) { return check_state(st); }
 int64_t vegas_nh_blocks(const tq_vegas_state* st) { return nh_blocks(st); }
 int64_t vegas_finish_blocks(const tq_vegas_state* st) { return finish_blocks(st); }
+int64_t vegas_sample_ctas(const tq_vegas_state*, int64_t points) {
+  // Two 32-point tiles per warp.  Fatter CTAs would spend less on their own
+  // copy of the map and their histograms (O(dim x intervals) to fill and
+  // flush), but a lone state then waits on fewer, longer CTAs; a batch
+  // sizes its states the same way, so each gets the CTA split (and the fp32
+  // partial sums) of its own per-call run.
+  const int64_t per = 2 * kTile;
+  const int64_t cap = (int64_t)sm_count() * TQ_SAMPLE_MIN_BLOCKS;
+  const int64_t c = (points + per - 1) / per;
+  return c < 1 ? 1 : (c > cap ? cap : c);
+}
 VegasWsView vegas_workspace_view(const tq_vegas_state* st, void* base) {
   const VegasWs w = vegas_ws(st, base);
   VegasWsView v;
@@ -696,7 +707,8 @@ VegasWsView vegas_workspace_view(const tq_vegas_state* st, void* base) {
   return v;
 }
 SampleArgs vegas_sample_args(const tq_vegas_state* st, int family, const double* params, int64_t n_samples,
-                             int use_map, unsigned* ticket, const int64_t* block_pre, size_t* smem) {
+                             int use_map, unsigned* ticket, const int64_t* block_pre, size_t* smem,
+                             size_t edges_limit) {
   SampleArgs a;
   a.st = *st;
   a.family = family;
@@ -708,10 +720,12 @@ SampleArgs vegas_sample_args(const tq_vegas_state* st, int family, const double*
   a.small_cubes = st->n_cubes < (int64_t(1) << 32) && st->n_strat < (int64_t(1) << 31);
   a.ns_div = make_fastdiv((uint32_t)(a.small_cubes ? st->n_strat : 1));
   const size_t tsize = dtype_size(st->dtype);
-  const size_t limit = 96 * 1024;
-  a.hist_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, true, false) <= limit / 2 &&
+  // The histograms go to shared memory up to 48 KB whatever the launch (the
+  // choice changes how the fp32 sums are grouped, so it depends on the state
+  // alone); the map edges join them up to edges_limit in all.
+  a.hist_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, true, false) <= 48 * 1024 &&
                 st->dim * st->n_bins < (int64_t(1) << 30);
-  a.edges_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, true) <= limit;
+  a.edges_smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, true) <= edges_limit;
   *smem = sample_smem_bytes(st->dim, st->n_bins, tsize, a.hist_smem, a.edges_smem);
   return a;
 }
@@ -723,11 +737,7 @@ static int launch_sample(const tq_vegas_state* st, int family, const double* par
   size_t smem = 0;
   SampleArgs a = vegas_sample_args(st, family, params, n_samples, use_map, ticket, block_pre, &smem);
   const int64_t cap = (int64_t)sm_count() * TQ_SAMPLE_MIN_BLOCKS;  // resident CTAs
-  // known point counts (warm-up): about two 32-point tiles per warp
-  int64_t tiles = max_points > 0 ? (max_points + 2 * kTile - 1) / (2 * kTile) : cap;
-  if (tiles > cap) tiles = cap;
-  if (tiles < 1) tiles = 1;
-  const dim3 grid((unsigned)tiles);
+  const dim3 grid((unsigned)(max_points > 0 ? vegas_sample_ctas(st, max_points) : cap));
   if (st->dtype == TQ_F32 && st->dim <= 8)
     return launch_sample_f32_dims(a, family, st->dim, warm, grid.x, smem, s);
 #define TQ_SAMPLE_LAUNCH(T, WARMB)                                                          \

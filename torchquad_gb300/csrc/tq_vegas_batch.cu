@@ -17,6 +17,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <type_traits>
 #include <vector>
 
@@ -26,8 +27,10 @@
 namespace tq {
 
 constexpr int kBatchAbortThreads = 32;
-constexpr int64_t kBatchMaxCtasPerState = 608;  // the single-state sampler's grid cap (152 SMs x 4)
 constexpr int64_t kBatchInitCtas = 64;
+// Dynamic shared memory of a batched sampling launch (the largest state's):
+// four CTAs of the sampler (64 registers a thread) fit an SM's 228 KB.
+constexpr size_t kBatchSampleSmem = 56 * 1024;
 
 // One state of the batch: the arguments of every phase body, built on the
 // host by the same helpers the single-state launchers use.
@@ -200,16 +203,12 @@ int item_ctas(const tq_vegas_item& it, int32_t ctas[TQ_VB_PHASES], int32_t* map_
   if (it.family < TQ_FN_EXP_SUM || it.family > TQ_FN_SUM_SIN) return TQ_ERR_FAMILY;
   const int64_t work = st->n_cubes > st->dim * (st->n_bins + 1) ? st->n_cubes : st->dim * (st->n_bins + 1);
   ctas[TQ_VB_BEGIN] = (int32_t)clamp_ctas((work + kBlock - 1) / kBlock, kBatchInitCtas);
-  ctas[TQ_VB_WARM] = (it.use_warmup && it.warm_samples > 0)
-                         ? (int32_t)clamp_ctas((it.warm_samples + 2 * kTile - 1) / (2 * kTile),
-                                               kBatchMaxCtasPerState)
-                         : 0;
+  ctas[TQ_VB_WARM] = (it.use_warmup && it.warm_samples > 0) ? (int32_t)vegas_sample_ctas(st, it.warm_samples) : 0;
   ctas[TQ_VB_MAP] = it.use_warmup ? st->dim : 0;
   const int64_t nh = vegas_nh_blocks(st);
   if (nh > (int64_t(1) << 24)) return TQ_ERR_TOO_LARGE;
   ctas[TQ_VB_NH] = (int32_t)nh;
-  ctas[TQ_VB_SAMPLE] =
-      (int32_t)clamp_ctas((it.expected_points + 2 * kTile - 1) / (2 * kTile), kBatchMaxCtasPerState);
+  ctas[TQ_VB_SAMPLE] = (int32_t)vegas_sample_ctas(st, it.expected_points);
   *map_rows = it.use_grid_improve ? st->dim : 0;
   ctas[TQ_VB_FINISH] = (int32_t)(*map_rows + vegas_finish_blocks(st));
   ctas[TQ_VB_ABORT] = 1;
@@ -271,10 +270,10 @@ extern "C" int tq_vegas_batch_build(const tq_vegas_item* items, int64_t n_items,
     const VegasWsView ws = vegas_workspace_view(st, it.workspace);
     size_t sm = 0;
     e.warm = vegas_sample_args(st, it.family, it.params, it.warm_samples > 0 ? it.warm_samples : 1, 1,
-                               ws.t_sample, nullptr, &sm);
+                               ws.t_sample, nullptr, &sm, kBatchSampleSmem);
     if (e.ctas[TQ_VB_WARM] > 0 && sm > smem_warm) smem_warm = sm;
     e.iter = vegas_sample_args(st, it.family, it.params, 0, it.use_grid_improve ? 1 : 0, ws.t_sample,
-                               ws.block_tot, &sm);
+                               ws.block_tot, &sm, kBatchSampleSmem);
     if (sm > smem_sample) smem_sample = sm;
     e.nh.st = *st;
     e.nh.block_tot = ws.block_tot;
@@ -289,6 +288,18 @@ extern "C" int tq_vegas_batch_build(const tq_vegas_item* items, int64_t n_items,
     e.params = it.params;
     e.t_map = ws.t_map;
     if (st->n_bins > max_bins) max_bins = st->n_bins;
+  }
+  // CTAs in order of integrand family and dimension: the CTAs resident on
+  // an SM at once then mostly run the same code (one instantiation of the
+  // sampler per family), which keeps the instruction cache warm
+  std::vector<int64_t> order((size_t)n_items);
+  for (int64_t i = 0; i < n_items; ++i) order[(size_t)i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) {
+    if (items[x].family != items[y].family) return items[x].family < items[y].family;
+    return items[x].st.dim < items[y].st.dim;
+  });
+  for (const int64_t i : order) {
+    const BatchEntry& e = ents[i];
     for (int p = 0; p < TQ_VB_PHASES; ++p) {
       uint2* m = (uint2*)(host.data() + L.map[p]);
       for (int32_t c = 0; c < e.ctas[p]; ++c) m[cursor[p] + c] = make_uint2((unsigned)i, (unsigned)c);

@@ -840,6 +840,8 @@ static __device__ void init_body(const tq_vegas_state& st, unsigned bid, unsigne
 int vegas_check_state(const tq_vegas_state* st);
 int64_t vegas_nh_blocks(const tq_vegas_state* st);
 int64_t vegas_finish_blocks(const tq_vegas_state* st);
+// CTAs of a sampling launch sized for `points` points (at most one wave).
+int64_t vegas_sample_ctas(const tq_vegas_state* st, int64_t points);
 struct VegasWsView {
   unsigned* t_sample;
   unsigned* t_nh;
@@ -850,8 +852,12 @@ struct VegasWsView {
   size_t total;
 };
 VegasWsView vegas_workspace_view(const tq_vegas_state* st, void* base);
-// The sampler's arguments and dynamic shared memory for a state.
+// The sampler's arguments and dynamic shared memory for a state; the map
+// edges are copied to shared memory while the total stays within
+// edges_limit bytes (a lone state affords 96 KB; a batch keeps its launch
+// at four resident CTAs per SM).
 SampleArgs vegas_sample_args(const tq_vegas_state* st, int family, const double* params, int64_t n_samples,
-                             int use_map, unsigned* ticket, const int64_t* block_pre, size_t* smem);
+                             int use_map, unsigned* ticket, const int64_t* block_pre, size_t* smem,
+                             size_t edges_limit = 96 * 1024);
 
 }  // namespace tq

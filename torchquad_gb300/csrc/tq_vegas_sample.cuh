@@ -151,7 +151,7 @@ __host__ __device__ inline size_t sample_smem_bytes(int d, int64_t B, size_t tsi
   size_t off = 0;
   if (edges) off += tsize * (d * (B + 1) + d * B);
   off = (off + 15) & ~size_t(15);
-  if (hist) off += (size_t)kWarps * d * B * (sizeof(double) + sizeof(unsigned));
+  if (hist) off += (size_t)kWarps * d * B * (tsize + sizeof(unsigned));  // HistT<T> weight, u32 count
   return off;
 }
 
@@ -173,7 +173,7 @@ __device__ Smem<T> carve(unsigned char* base, const SampleArgs& a) {
   off = (off + 15) & ~size_t(15);
   if (a.hist_smem) {
     s.hw = (typename HistT<T>::type*)(base + off);
-    off += (size_t)kWarps * d * B * sizeof(double);
+    off += (size_t)kWarps * d * B * sizeof(typename HistT<T>::type);
     s.hc = (unsigned*)(base + off);
   } else {
     s.hw = nullptr;

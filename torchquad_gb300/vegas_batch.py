@@ -36,8 +36,18 @@ from .integration._vegas_state import VegasDevice, n_strat_for
 MAX_BATCH_INTERVALS = 1024
 
 
-def _unit_domain(dim):
-    return [[0.0, 1.0]] * dim
+def _run_dtype():
+    """numpy view of tq_vegas_run (the ctypes mirror's field offsets)."""
+    R = L.VegasRun
+    fields = [("nevals_exp", "<i8"), ("N", "<i8"), ("N_increment", "<i8"), ("max_iterations", "<i8"),
+              ("warm_evals", "<i8"), ("eps_rel", "<f8"), ("eps_abs", "<f8"), ("seed", "<u8"),
+              ("stream_id", "<u8"), ("rng_offset", "<u8"), ("n_params", "<i4"), ("n_domain", "<i4"),
+              ("params", ("<f8", 2 + 2 * L.TQ_MAX_DIM)), ("domain", ("<f8", 2 * L.TQ_MAX_DIM))]
+    return np.dtype({"names": [f for f, _ in fields], "formats": [t for _, t in fields],
+                     "offsets": [getattr(R, f).offset for f, _ in fields], "itemsize": ctypes.sizeof(R)})
+
+
+RUN_DTYPE = _run_dtype()
 
 
 class VegasBatch:
@@ -85,8 +95,6 @@ class VegasBatch:
                                  f"dimension (N = {int(N)} gives {B})")
             dev = VegasDevice(dim, dtype, B, n_strat_for(n_inc, dim), self.device, None, stats_slots=slots,
                               readback=(self._rb[i], self._rb_host[i]))
-            # the run record sits in the pinned buffer copied to the device per call
-            dev._run = L.VegasRun.from_address(self._runs_host.data_ptr() + i * run_size)
             self.states.append(dev)
             ns = n_inc // 5 if self.use_warmup else 0
             self.warm_samples.append(ns)
@@ -100,6 +108,8 @@ class VegasBatch:
             it.use_grid_improve = int(self.use_grid_improve)
             it.use_warmup = int(self.use_warmup)
         self._items = items
+        self.dims = np.asarray([fn.dim for fn in self.integrands], dtype=np.int32)
+        self._runs = self._runs_host.numpy().view(RUN_DTYPE)  # shares the pinned memory
         nbytes = L.lib().tq_vegas_batch_table_size(items, n)
         if nbytes == 0:
             raise ValueError("invalid VEGAS batch (shapes or dtypes)")
@@ -176,16 +186,35 @@ class VegasBatch:
                 rngs = [RNG(seed=s) for s in seeds]
         if len(rngs) != n or (domains is not None and len(domains) != n):
             raise ValueError("one domain and one seed or RNG per integral")
-        er = np.broadcast_to(np.asarray(eps_rel, dtype=np.float64), (n,))
-        ea = np.broadcast_to(np.asarray(eps_abs, dtype=np.float64), (n,))
-        for i, (dev, fn, rng) in enumerate(zip(self.states, self.integrands, rngs)):
-            dom = domains[i] if domains is not None else _unit_domain(dev.dim)
-            if len(dom) != dev.dim:
-                raise ValueError(f"domain {i} has {len(dom)} dimensions, its integrand {dev.dim}")
-            sN = int(self.starting_N[i])
-            dev.fill_run(sN, int(self.N[i]), sN, self.max_iterations, 5 * self.warm_samples[i], float(er[i]),
-                         float(ea[i]), rng.seed, rng.stream_id, rng.offset, fn.params_numpy(),
-                         [(float(lo), float(hi)) for lo, hi in dom])
+        # the run records (tq_vegas_run), column by column, in the pinned
+        # buffer the BEGIN phase reads after one copy
+        rec = self._runs
+        rec["nevals_exp"] = self.starting_N
+        rec["N"] = self.N
+        rec["N_increment"] = self.starting_N
+        rec["max_iterations"] = self.max_iterations
+        rec["warm_evals"] = 5 * np.asarray(self.warm_samples, dtype=np.int64)
+        rec["eps_rel"] = np.broadcast_to(np.asarray(eps_rel, dtype=np.float64), (n,))
+        rec["eps_abs"] = np.broadcast_to(np.asarray(eps_abs, dtype=np.float64), (n,))
+        mask = (1 << 64) - 1
+        rec["seed"] = np.fromiter((r.seed & mask for r in rngs), dtype=np.uint64, count=n)
+        rec["stream_id"] = np.fromiter((r.stream_id & mask for r in rngs), dtype=np.uint64, count=n)
+        rec["rng_offset"] = np.fromiter((r.offset & mask for r in rngs), dtype=np.uint64, count=n)
+        rec["n_domain"] = 2 * self.dims
+        params = rec["params"]
+        dom_out = rec["domain"]
+        for i, fn in enumerate(self.integrands):
+            p = fn.params_numpy()
+            params[i, : len(p)] = p
+            rec["n_params"][i] = len(p)
+            d = self.dims[i]
+            if domains is None:
+                dom_out[i, : 2 * d] = np.tile([0.0, 1.0], d)
+            else:
+                dm = np.asarray(domains[i], dtype=np.float64)
+                if dm.shape != (d, 2):
+                    raise ValueError(f"domain {i} has shape {dm.shape}, its integrand needs ({d}, 2)")
+                dom_out[i, : 2 * d] = dm.reshape(-1)
         self._runs_dev.copy_(self._runs_host, non_blocking=True)
         self.calls += 1
         if self.graph is None and self.calls > 1 and _graphs_enabled():
