@@ -81,11 +81,12 @@ __device__ __forceinline__ T strat_y(int pos, T u, T nsf) {
 }
 
 // cube_start[c] for c < n_cubes; pre != nullptr: cube_start is split
-// (kCtlSplit) and pre holds the offsets of its kBlock-cube blocks.
-// Loads through L2 (__ldcg), never the read-only cache: the prefix is
-// rewritten by other kernels between samplings of the same state.
+// (kCtlSplit) and pre holds the offsets of its kBlock-cube blocks.  Both
+// are read-only for the lifetime of a sampling launch (get_NH and finish,
+// which write them, are launches of their own), so the loads take the
+// read-only data path.
 __device__ __forceinline__ int64_t cube_start_at(const int64_t* cs, const int64_t* pre, int64_t c) {
-  return pre ? __ldcg(cs + c) + __ldcg(pre + c / kBlock) : __ldcg(cs + c);
+  return pre ? __ldg(cs + c) + __ldg(pre + c / kBlock) : __ldg(cs + c);
 }
 
 // Largest c in [0, n) with cube_start[c] <= target; strictly increasing,
@@ -212,26 +213,32 @@ __device__ __forceinline__ void warp_hist_add(H* hw, unsigned* hc, int key, bool
   }
 }
 
-// The integrand inside the sampler with every operation rounded on its own
-// (no FMA contraction), as the reference's separate tensor operations round
-// them: the dimension-specialised and the generic samplers (and the batched
-// one) then compute the same values.
+// The integrand inside the sampler with every rounding spelled out (the
+// products of the separable sum fused into its adds, one rounding each), so
+// that the dimension-specialised, the generic and the batched samplers
+// compute the same values whatever the compiler would contract.
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// s + g_k(x) (g_0(x) for k = 0).
 template <int FAM, typename T>
-__device__ __forceinline__ T vegas_term(const Family<T>& f, int k, T x) {
+__device__ __forceinline__ T vegas_sum(const Family<T>& f, int k, T x, T s) {
   if (FAM == TQ_FN_GAUSSIAN) {
     const T d = sub_rn(x, f.u[k]);
-    return mul_rn(f.a[k], mul_rn(d, d));
+    const T dd = mul_rn(d, d);
+    return k == 0 ? mul_rn(f.a[k], dd) : fma_rn(f.a[k], dd, s);
   } else if (FAM == TQ_FN_SUM_SIN) {
-    return sin(mul_rn(f.a[k], x));
+    const T g = sin(mul_rn(f.a[k], x));
+    return k == 0 ? g : add_rn(s, g);
   } else {
-    return mul_rn(f.a[k], x);
+    return k == 0 ? mul_rn(f.a[k], x) : fma_rn(f.a[k], x, s);
   }
 }
 template <int FAM, typename T>
 __device__ __forceinline__ T vegas_outer(const Family<T>& f, T s) {
   if (FAM == TQ_FN_EXP_SUM) return mul_rn(f.c, exp(add_rn(s, f.b)));
   if (FAM == TQ_FN_GAUSSIAN) return mul_rn(f.c, exp(-s));
-  if (FAM == TQ_FN_OSCILLATORY) return mul_rn(f.c, cos(add_rn(mul_rn((T)(2.0 * CUDART_PI), f.b), s)));
+  if (FAM == TQ_FN_OSCILLATORY) return mul_rn(f.c, cos(fma_rn((T)(2.0 * CUDART_PI), f.b, s)));
   return mul_rn(f.c, s);  // TQ_FN_SUM_SIN
 }
 
@@ -320,7 +327,7 @@ __device__ void sample_body(const SampleArgs& a, unsigned bid, unsigned nblk) {
     if (!WARM) {
       const int64_t cl = c0 + lane;
       csl = cl < st.n_cubes ? cube_start_at(st.cube_start, pre, cl)
-                            : (cl == st.n_cubes ? __ldcg(st.cube_start + cl) : INT64_MAX);
+                            : (cl == st.n_cubes ? __ldg(st.cube_start + cl) : INT64_MAX);
       // bit p: a cube starts at point j0 + p (cube c0 holds j0, so the
       // starts of cubes c0 + 1.. lie after j0); the slot of point j0 + p
       // (largest l with cube_start[c0 + l] <= j) counts the starts in bits 1..p
@@ -399,8 +406,7 @@ __device__ void sample_body(const SampleArgs& a, unsigned bid, unsigned nblk) {
           jac = mul_rn(jac, jf_k);
           // vegas.py:110: fn(x * domain_sizes + domain_starts) * domain_volume
           const T xt = add_rn(mul_rn(x, wid[k]), lo[k]);
-          const T g = vegas_term<FAM, T>(fam, k, xt);
-          s = (k == 0) ? g : add_rn(s, g);
+          s = vegas_sum<FAM, T>(fam, k, xt, s);
         }
       }
       const T f = mul_rn(vegas_outer<FAM, T>(fam, s), volume);
