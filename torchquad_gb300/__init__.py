@@ -30,6 +30,8 @@ from .utils.set_up_backend import set_up_backend
 from . import integrands
 from . import batch
 from . import serving
+from . import vegas_batch
+from .vegas_batch import VegasBatch
 from .integrands import ExpSum, GaussianPeak, Oscillatory, SumSin, BuiltinIntegrand
 
 __all__ = [
@@ -55,6 +57,8 @@ __all__ = [
     "integrands",
     "batch",
     "serving",
+    "vegas_batch",
+    "VegasBatch",
     "ExpSum",
     "GaussianPeak",
     "Oscillatory",
