@@ -108,3 +108,65 @@ def test_batch_fp32_matches_per_call(cuda):
 def test_batch_rejects_large_maps(cuda):
     with pytest.raises(ValueError):
         VegasBatch([tq.ExpSum(2)], [2_000_000])
+
+
+@pytest.mark.parametrize("opts", [dict(use_grid_improve=False), dict(use_warmup=False),
+                                  dict(max_iterations=12)])
+def test_batch_options_match_per_call(cuda, opts):
+    """The reference's VEGAS options (vegas.py:30-44) through the batch:
+    each integral equals its per-call run with the same options."""
+    fns = [tq.GaussianPeak(3, a=[5.0, 8.0, 3.0], u=[0.3, 0.5, 0.7]), tq.Oscillatory(2, a=[1.0, -2.0], b=0.1),
+           tq.ExpSum(5, a=0.3, b=-0.2), tq.SumSin(1, a=2.0)]
+    Ns = [40_000, 25_000, 60_000, 12_000]
+    doms = [[[0.0, 1.0], [-1.0, 1.0], [0.0, 2.0]], [[0.0, 1.0]] * 2, [[0.0, 0.5]] * 5, [[-1.0, 3.0]]]
+    seeds = [21, 22, 23, 24]
+    ref = _per_call(fns, Ns, doms, seeds, torch.float64, **opts)
+    vb = VegasBatch(fns, Ns, dtype=torch.float64, **opts)
+    res = vb.integrate(domains=doms, seeds=seeds).cpu().numpy()
+    for i, (r, it, ev, sN) in enumerate(ref):
+        assert _close(res[i], r, 1e-9), (i, res[i], r)
+        assert vb.it[i] == it and vb.nr_of_fevals[i] == ev and vb.starting_N_out[i] == sN, i
+
+
+def test_batch_edge_states(cuda):
+    """Edge states in one batch: a zero integrand (every map update finds an
+    all-zero row of weights and only resets, vegas_map.py:187-196), a tiny
+    budget whose warm-up draws no points (_starting_N // 5 = 0), the largest
+    dimension (16) and the largest map (1024 intervals); each equals its
+    per-call run, the zero integrand exactly 0."""
+    fns = [tq.ExpSum(2, c=0.0), tq.GaussianPeak.normal(2, 0.5, 0.2), tq.Oscillatory(16, a=0.2, b=0.3),
+           tq.GaussianPeak.normal(3, 0.4, 0.2)]
+    Ns = [20_000, 120, 30_000, 256_000]
+    doms = [[[0.0, 1.0]] * f.dim for f in fns]
+    seeds = [5, 6, 7, 8]
+    ref = _per_call(fns, Ns, doms, seeds, torch.float64)
+    vb = VegasBatch(fns, Ns, dtype=torch.float64)
+    assert vb.warm_samples[1] == 0 and vb.states[3].n_bins == 1024
+    res = vb.integrate(domains=doms, seeds=seeds).cpu().numpy()
+    assert res[0] == 0.0
+    for i, (r, it, ev, _) in enumerate(ref):
+        assert _close(res[i], r, 1e-9), (i, res[i], r)
+        assert vb.it[i] == it and vb.nr_of_fevals[i] == ev, i
+
+
+def test_batch_rng_offsets_advance_like_per_call(cuda):
+    """RNG objects passed to the batch advance as VEGAS().integrate advances
+    them, so a second call continues each stream; results match two
+    consecutive per-call runs on the same RNG objects."""
+    from torchquad_gb300.integration.rng import RNG
+
+    fns = [tq.GaussianPeak.normal(2, 0.5, 0.2), tq.ExpSum(3, a=0.5)]
+    Ns = [30_000, 50_000]
+    doms = [[[0.0, 1.0]] * f.dim for f in fns]
+    ra, rb = [RNG(seed=1), RNG(seed=2)], [RNG(seed=1), RNG(seed=2)]
+    want = []
+    for _ in range(2):
+        for f, N, d, r in zip(fns, Ns, doms, ra):
+            v = tq.VEGAS()
+            want.append(float(v.integrate(f, f.dim, N=N, integration_domain=torch.tensor(d, dtype=torch.float64,
+                                                                                          device="cuda"), rng=r)))
+    vb = VegasBatch(fns, Ns, dtype=torch.float64)
+    got = list(vb.integrate(domains=doms, rngs=rb).cpu().numpy()) + list(vb.integrate(domains=doms, rngs=rb).cpu().numpy())
+    assert [r.offset for r in ra] == [r.offset for r in rb]
+    for g, w in zip(got, want):
+        assert _close(g, w, 1e-9)

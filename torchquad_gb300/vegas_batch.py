@@ -23,6 +23,7 @@ reference's N_increment // 10 intervals).
 from __future__ import annotations
 
 import ctypes
+import warnings
 
 import numpy as np
 import torch
@@ -32,6 +33,7 @@ from .integrands import BuiltinIntegrand
 from .integration.rng import RNG
 from .integration.vegas import ALPHA, BETA, _graphs_enabled
 from .integration._vegas_state import VegasDevice, n_strat_for
+from .integration.vegas_map import _cannot_update_warning
 
 MAX_BATCH_INTERVALS = 1024
 
@@ -251,6 +253,12 @@ class VegasBatch:
         flags = h[:, 16:20].view(np.int32)
         if np.any(flags[:, 2]):
             raise RuntimeError("Could not replace all infinite edges")
+        # the reference's warnings (vegas_map.py:187-196, :247-257), one per
+        # update of each integral, as the per-call API emits them
+        for _ in range(int(flags[:, 0].sum())):
+            _cannot_update_warning()
+        if np.any(flags[:, 1]):
+            warnings.warn("Some calculated VEGASMap edges were infinite", RuntimeWarning)
         self.it = ctl[:, L.VC_IT].copy()
         self.starting_N_out = ctl[:, L.VC_NEVALS].copy()
         self.nr_of_fevals = ctl[:, L.VC_EVALS].copy()
