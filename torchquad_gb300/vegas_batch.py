@@ -23,6 +23,7 @@ reference's N_increment // 10 intervals).
 from __future__ import annotations
 
 import ctypes
+import itertools
 import warnings
 
 import numpy as np
@@ -111,6 +112,15 @@ class VegasBatch:
             it.use_warmup = int(self.use_warmup)
         self._items = items
         self.dims = np.asarray([fn.dim for fn in self.integrands], dtype=np.int32)
+        # (record, column) of every parameter and every domain bound, in the
+        # order of the integrands' flat vectors
+        reps_p, reps_d = 2 + 2 * self.dims, 2 * self.dims
+        self._p_rows = np.repeat(np.arange(n), reps_p)
+        self._p_cols = np.concatenate([np.arange(k) for k in reps_p])
+        self._d_rows = np.repeat(np.arange(n), reps_d)
+        self._d_cols = np.concatenate([np.arange(k) for k in reps_d])
+        self._unit_domains = np.tile([0.0, 1.0], int(self.dims.sum()))
+        self.rng_offsets = np.zeros(n, dtype=np.uint64)
         self._runs = self._runs_host.numpy().view(RUN_DTYPE)  # shares the pinned memory
         nbytes = L.lib().tq_vegas_batch_table_size(items, n)
         if nbytes == 0:
@@ -174,20 +184,19 @@ class VegasBatch:
         return warm + blocks * per_block
 
     # ---------------------------------------------------------------- run
-    def integrate(self, domains=None, seeds=None, rngs=None, eps_rel=0.0, eps_abs=0.0):
+    def integrate(self, domains=None, seeds=None, rngs=None, eps_rel=0.0, eps_abs=0.0, params=None):
         """Integrate every integral of the batch; returns a [n] tensor (the
         batch's dtype) of VEGAS results.  domains: per integral [[lo, hi]] *
-        dim host values (default the unit cube); seeds or rngs: per integral
-        (an RNG's offset advances as VEGAS().integrate advances it);
-        eps_rel / eps_abs: scalars or one per integral."""
+        dim host values (default the unit cube); seeds (a fresh stream per
+        integral, as ``VEGAS().integrate(seed=...)``; default random) or
+        rngs (RNG objects whose offsets advance as VEGAS().integrate
+        advances them); eps_rel / eps_abs: scalars or one per integral;
+        params: optional [n, >= 2 + 2 dim] fp64 parameter rows in place of
+        the integrands' current parameters.  The RNG offsets after the run
+        are also in ``rng_offsets``."""
         n = self.n
-        if rngs is None:
-            if seeds is None:
-                rngs = [RNG(seed=None) for _ in range(n)]
-            else:
-                rngs = [RNG(seed=s) for s in seeds]
-        if len(rngs) != n or (domains is not None and len(domains) != n):
-            raise ValueError("one domain and one seed or RNG per integral")
+        if domains is not None and len(domains) != n:
+            raise ValueError("one domain per integral")
         # the run records (tq_vegas_run), column by column, in the pinned
         # buffer the BEGIN phase reads after one copy
         rec = self._runs
@@ -199,24 +208,46 @@ class VegasBatch:
         rec["eps_rel"] = np.broadcast_to(np.asarray(eps_rel, dtype=np.float64), (n,))
         rec["eps_abs"] = np.broadcast_to(np.asarray(eps_abs, dtype=np.float64), (n,))
         mask = (1 << 64) - 1
-        rec["seed"] = np.fromiter((r.seed & mask for r in rngs), dtype=np.uint64, count=n)
-        rec["stream_id"] = np.fromiter((r.stream_id & mask for r in rngs), dtype=np.uint64, count=n)
-        rec["rng_offset"] = np.fromiter((r.offset & mask for r in rngs), dtype=np.uint64, count=n)
+        if rngs is not None:
+            if seeds is not None:
+                raise ValueError("seed and rng cannot both be passed")
+            if len(rngs) != n:
+                raise ValueError("one RNG per integral")
+            rec["seed"] = np.fromiter((r.seed & mask for r in rngs), dtype=np.uint64, count=n)
+            rec["stream_id"] = np.fromiter((r.stream_id & mask for r in rngs), dtype=np.uint64, count=n)
+            rec["rng_offset"] = np.fromiter((r.offset & mask for r in rngs), dtype=np.uint64, count=n)
+        else:
+            if seeds is None:
+                seeds = [RNG(seed=None).seed for _ in range(n)]
+            seeds = list(seeds)
+            if len(seeds) != n:
+                raise ValueError("one seed per integral")
+            rec["seed"] = np.fromiter((int(x) & mask for x in seeds), dtype=np.uint64, count=n)
+            rec["stream_id"] = 0
+            rec["rng_offset"] = 0
         rec["n_domain"] = 2 * self.dims
-        params = rec["params"]
-        dom_out = rec["domain"]
-        for i, fn in enumerate(self.integrands):
-            p = fn.params_numpy()
-            params[i, : len(p)] = p
-            rec["n_params"][i] = len(p)
-            d = self.dims[i]
-            if domains is None:
-                dom_out[i, : 2 * d] = np.tile([0.0, 1.0], d)
-            else:
-                dm = np.asarray(domains[i], dtype=np.float64)
-                if dm.shape != (d, 2):
-                    raise ValueError(f"domain {i} has shape {dm.shape}, its integrand needs ({d}, 2)")
-                dom_out[i, : 2 * d] = dm.reshape(-1)
+        rec["n_params"] = 2 + 2 * self.dims
+        # parameters and domains as flat vectors scattered into the records
+        if params is None:
+            flat_p = np.concatenate([fn.params_numpy() for fn in self.integrands])
+        else:
+            pa = np.asarray(params, dtype=np.float64)
+            if pa.ndim != 2 or pa.shape[0] != n or pa.shape[1] < int(2 + 2 * self.dims.max()):
+                raise ValueError("params must be [n, >= 2 + 2 * max dim] fp64 rows")
+            flat_p = pa[self._p_rows, self._p_cols]
+        rec["params"][self._p_rows, self._p_cols] = flat_p
+        if domains is None:
+            flat_d = self._unit_domains
+        else:
+            for i, dm in enumerate(domains):
+                if len(dm) != self.dims[i]:
+                    raise ValueError(f"domain {i} has {len(dm)} dimensions, its integrand {self.dims[i]}")
+            chain = itertools.chain.from_iterable
+            try:
+                flat_d = np.fromiter(chain(chain(domains)), dtype=np.float64, count=self._d_rows.size)
+            except (TypeError, ValueError) as e:
+                raise ValueError("domains must be [[lo, hi]] * dim per integral") from e
+        rec["domain"][self._d_rows, self._d_cols] = flat_d
         self._runs_dev.copy_(self._runs_host, non_blocking=True)
         self.calls += 1
         if self.graph is None and self.calls > 1 and _graphs_enabled():
@@ -232,12 +263,15 @@ class VegasBatch:
                     break
         self._rb_host.copy_(self._rb, non_blocking=True)
         torch.cuda.current_stream().synchronize()
-        out = self._collect(rngs)
+        out = self._collect()
+        if rngs is not None:
+            for rng, off in zip(rngs, self.rng_offsets):
+                rng.offset = int(off)
         if self.graph is not None:
             L.count_launches(self._launches_per_call(int(self.it.max()) // 5))
         return out
 
-    def _collect(self, rngs):
+    def _collect(self):
         """The reference's per-integral attributes and results (_get_result,
         EQ 30, in the batch's dtype with left-to-right sums) from the one
         read-back of every state."""
@@ -262,8 +296,7 @@ class VegasBatch:
         self.it = ctl[:, L.VC_IT].copy()
         self.starting_N_out = ctl[:, L.VC_NEVALS].copy()
         self.nr_of_fevals = ctl[:, L.VC_EVALS].copy()
-        for rng, off in zip(rngs, h[:, 20]):
-            rng.offset = int(off)
+        self.rng_offsets = h[:, 20].view(np.uint64).copy()
         stats = h[:, R:].view(np.float64).reshape(self.n, -1, 4)
         rows = self.it[:, None] - 5 + np.arange(5)[None, :]
         idx = np.arange(self.n)[:, None]
