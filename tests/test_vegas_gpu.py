@@ -129,6 +129,13 @@ def test_fused_iteration_matches_reference_state(case, cuda):
         want = _load(st["dh_new"], dtype, cuda)
         dtol = 2e-3 if dtype == torch.float32 else 1e-9
         assert float((dev.dh - want).abs().max()) <= dtol * float(want.max())
+        # what the next iteration consumes of dh (vegas_stratification.py:
+        # 92-103): floor(dh * N) per cube, in dh's dtype, from the
+        # reference's normalised dh, exactly
+        nd = np.float32 if dtype == torch.float32 else np.float64
+        dh_ref = want.cpu().numpy().astype(nd)
+        nh_ref = np.clip(np.floor(dh_ref * nd(st["starting_N"])), 2, None).astype(np.int64)
+        assert dev.neval.cpu().numpy().tolist() == nh_ref.tolist()
 
 
 @pytest.mark.parametrize("case", VG["steps"], ids=lambda c: c["dtype"])

@@ -410,17 +410,18 @@ static __device__ void map_rows_body(const tq_vegas_state& st, double alpha, voi
   int32_t* ind = mk + B;                               // [B+1] old interval per new edge
   unsigned char* z = (unsigned char*)(ind + (B + 1));  // [B] empty intervals
   unsigned char* zt = z + B;                           // [B]
-  // zero-row test over the whole map
+  // zero-row test over the whole map; a row's remaining averages are
+  // skipped once some thread has found a nonzero one (the flag only ever
+  // goes from 0 to 1, so the outcome is the same)
   if (threadIdx.x < d) rownz[threadIdx.x] = 0;
   __syncthreads();
+  volatile int* rnz = rownz;
   for (int kk = 0; kk < d; ++kk) {
-    int nz = 0;
-    for (int b = threadIdx.x; b < B; b += blockDim.x) {
+    for (int b = threadIdx.x; b < B && !rnz[kk]; b += blockDim.x) {
       const int64_t c = st.counts[(int64_t)kk * B + b];
       const T wi = (T)st.weights[(int64_t)kk * B + b];
-      nz |= (c == 0 ? wi : div_rn(wi, (T)c)) != (T)0;
+      if ((c == 0 ? wi : div_rn(wi, (T)c)) != (T)0) rnz[kk] = 1;
     }
-    if (nz) rownz[kk] = 1;
   }
   __syncthreads();
   int zero_row = 0;
@@ -662,12 +663,14 @@ static __device__ void map_rows_f32_body(const tq_vegas_state& st, double alpha,
     for (int b = threadIdx.x; b < B; b += blockDim.x) dxe[b] = dxe_g[b];
   }
   int anyz = 0;
+  volatile int* rnz = rownz;  // other rows: skipped once found nonzero (0 -> 1 only)
   for (int i = threadIdx.x; i < d * B; i += blockDim.x) {
+    const int kk = i / B, b = i - kk * B;
+    if (kk != k && rnz[kk]) continue;
     const int64_t c = st.counts[i];
     const T wi = (T)st.weights[i];
     const T av = c == 0 ? wi : div_rn(wi, (T)c);
-    const int kk = i / B, b = i - kk * B;
-    if (av != (T)0 && !rownz[kk]) rownz[kk] = 1;
+    if (av != (T)0) rnz[kk] = 1;
     if (kk == k) {
       z[b] = c == 0;
       anyz |= c == 0;
