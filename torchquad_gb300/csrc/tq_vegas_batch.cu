@@ -29,8 +29,10 @@ namespace tq {
 constexpr int kBatchAbortThreads = 32;
 constexpr int64_t kBatchInitCtas = 64;
 // Dynamic shared memory of a batched sampling launch (the largest state's):
-// four CTAs of the sampler (64 registers a thread) fit an SM's 228 KB.
+// four fp32 sampler CTAs (64 registers a thread), or three fp64 ones (85),
+// fit an SM's 228 KB.
 constexpr size_t kBatchSampleSmem = 56 * 1024;
+constexpr size_t kBatchSampleSmemF64 = 72 * 1024;
 
 // One state of the batch: the arguments of every phase body, built on the
 // host by the same helpers the single-state launchers use.
@@ -101,7 +103,8 @@ __device__ __forceinline__ void batch_sample(const SampleArgs& a, int family, un
 }
 
 template <typename T, bool WARM>
-__global__ void __launch_bounds__(kTile, TQ_SAMPLE_MIN_BLOCKS) vegas_batch_sample_kernel(BatchLaunch L) {
+__global__ void __launch_bounds__(kTile, std::is_same<T, double>::value ? 3 : TQ_SAMPLE_MIN_BLOCKS)
+    vegas_batch_sample_kernel(BatchLaunch L) {
   const uint2 m = L.map[blockIdx.x];
   const BatchEntry& e = L.e[m.x];
   if (!WARM && batch_stopped(e)) return;
@@ -261,6 +264,7 @@ extern "C" int tq_vegas_batch_build(const tq_vegas_item* items, int64_t n_items,
   int64_t cursor[TQ_VB_PHASES] = {0};
   size_t smem_sample = 0, smem_warm = 0;
   int64_t max_bins = 2;
+  const size_t edges_limit = items[0].st.dtype == TQ_F64 ? kBatchSampleSmemF64 : kBatchSampleSmem;
   for (int64_t i = 0; i < n_items; ++i) {
     const tq_vegas_item& it = items[i];
     const tq_vegas_state* st = &it.st;
@@ -270,10 +274,10 @@ extern "C" int tq_vegas_batch_build(const tq_vegas_item* items, int64_t n_items,
     const VegasWsView ws = vegas_workspace_view(st, it.workspace);
     size_t sm = 0;
     e.warm = vegas_sample_args(st, it.family, it.params, it.warm_samples > 0 ? it.warm_samples : 1, 1,
-                               ws.t_sample, nullptr, &sm, kBatchSampleSmem);
+                               ws.t_sample, nullptr, &sm, edges_limit);
     if (e.ctas[TQ_VB_WARM] > 0 && sm > smem_warm) smem_warm = sm;
     e.iter = vegas_sample_args(st, it.family, it.params, 0, it.use_grid_improve ? 1 : 0, ws.t_sample,
-                               ws.block_tot, &sm, kBatchSampleSmem);
+                               ws.block_tot, &sm, edges_limit);
     if (sm > smem_sample) smem_sample = sm;
     e.nh.st = *st;
     e.nh.block_tot = ws.block_tot;
