@@ -57,7 +57,10 @@ class VegasBatch:
     """A batch of VEGAS integrals sharing one graph (see module docstring).
 
     integrands: BuiltinIntegrand per integral (its ``dim`` must match);
-    Ns: evaluation budget per integral (the reference's ``N``)."""
+    Ns: evaluation budget per integral (the reference's ``N``).  After a
+    call, ``it``, ``nr_of_fevals``, ``starting_N_out``, ``results``,
+    ``sigma2`` and ``rng_offsets`` hold each integral's counterpart of the
+    reference's attributes.  A batch is used from one thread at a time."""
 
     def __init__(self, integrands, Ns, dtype=torch.float64, max_iterations=20, use_grid_improve=True,
                  use_warmup=True, n_intervals=None, device=None):
@@ -279,11 +282,15 @@ class VegasBatch:
         R = VegasDevice._RB_STATS
         ctl = h[:, :16]
         stop = ctl[:, L.VC_STOP]
-        for code, exc in ((4, RuntimeError("VEGAS ran out of statistics slots")),
-                          (5, OverflowError("cannot convert float infinity to integer")),
-                          (6, ValueError("cannot convert float NaN to integer"))):
-            if np.any(stop == code):
-                raise exc
+        # where a per-call run raises (the reference's int() of a
+        # non-finite value in the abort test), the batch raises the same
+        # exception, naming the first integral concerned
+        for code, exc, msg in ((4, RuntimeError, "VEGAS ran out of statistics slots"),
+                               (5, OverflowError, "cannot convert float infinity to integer"),
+                               (6, ValueError, "cannot convert float NaN to integer")):
+            bad = np.nonzero(stop == code)[0]
+            if bad.size:
+                raise exc(f"{msg} (integral {int(bad[0])} of the batch)")
         flags = h[:, 16:20].view(np.int32)
         if np.any(flags[:, 2]):
             raise RuntimeError("Could not replace all infinite edges")
