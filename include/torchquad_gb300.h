@@ -439,8 +439,9 @@ int tq_vegas_batch_build(const tq_vegas_item* items, int64_t n_items, void* tabl
 
 /* Runs `phase` for every state of the batch in one launch.  runs[n_items]
  * (device; TQ_VB_BEGIN only): each state's run inputs, as
- * tq_vegas_begin_run takes them.  States stopped by their abort test
- * (control[12] != 0) skip TQ_VB_NH .. TQ_VB_ABORT.  cond_handle (ABORT):
+ * tq_vegas_begin_run takes them (at most 2 + 2 dim parameters are copied,
+ * and the domain only when n_domain is 2 dim).  States stopped by their
+ * abort test (control[12] != 0) skip TQ_VB_NH .. TQ_VB_ABORT.  cond_handle (ABORT):
  * the cudaGraphConditionalHandle of the WHILE node the launch runs in, or 0. */
 int tq_vegas_batch_phase(const tq_vegas_batch_info* info, const void* table, int phase,
                          const tq_vegas_run* runs, double alpha, double beta, uint64_t cond_handle,

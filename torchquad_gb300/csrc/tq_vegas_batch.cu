@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kBlock) vegas_batch_begin_kernel(BatchLaunch L
   const BatchEntry& e = L.e[m.x];
   if (m.y == 0 && threadIdx.x == 0)
     begin_run_from(L.runs[m.x], e.st.control, e.st.rng_offset, e.params, const_cast<void*>(e.st.domain),
-                   e.st.dtype);
+                   e.st.dtype, 2 + 2 * e.st.dim, 2 * e.st.dim);
   init_body<T>(e.st, m.y, (unsigned)e.ctas[TQ_VB_BEGIN]);
 }
 

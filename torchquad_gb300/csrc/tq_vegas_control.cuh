@@ -41,9 +41,12 @@ struct RunArgs {
 };
 
 // The run inputs r into a state's control block, RNG offset, parameter
-// vector and domain buffer (one thread).
+// vector and domain buffer (one thread).  At most max_params parameters and
+// max_domain domain values are copied (the state's 2 + 2 dim and 2 dim: a
+// run record read from device memory is bounded by its state, not trusted).
 static __device__ void begin_run_from(const tq_vegas_run& r, int64_t* c, uint64_t* rng_offset,
-                                      double* params_dev, void* domain, int dtype) {
+                                      double* params_dev, void* domain, int dtype,
+                                      int max_params = 2 + 2 * TQ_MAX_DIM, int max_domain = 2 * TQ_MAX_DIM) {
   c[kCtlNevals] = r.nevals_exp;
   c[kCtlSeed] = (int64_t)r.seed;
   c[kCtlStream] = (int64_t)r.stream_id;
@@ -57,8 +60,10 @@ static __device__ void begin_run_from(const tq_vegas_run& r, int64_t* c, uint64_
   c[kCtlStop] = 0;
   c[kCtlEvals] = r.warm_evals;
   *rng_offset = r.rng_offset;
-  for (int i = 0; i < r.n_params; ++i) params_dev[i] = r.params[i];
-  for (int i = 0; i < r.n_domain; ++i) {
+  const int n_params = r.n_params < 0 ? 0 : (r.n_params > max_params ? max_params : r.n_params);
+  const int n_domain = r.n_domain == max_domain ? max_domain : 0;  // the whole domain or none
+  for (int i = 0; i < n_params; ++i) params_dev[i] = r.params[i];
+  for (int i = 0; i < n_domain; ++i) {
     if (dtype == TQ_F64)
       ((double*)domain)[i] = r.domain[i];
     else
@@ -67,7 +72,9 @@ static __device__ void begin_run_from(const tq_vegas_run& r, int64_t* c, uint64_
 }
 
 static __device__ void begin_run_body(const RunArgs& a) {
-  begin_run_from(a.run, a.control, a.rng_offset, a.params_dev, a.domain, a.dtype);
+  // the host checked n_params and n_domain (tq_vegas_begin_run)
+  begin_run_from(a.run, a.control, a.rng_offset, a.params_dev, a.domain, a.dtype, a.run.n_params,
+                 a.run.n_domain);
 }
 
 // Arithmetic of the abort test in the state's dtype, each operation rounded
