@@ -66,6 +66,7 @@ __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t til
     if (dim >= 2 && n <= kTabMax) use_tab = build_inner_tab<FAM>(*tab, g, fam, last, n32, gl, rule, gln, glw);
   }
   Acc acc{0.0, 0.0};
+  RecurConst rc{1.0, 1.0, 0.0};
   if constexpr (std::is_same<T, double>::value) {
     if (use_tab) {
       if (threadIdx.x == 0) *fdn = make_fastdiv((uint32_t)n);
@@ -73,6 +74,9 @@ __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t til
       acc = tab_rows_sum<FAM>(g, fam, *tab, *rt, dim, rule, gl, n, *fdn, gln, glw, begin, end);
       return block_reduce<256>(acc);
     }
+    // rows without a table (one dimension, or longer than a table): equally
+    // spaced nodes by recurrence along the row
+    if (!gl) rc = recur_const<FAM>(fam, last, st_l);
   }
   for (int64_t base = begin + (int64_t)threadIdx.x * P; base < end; base += (int64_t)blockDim.x * P) {
     uint64_t row = (uint64_t)base / (uint64_t)n;
@@ -93,6 +97,15 @@ __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t til
       T sum = T(0), comp = T(0);
       bool tabbed = false;
       if constexpr (std::is_same<T, double>::value) {
+        if (!gl) {
+          double v;
+          const double x0 = linspace_node<double>(a_l, b_l, st_l, n, jl);
+          const double x1 = linspace_node<double>(a_l, b_l, st_l, n, seg_end - 1);
+          if (recur_seg_rule<FAM>(rule, fam, rc, last, s_outer, x0, x1, st_l, jl, seg_end, n32, &v)) {
+            sum = v;
+            tabbed = true;
+          }
+        }
         if (use_tab) {
           const RowFactor rf = row_factor<FAM>(fam, s_outer);
           if (rf.ok) {

@@ -147,6 +147,10 @@ __global__ void __launch_bounds__(kBlock, 2) grid_fused_kernel(FusedArgs args) {
       rows_done = true;
     }
   }
+  RecurConst rc{1.0, 1.0, 0.0};
+  if constexpr (std::is_same<T, double>::value) {
+    if (!rows_done && !use_tab && !GL) rc = recur_const<FAM>(fam, last, st_l);
+  }
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * P; base < total && !rows_done;
        base += nthreads * P) {
@@ -174,6 +178,16 @@ __global__ void __launch_bounds__(kBlock, 2) grid_fused_kernel(FusedArgs args) {
           const RowFactor rf = row_factor<FAM>(fam, s_outer);
           if (rf.ok) {
             for (int j = jl; j < seg_end; ++j) seg.add(tab->w[j] * tab_value<FAM>(rf, tab->t1[j], tab->t2[j]));
+            tabbed = true;
+          }
+        } else if (!GL) {
+          // rows without a table (one dimension, or longer than a table):
+          // equally spaced nodes by recurrence along the row
+          double v;
+          const double x0 = linspace_node<double>(a_l, b_l, st_l, n, jl);
+          const double x1 = linspace_node<double>(a_l, b_l, st_l, n, seg_end - 1);
+          if (recur_seg<FAM, RULE>(fam, rc, last, s_outer, x0, x1, st_l, jl, seg_end, n32, &v)) {
+            seg.add(v);
             tabbed = true;
           }
         }

@@ -82,6 +82,113 @@ __device__ __forceinline__ int nc_int_t(int j, int n) {
   return (m & 1) ? 32 : (m == 2 ? 12 : 14);
 }
 
+// ------------------------------- fp64 rows of equally spaced nodes by recurrence
+// Along a grid row of a Newton-Cotes rule the last coordinate steps by h,
+// so each built-in family's value at the next node follows from the
+// current one by a few multiplies instead of an exp / cos (one FP64 warp
+// instruction holds a GB300 sub-partition's FP64 unit for about 64 cycles):
+//   exp sum      f_{j+1} = f_j q,                 q = exp(a h)
+//   Gaussian     f_{j+1} = f_j r_j,  r_{j+1} = r_j q,  q = exp(-2 a h^2),
+//                r_j = exp(-a h (2 (x_j - u) + h))
+//   oscillatory  (cos, sin) of the angle rotated by a h each node
+//   sum of sines sin(a x) rotated likewise.
+// A segment starts from a direct evaluation at its first node, so rounding
+// accumulates over at most a segment's length (16-32 nodes): a few ulps
+// per node value, far inside the grid rules' 1e-12 tolerance.
+struct RecurConst {
+  double q, cd, sd;  // exp-family factor; cosine and sine of the angle step
+};
+
+template <int FAM>
+__device__ __forceinline__ RecurConst recur_const(const Family<double>& fam, int last, double h) {
+  RecurConst rc{1.0, 1.0, 0.0};
+  const double a = fam.a[last];
+  if (FAM == TQ_FN_EXP_SUM) {
+    rc.q = exp(a * h);
+  } else if (FAM == TQ_FN_GAUSSIAN) {
+    rc.q = exp(-2.0 * a * h * h);
+  } else {
+    sincos(a * h, &rc.sd, &rc.cd);
+  }
+  return rc;
+}
+
+// Newton-Cotes integer coefficient of node j as a double, without an
+// integer-to-double conversion.
+template <int RULE>
+__device__ __forceinline__ double nc_coef_d(int j, int n) {
+  if (j == 0 || j == n - 1) return RULE == TQ_RULE_TRAPEZOID ? 1.0 : (RULE == TQ_RULE_SIMPSON ? 1.0 : 7.0);
+  if (RULE == TQ_RULE_TRAPEZOID) return 2.0;
+  if (RULE == TQ_RULE_SIMPSON) return (j & 1) ? 4.0 : 2.0;
+  const int m = j & 3;
+  return (m & 1) ? 32.0 : (m == 2 ? 12.0 : 14.0);
+}
+
+// sum_{j0 <= j < j1} coef_j f(s + g(x_j)), x_j0 = x0, x_{j+1} = x_j + h, for
+// a row of n nodes (fp64, Newton-Cotes rules), into *out.  Returns false
+// (nothing computed) where a recurrence could leave the range of doubles,
+// and the caller then evaluates the nodes directly: the exponent must stay
+// in [-600, 600] over the segment (linear in j for the exp sum, so its ends
+// bound it; concave for a Gaussian with a >= 0, so its ends bound it from
+// below and its peak value -s from above) and change by at most 690 from
+// one node to the next (for the Gaussian that change is linear in j: its
+// first and last steps bound it).
+template <int FAM, int RULE>
+__device__ bool recur_seg(const Family<double>& fam, const RecurConst& rc, int last, double s, double x0,
+                          double x1, double h, int j0, int j1, int n, double* out) {
+  const double a = fam.a[last];
+  double acc = 0.0;
+  if (FAM == TQ_FN_EXP_SUM) {
+    const double e0 = s + a * x0 + fam.b, e1 = s + a * x1 + fam.b;
+    if (!(fabs(e0) <= 600.0 && fabs(e1) <= 600.0 && fabs(a * h) <= 690.0)) return false;
+    double f = fam.c * exp(e0);
+    for (int j = j0; j < j1; ++j) {
+      acc = fma(nc_coef_d<RULE>(j, n), f, acc);
+      f *= rc.q;
+    }
+  } else if (FAM == TQ_FN_GAUSSIAN) {
+    const double d0 = x0 - fam.u[last], d1 = x1 - fam.u[last];
+    const double e0 = -(s + a * (d0 * d0)), e1 = -(s + a * (d1 * d1));
+    if (!(a >= 0.0 && -s <= 600.0 && fabs(e0) <= 600.0 && fabs(e1) <= 600.0 &&
+          fabs(a * h * (2.0 * d0 + h)) <= 690.0 && fabs(a * h * (2.0 * d1 - h)) <= 690.0 && rc.q > 1e-300))
+      return false;
+    double f = fam.c * exp(e0);
+    double r = exp(-a * h * (2.0 * d0 + h));
+    for (int j = j0; j < j1; ++j) {
+      acc = fma(nc_coef_d<RULE>(j, n), f, acc);
+      f *= r;
+      r *= rc.q;
+    }
+  } else {
+    double sn, cs;  // oscillatory: angle 2 pi b + s + a x; sum of sines: a x
+    if (FAM == TQ_FN_OSCILLATORY)
+      sincos(2.0 * CUDART_PI * fam.b + s + a * x0, &sn, &cs);
+    else
+      sincos(a * x0, &sn, &cs);
+    for (int j = j0; j < j1; ++j) {
+      const double v = FAM == TQ_FN_OSCILLATORY ? cs : s + sn;
+      acc = fma(nc_coef_d<RULE>(j, n), v, acc);
+      const double c2 = fma(cs, rc.cd, -(sn * rc.sd));
+      sn = fma(sn, rc.cd, cs * rc.sd);
+      cs = c2;
+    }
+    acc *= fam.c;
+  }
+  *out = acc;
+  return true;
+}
+
+// recur_seg with the rule chosen at run time.
+template <int FAM>
+__device__ __forceinline__ bool recur_seg_rule(int rule, const Family<double>& fam, const RecurConst& rc, int last,
+                                               double s, double x0, double x1, double h, int j0, int j1, int n,
+                                               double* out) {
+  if (rule == TQ_RULE_TRAPEZOID)
+    return recur_seg<FAM, TQ_RULE_TRAPEZOID>(fam, rc, last, s, x0, x1, h, j0, j1, n, out);
+  if (rule == TQ_RULE_SIMPSON) return recur_seg<FAM, TQ_RULE_SIMPSON>(fam, rc, last, s, x0, x1, h, j0, j1, n, out);
+  return recur_seg<FAM, TQ_RULE_BOOLE>(fam, rc, last, s, x0, x1, h, j0, j1, n, out);
+}
+
 // ---------------------------------------------- fp64 inner-dimension tables
 // The built-in families are functions of a separable sum s + t, where s
 // gathers the outer dimensions of a grid row and t = g_last(x_j) the node's
