@@ -1109,6 +1109,7 @@ def run_case(name):
       points_n301     tq_grid_points, Simpson, dim 3, 301^3 nodes, fp64
       wsum_n301       tq_weighted_sum of those 301^3 fp64 values
       c3_fp64         the 4096-integral batch, fp64, one tq_batch_grid launch
+      c3_fp32         the same batch in fp32
       c4_batch        1024 differentiation integrals, one tq_batch_grid_adjoint
       c2              one plain VEGAS integration (dim 6, N = 1e7, 50 intervals),
                       its kernels launched eagerly
@@ -1141,10 +1142,11 @@ def run_case(name):
             runs = [lambda: L.check(lib.tq_weighted_sum(L.TQ_F64, L.TQ_RULE_SIMPSON, 3, 301, dom.data_ptr(), None, 0,
                                                         tot, fv.data_ptr(), L.TQ_F64, 1, acc.data_ptr(),
                                                         ws.data_ptr(), ws.numel(), L.stream_handle()), "wsum")]
-    elif name == "c3_fp64":
+    elif name in ("c3_fp64", "c3_fp32"):
         specs, _ = c3_workload()
         fs = [tq.GaussianPeak(d, a=a.tolist(), u=u.tolist()) for (_, d, _, _, a, u) in specs]
-        bg = B.BatchedGrid(dtype=torch.float64, autotune=False, block=128, strip=16, tile_points=32768)
+        dt = torch.float64 if name == "c3_fp64" else torch.float32
+        bg = B.BatchedGrid(dtype=dt, autotune=False, block=256, strip=16, tile_points=32768)
         plan = bg.plan(fs, [sp[0] for sp in specs], [sp[2] for sp in specs], [sp[3] for sp in specs])
         runs = [lambda: bg.run(plan)]
     elif name == "c4_batch":

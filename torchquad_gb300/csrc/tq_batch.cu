@@ -47,7 +47,7 @@ struct BatchArgs {
 template <typename T, int FAM, int P>
 __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t tile, int64_t tile0,
                              const Geo<T>& g, const Family<T>& fam, const uint64_t* rstride,
-                             InnerTab* tab, RowTab* rt, FastDiv* fdn) {
+                             InnerTab* tab, RowTab* rt, FastDiv* fdn, const F2* wsf) {
   const int dim = d.dim, rule = d.rule, last = dim - 1;
   const int64_t n = d.n;
   const int n32 = (int)n;
@@ -78,15 +78,85 @@ __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t til
     // spaced nodes by recurrence along the row
     if (!gl) rc = recur_const<FAM>(fam, last, st_l);
   }
+  // node indices of an integral below 2^32: 32-bit divisions
+  const bool small = d.total <= (int64_t)0xffffffffll;
+  if constexpr (std::is_same<T, float>::value) {
+    // fp32: the row weights and the running sums as double-floats on the
+    // FP32 pipe (wsf: each dimension's weight scale); one conversion to
+    // fp64 per thread and tile.  (fp64 arithmetic per row segment made this
+    // path FP64-bound on GB300.)
+    F2 facc{0.f, 0.f};
+    // Gauss-Legendre: the last dimension's nodes and weights rounded to
+    // fp32 once per tile (fp64 node mapping, as per node before)
+    __shared__ float glx[kTabMax], glwf[kTabMax];
+    const bool gl_tab = gl && n <= kTabMax;
+    if (gl_tab) {
+      for (int j = threadIdx.x; j < n32; j += blockDim.x) {
+        glx[j] = (float)__dadd_rn(__dmul_rn(g.half[last], __ldg(gln + j)), g.mid[last]);
+        glwf[j] = __double2float_rn(__ldg(glw + j));
+      }
+      __syncthreads();
+    }
+    for (int64_t base = begin + (int64_t)threadIdx.x * P; base < end; base += (int64_t)blockDim.x * P) {
+      uint64_t row = small ? (uint64_t)((uint32_t)base / (uint32_t)n) : (uint64_t)base / (uint64_t)n;
+      int jl = (int)(base - (int64_t)row * n);
+      int64_t left = min((int64_t)P, end - base);
+      while (left > 0) {
+        float s_outer = 0.f;
+        F2 w_outer{1.f, 0.f};
+        for (int k = 0; k < dim - 1; ++k) {
+          const int64_t digit = small ? (int64_t)(((uint32_t)row / (uint32_t)rstride[k]) % (uint32_t)n)
+                                      : (int64_t)((row / rstride[k]) % (uint64_t)n);
+          const float x = gl ? (float)__dadd_rn(__dmul_rn(g.half[k], __ldg(gln + digit)), g.mid[k])
+                             : linspace_node<float>(g.a[k], g.b[k], g.step[k], n, digit);
+          const float t = fam_term<FAM, float>(fam, k, x);
+          s_outer = (k == 0) ? t : s_outer + t;
+          w_outer = f2_mul(w_outer, wsf[k]);
+          w_outer = gl ? f2_mul(w_outer, f2_from_double(__ldg(glw + digit)))
+                       : f2_mul(w_outer, (float)nc_int(rule, digit, n));
+        }
+        const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
+        float sum = 0.f, comp = 0.f;
+        for (int j = jl; j < seg_end; ++j) {
+          float x, wj;
+          if (gl_tab) {
+            x = glx[j];
+            wj = glwf[j];
+          } else if (gl) {
+            x = (float)__dadd_rn(__dmul_rn(g.half[last], __ldg(gln + j)), g.mid[last]);
+            wj = __double2float_rn(__ldg(glw + j));
+          } else {
+            x = (j < half) ? fmaf(st_l, (float)j, a_l) : fmaf(-st_l, (float)(n32 - 1 - j), b_l);
+            wj = (float)nc_int(rule, j, n);
+          }
+          const float f = fam_outer<FAM, float>(fam, s_outer + fam_term<FAM, float>(fam, last, x));
+          // Kahan within the segment
+          const float y = wj * f - comp;
+          const float tt = sum + y;
+          comp = (tt - sum) - y;
+          sum = tt;
+        }
+        facc = f2_add(facc, f2_mul(f2_mul(two_sum(sum, -comp), w_outer), wsf[last]));
+        left -= seg_end - jl;
+        jl = 0;
+        ++row;
+      }
+    }
+    acc_add(acc, f2_value(facc));
+    acc = block_reduce<256>(acc);
+    if (gl_tab) __syncthreads();  // the tables are rewritten by the next tile
+    return acc;
+  }
   for (int64_t base = begin + (int64_t)threadIdx.x * P; base < end; base += (int64_t)blockDim.x * P) {
-    uint64_t row = (uint64_t)base / (uint64_t)n;
+    uint64_t row = small ? (uint64_t)((uint32_t)base / (uint32_t)n) : (uint64_t)base / (uint64_t)n;
     int jl = (int)(base - (int64_t)row * n);
     int64_t left = min((int64_t)P, end - base);
     while (left > 0) {
       T s_outer = T(0);
       double w_outer = 1.0;
       for (int k = 0; k < dim - 1; ++k) {
-        const int64_t digit = (int64_t)((row / rstride[k]) % (uint64_t)n);
+        const int64_t digit = small ? (int64_t)(((uint32_t)row / (uint32_t)rstride[k]) % (uint32_t)n)
+                                    : (int64_t)((row / rstride[k]) % (uint64_t)n);
         const T x = gl ? (T)__dadd_rn(__dmul_rn(g.half[k], __ldg(gln + digit)), g.mid[k])
                        : linspace_node<T>(g.a[k], g.b[k], g.step[k], n, digit);
         const T t = fam_term<FAM, T>(fam, k, x);
@@ -155,6 +225,7 @@ __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
   InnerTab* tab = nullptr;
   RowTab* rt = nullptr;
   __shared__ FastDiv fdn;
+  __shared__ F2 wsf[kMaxDim];  // fp32: the dimensions' weight scales as double-floats
   if constexpr (std::is_same<T, double>::value) {
     __shared__ InnerTab tab_s;
     __shared__ RowTab rt_s;
@@ -178,21 +249,23 @@ __global__ void __launch_bounds__(256) batch_grid_kernel(BatchArgs a) {
         rstride[k] = st;
         st *= (uint64_t)d.n;
       }
+      if constexpr (std::is_same<T, float>::value)
+        for (int k = 0; k < d.dim; ++k) wsf[k] = f2_from_double(g.wscale[k]);
     }
     __syncthreads();
     Acc acc{CUDART_NAN, 0.0};  // an unknown family (rejected on the host) gives NaN
     switch (fam.id) {
       case TQ_FN_EXP_SUM:
-        acc = grid_tile_sum<T, TQ_FN_EXP_SUM, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn);
+        acc = grid_tile_sum<T, TQ_FN_EXP_SUM, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn, wsf);
         break;
       case TQ_FN_GAUSSIAN:
-        acc = grid_tile_sum<T, TQ_FN_GAUSSIAN, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn);
+        acc = grid_tile_sum<T, TQ_FN_GAUSSIAN, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn, wsf);
         break;
       case TQ_FN_OSCILLATORY:
-        acc = grid_tile_sum<T, TQ_FN_OSCILLATORY, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn);
+        acc = grid_tile_sum<T, TQ_FN_OSCILLATORY, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn, wsf);
         break;
       case TQ_FN_SUM_SIN:
-        acc = grid_tile_sum<T, TQ_FN_SUM_SIN, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn);
+        acc = grid_tile_sum<T, TQ_FN_SUM_SIN, P>(a, d, tile, tile0, g, fam, rstride, tab, rt, &fdn, wsf);
         break;
       default:
         break;

@@ -132,6 +132,26 @@ __device__ __forceinline__ F2 f2_shfl_up(F2 a, int off) {
   return F2{__shfl_up_sync(0xffffffffu, a.hi, off), __shfl_up_sync(0xffffffffu, a.lo, off)};
 }
 __device__ __forceinline__ double f2_value(F2 a) { return (double)a.hi + (double)a.lo; }
+// Products (Dekker's TwoProduct through an FMA, then one renormalisation):
+// about 48 significant bits, FP32 pipe only.
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ F2 f2_mul(F2 a, float b) {
+  const float p = __fmul_rn(a.hi, b);
+  float e = __fmaf_rn(a.hi, b, -p);
+  e = __fmaf_rn(a.lo, b, e);
+  return fast_two_sum(p, e);
+}
+// A double split into a double-float (two conversions; once per set-up).
+__device__ __forceinline__ F2 f2_from_double(double x) {
+  const float hi = __double2float_rn(x);
+  return F2{hi, __double2float_rn(x - (double)hi)};
+}
 // The double-float rounded to the nearest float.
 __device__ __forceinline__ float f2_round(F2 a) { return __fadd_rn(a.hi, a.lo); }
 
