@@ -379,6 +379,7 @@ __device__ void mc_tile_sums(const McDesc& d, int64_t begin, int64_t end, const 
                              const T* lo, const T* wid, Acc& s1, Acc& s2) {
   constexpr int PB = Uniform<T>::per_block;
   const int dim = d.dim;
+  F2 f1{0.f, 0.f}, f2{0.f, 0.f};  // fp32 running sums of f and f^2
   for (int64_t q = begin + threadIdx.x; q < end; q += blockDim.x) {
     const uint64_t p = (uint64_t)(d.first + q);
     const uint64_t e0 = p * (uint64_t)dim;
@@ -398,9 +399,22 @@ __device__ void mc_tile_sums(const McDesc& d, int64_t begin, int64_t end, const 
       const T g = fam_term<FAM, T>(fam, k, x);
       s = (k == 0) ? g : s + g;
     }
-    const double f = (double)fam_outer<FAM, T>(fam, s);
-    acc_add(s1, f);
-    acc_add(s2, f * f);
+    if constexpr (std::is_same<T, float>::value) {
+      // fp32: f and f^2 (exactly, as a TwoProduct) into double-floats on the
+      // FP32 pipe; fp64 sums per sample made this path FP64-bound on GB300
+      const float f = fam_outer<FAM, T>(fam, s);
+      const float ff = __fmul_rn(f, f);
+      f1 = f2_add(f1, f);
+      f2 = f2_add(f2_add(f2, ff), __fmaf_rn(f, f, -ff));
+    } else {
+      const double f = (double)fam_outer<FAM, T>(fam, s);
+      acc_add(s1, f);
+      acc_add(s2, f * f);
+    }
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    acc_add(s1, f2_value(f1));
+    acc_add(s2, f2_value(f2));
   }
   s1 = block_reduce<256>(s1);
   s2 = block_reduce<256>(s2);

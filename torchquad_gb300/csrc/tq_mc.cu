@@ -7,6 +7,8 @@
 // offset, so the fused kernel regenerates in registers exactly the values
 // tq_uniform writes for the materialised path, and no [N, dim] buffer exists.
 
+#include <type_traits>
+
 #include "tq_common.cuh"
 
 namespace tq {
@@ -58,6 +60,7 @@ __global__ void __launch_bounds__(kBlock) mc_fused_kernel(McArgs a) {
   constexpr int PB = Uniform<T>::per_block;
   const int dim = a.dim;
   Acc acc{0.0, 0.0};
+  F2 facc{0.f, 0.f};  // fp32: the strip sums as a double-float on the FP32 pipe
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * P; base < a.n_points;
        base += nthreads * P) {
@@ -86,8 +89,12 @@ __global__ void __launch_bounds__(kBlock) mc_fused_kernel(McArgs a) {
       comp += (fabs(inner) >= fabs(f)) ? ((inner - t) + f) : ((f - t) + inner);
       inner = t;
     }
-    acc_add(acc, (double)inner + (double)comp);
+    if constexpr (std::is_same<T, float>::value)
+      facc = f2_add(f2_add(facc, inner), comp);
+    else
+      acc_add(acc, (double)inner + (double)comp);
   }
+  if constexpr (std::is_same<T, float>::value) acc_add(acc, f2_value(facc));
   acc = block_reduce<kBlock>(acc);
   if (threadIdx.x == 0) a.partials[blockIdx.x] = acc;
   if (last_block_arrives(a.ticket)) {
