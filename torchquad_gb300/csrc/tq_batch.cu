@@ -180,7 +180,7 @@ __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t til
           const RowFactor rf = row_factor<FAM>(fam, s_outer);
           if (rf.ok) {
             for (int j = jl; j < seg_end; ++j) {
-              const double y = tab->w[j] * tab_value<FAM>(rf, tab->t1[j], tab->t2[j]) - comp;
+              const double y = tab_accum<FAM>(0.0, rf.r1, rf.r2, *tab, j) - comp;
               const double tt = sum + y;
               comp = (tt - sum) - y;
               sum = tt;

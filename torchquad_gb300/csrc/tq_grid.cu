@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kBlock, 2) grid_fused_kernel(FusedArgs args) {
         if (use_tab) {
           const RowFactor rf = row_factor<FAM>(fam, s_outer);
           if (rf.ok) {
-            for (int j = jl; j < seg_end; ++j) seg.add(tab->w[j] * tab_value<FAM>(rf, tab->t1[j], tab->t2[j]));
+            for (int j = jl; j < seg_end; ++j) seg.add(tab_accum<FAM>(0.0, rf.r1, rf.r2, *tab, j));
             tabbed = true;
           }
         } else if (!GL) {

@@ -204,10 +204,13 @@ __device__ __forceinline__ bool recur_seg_rule(int rule, const Family<double>& f
 // entry that is not, take the direct formula.
 constexpr int kTabMax = 1024;  // last-dimension nodes a table holds
 
+// The node entries carry the node's weight: a node then costs one fused
+// multiply-add into the row sum (two for the oscillatory and sum-of-sines
+// families).
 struct InnerTab {
   double w[kTabMax];   // unscaled 1-D weight of the last dimension
-  double t1[kTabMax];  // exp(t), exp(-t), cos(t) or sin(a x)
-  double t2[kTabMax];  // sin(t) (oscillatory)
+  double t1[kTabMax];  // w exp(t), w exp(-t), w cos(t) or w sin(a x)
+  double t2[kTabMax];  // w sin(t) (oscillatory)
 };
 
 __device__ __forceinline__ bool normal_factor(double v) {
@@ -225,19 +228,20 @@ __device__ bool build_inner_tab(InnerTab& tb, const Geo<double>& g, const Family
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     const double x = gl ? __dadd_rn(__dmul_rn(g.half[last], __ldg(gl_nodes + j)), g.mid[last])
                         : linspace_node<double>(g.a[last], g.b[last], g.step[last], n, j);
-    tb.w[j] = gl ? __ldg(gl_w + j) : (double)nc_int(rule, j, n);
+    const double w = gl ? __ldg(gl_w + j) : (double)nc_int(rule, j, n);
+    tb.w[j] = w;
     const double t = fam_term<FAM, double>(fam, last, x);
     if (FAM == TQ_FN_OSCILLATORY) {
       double sn, cs;
       sincos(t, &sn, &cs);
-      tb.t1[j] = cs;
-      tb.t2[j] = sn;
+      tb.t1[j] = w * cs;
+      tb.t2[j] = w * sn;
     } else if (FAM == TQ_FN_SUM_SIN) {
-      tb.t1[j] = t;
+      tb.t1[j] = w * t;
     } else {
       const double e = exp(FAM == TQ_FN_GAUSSIAN ? -t : t);
-      tb.t1[j] = e;
-      bad |= !normal_factor(e);
+      tb.t1[j] = w * e;
+      bad |= !normal_factor(e) || !normal_factor(w * e);
     }
   }
   return !__syncthreads_or(bad);
@@ -268,13 +272,13 @@ __device__ __forceinline__ RowFactor row_factor(const Family<double>& fam, doubl
   }
   return f;
 }
-// The integrand at a node of the row from the row's factors and the node's
-// table entries.
+// seg + w_j f(node j) of a row from the row's factors and the node's
+// weighted table entries (one or two fused multiply-adds).
 template <int FAM>
-__device__ __forceinline__ double tab_value(const RowFactor& f, double t1, double t2) {
-  if (FAM == TQ_FN_OSCILLATORY) return fma(f.r1, t1, -(f.r2 * t2));
-  if (FAM == TQ_FN_SUM_SIN) return f.r2 * (f.r1 + t1);
-  return f.r1 * t1;
+__device__ __forceinline__ double tab_accum(double seg, double r1, double r2, const InnerTab& tb, int j) {
+  if (FAM == TQ_FN_OSCILLATORY) return fma(-r2, tb.t2[j], fma(r1, tb.t1[j], seg));
+  if (FAM == TQ_FN_SUM_SIN) return fma(r2, fma(r1, tb.w[j], tb.t1[j]), seg);
+  return fma(r1, tb.t1[j], seg);
 }
 
 // Weighted sum over the nodes [begin, end) of an fp64 grid whose last
@@ -355,15 +359,14 @@ __device__ Acc tab_rows_sum(const Geo<double>& g, const Family<double>& fam, con
       }
       double seg = 0.0, ga = 0.0;
       for (int e = 0; e < cnt; ++e) {
-        double v;
         if (rt.ok[ri]) {
-          v = tab_value<FAM>(RowFactor{rt.p[ri], rt.q[ri], true}, tab.t1[j], tab.t2[j]);
+          seg = tab_accum<FAM>(seg, rt.p[ri], rt.q[ri], tab, j);
         } else {  // a row whose factor is not a normal number: the direct formula
           const double x = gl ? __dadd_rn(__dmul_rn(g.half[last], __ldg(gl_nodes + j)), g.mid[last])
                               : linspace_node<double>(g.a[last], g.b[last], g.step[last], n, j);
-          v = fam_outer<FAM, double>(fam, rt.s[ri] + fam_term<FAM, double>(fam, last, x));
+          const double v = fam_outer<FAM, double>(fam, rt.s[ri] + fam_term<FAM, double>(fam, last, x));
+          seg = fma(tab.w[j], v, seg);
         }
-        seg = fma(tab.w[j], v, seg);
         if (++j == n32) {
           ga = fma(seg, rt.w[ri], ga);
           seg = 0.0;
