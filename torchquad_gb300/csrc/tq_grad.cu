@@ -34,12 +34,15 @@ namespace tq {
 constexpr int kAdjTab = 256;  // last-dimension nodes the adjoint's table holds
 constexpr int kAdjP = 16;     // consecutive nodes per thread and strip
 
+// The function entries carry the node's weight w, so a node's weighted value
+// and derivative cost one or two fused multiply-adds.
 struct AdjTab {
   double w[kAdjTab];   // unscaled 1-D weight
   double t[kAdjTab];   // unit node
-  double T1[kAdjTab];  // exp(+-t) | cos t | sin(a x)
-  double T2[kAdjTab];  // sin t (oscillatory)
+  double T1[kAdjTab];  // w exp(+-t) | w cos t | w sin(a x)
+  double T2[kAdjTab];  // w sin t (oscillatory)
   double gp[kAdjTab], ga[kAdjTab], gu[kAdjTab];
+  double gpt[kAdjTab];  // gp t (Gaussian, sum of sines; gp is a constant otherwise)
 };
 
 // Everything a thread needs to walk the nodes of one integral.
@@ -121,17 +124,18 @@ __device__ __forceinline__ AdjRow adj_row(const Family<double>& f, double s) {
   }
   return r;
 }
+// w F and w F' of node j from the row's factors and the weighted entries.
 template <int FAM>
-__device__ __forceinline__ void adj_value(const AdjRow& r, double t1, double t2, double& F, double& Fp) {
+__device__ __forceinline__ void adj_wvalue(const AdjRow& r, const AdjTab& tb, int j, double& WF, double& WFp) {
   if (FAM == TQ_FN_OSCILLATORY) {
-    F = fma(r.p, t1, -(r.q * t2));    // cos(p + t)
-    Fp = -fma(r.q, t1, r.p * t2);     // -sin(p + t)
+    WF = fma(r.p, tb.T1[j], -(r.q * tb.T2[j]));   // w cos(p + t)
+    WFp = -fma(r.q, tb.T1[j], r.p * tb.T2[j]);    // -w sin(p + t)
   } else if (FAM == TQ_FN_SUM_SIN) {
-    F = r.p + t1;
-    Fp = 1.0;
+    WF = fma(r.p, tb.w[j], tb.T1[j]);
+    WFp = tb.w[j];
   } else {
-    F = r.p * t1;
-    Fp = FAM == TQ_FN_GAUSSIAN ? -F : F;
+    WF = r.p * tb.T1[j];
+    WFp = FAM == TQ_FN_GAUSSIAN ? -WF : WF;
   }
 }
 
@@ -144,7 +148,8 @@ __device__ bool adj_build_tab(const AdjCtx<T, GL, DM>& c) {
   int bad = 0;
   for (int j = threadIdx.x; j < n32; j += blockDim.x) {
     const T x = node_at<T, GL>(*c.g, last, c.n, j, c.gln);
-    c.tab->w[j] = GL ? __ldg(c.glw + j) : (double)nc_int(c.rule, j, c.n);
+    const double w = GL ? __ldg(c.glw + j) : (double)nc_int(c.rule, j, c.n);
+    c.tab->w[j] = w;
     c.tab->t[j] = GL ? (double)(T)((__ldg(c.gln + j) + 1.0) * 0.5)
                      : (double)linspace_node<T>((T)0, (T)1, ustep, c.n, j);
     T gp, ga, gu;
@@ -152,20 +157,21 @@ __device__ bool adj_build_tab(const AdjCtx<T, GL, DM>& c) {
     c.tab->gp[j] = (double)gp;
     c.tab->ga[j] = (double)ga;
     c.tab->gu[j] = (double)gu;
+    c.tab->gpt[j] = (double)gp * c.tab->t[j];
     const double tv = (double)fam_term<FAM, T>(*c.fam, last, x);
     if (FAM == TQ_FN_OSCILLATORY) {
       double sn, cs;
       sincos(tv, &sn, &cs);
-      c.tab->T1[j] = cs;
-      c.tab->T2[j] = sn;
+      c.tab->T1[j] = w * cs;
+      c.tab->T2[j] = w * sn;
     } else if (FAM == TQ_FN_SUM_SIN) {
-      c.tab->T1[j] = tv;
+      c.tab->T1[j] = w * tv;
       c.tab->T2[j] = 0.0;
     } else {
       const double e = exp(FAM == TQ_FN_GAUSSIAN ? -tv : tv);
-      c.tab->T1[j] = e;
+      c.tab->T1[j] = w * e;
       c.tab->T2[j] = 0.0;
-      bad |= !normal_factor(e);
+      bad |= !normal_factor(e) || !normal_factor(w * e);
     }
   }
   return !__syncthreads_or(bad);
@@ -217,16 +223,24 @@ __device__ void adj_accumulate(const AdjCtx<T, GL, DM>& c, int64_t first, int64_
           if (rf.ok) {
             const AdjTab& tb = *c.tab;
             for (int j = jl; j < seg_end; ++j) {
-              double F, Fp;
-              adj_value<FAM>(rf, tb.T1[j], tb.T2[j], F, Fp);
-              const double W = tb.w[j];
-              const double wfp = W * Fp;
-              sF += W * F;
-              sFp += wfp;
-              sX += wfp * tb.gp[j];
-              sT += wfp * tb.gp[j] * tb.t[j];
-              sA += wfp * tb.ga[j];
-              sU += wfp * tb.gu[j];
+              double WF, WFp;
+              adj_wvalue<FAM>(rf, tb, j, WF, WFp);
+              sF += WF;
+              sFp += WFp;
+              if (FAM == TQ_FN_GAUSSIAN || FAM == TQ_FN_SUM_SIN) {
+                sX = fma(WFp, tb.gp[j], sX);
+                sT = fma(WFp, tb.gpt[j], sT);
+              } else {
+                sT = fma(WFp, tb.t[j], sT);  // times the constant g' = a below
+              }
+              sA = fma(WFp, tb.ga[j], sA);
+            }
+            if (FAM == TQ_FN_GAUSSIAN) {
+              sU = -sX;  // g'_u = -g'_x
+            } else if (FAM != TQ_FN_SUM_SIN) {  // g = a x: g'_x = a, g'_u = 0
+              const double al = (double)fam.a[last];
+              sX = al * sFp;
+              sT = al * sT;
             }
             tabbed = true;
           }
