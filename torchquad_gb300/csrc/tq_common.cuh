@@ -64,20 +64,25 @@ __device__ __forceinline__ Acc acc_shfl_down(const Acc& a, int off) {
   r.c = __shfl_down_sync(0xffffffffu, a.c, off);
   return r;
 }
-// Fixed-order tree reduction of one Acc per thread; result valid in thread 0.
+// Fixed-order reduction of one Acc per thread (blockDim.x <= BLOCK, whole
+// warps); result valid in thread 0.  One warp combines the partials: lane l
+// merges partials l, l + 32, ... in order, then the lanes in a shuffle tree.
+// (Merging in every warp first ran five compensated merges on all 256
+// threads: on GB300, where an FP64 warp instruction holds the FP64 unit for
+// about 64 cycles, that cost more than the grid itself for a C1-sized
+// fused launch.)
 template <int BLOCK>
 __device__ __forceinline__ Acc block_reduce(Acc a) {
-  __shared__ Acc warp_acc[BLOCK / 32];
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) acc_merge(a, acc_shfl_down(a, off));
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) warp_acc[warp] = a;
+  __shared__ Acc part[BLOCK];
+  part[threadIdx.x] = a;
   __syncthreads();
-  if (warp == 0) {
-    const int nw = min(BLOCK / 32, (int)(blockDim.x >> 5));
-    a = (lane < nw) ? warp_acc[lane] : Acc{0.0, 0.0};
+  if (threadIdx.x < 32) {
+    const int nt = min(BLOCK, (int)blockDim.x);
+    Acc r = part[threadIdx.x];
+    for (int i = threadIdx.x + 32; i < nt; i += 32) acc_merge(r, part[i]);
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc_merge(a, acc_shfl_down(a, off));
+    for (int off = 16; off > 0; off >>= 1) acc_merge(r, acc_shfl_down(r, off));
+    a = r;
   }
   __syncthreads();
   return a;
