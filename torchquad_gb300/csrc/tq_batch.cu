@@ -113,11 +113,15 @@ __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t til
           s_outer = (k == 0) ? t : s_outer + t;
           w_outer = f2_mul(w_outer, wsf[k]);
           w_outer = gl ? f2_mul(w_outer, f2_from_double(__ldg(glw + digit)))
-                       : f2_mul(w_outer, (float)nc_int(rule, digit, n));
+                       : f2_mul(w_outer, nc_coef_f(rule, (int)digit, n32));
         }
         const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
         float sum = 0.f, comp = 0.f;
-        for (int j = jl; j < seg_end; ++j) {
+        // the node index as a float, stepped by one (exact below 2^24; one
+        // conversion per segment instead of one per node)
+        float fj = (float)jl;
+        const float fn1 = (float)(n32 - 1);
+        for (int j = jl; j < seg_end; ++j, fj += 1.f) {
           float x, wj;
           if (gl_tab) {
             x = glx[j];
@@ -126,8 +130,8 @@ __device__ Acc grid_tile_sum(const BatchArgs& a, const BatchDesc& d, int64_t til
             x = (float)__dadd_rn(__dmul_rn(g.half[last], __ldg(gln + j)), g.mid[last]);
             wj = __double2float_rn(__ldg(glw + j));
           } else {
-            x = (j < half) ? fmaf(st_l, (float)j, a_l) : fmaf(-st_l, (float)(n32 - 1 - j), b_l);
-            wj = (float)nc_int(rule, j, n);
+            x = (j < half) ? fmaf(st_l, fj, a_l) : fmaf(-st_l, fn1 - fj, b_l);
+            wj = nc_coef_f(rule, j, n32);
           }
           const float f = fam_outer<FAM, float>(fam, s_outer + fam_term<FAM, float>(fam, last, x));
           // Kahan within the segment

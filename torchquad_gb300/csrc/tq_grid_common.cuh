@@ -113,6 +113,16 @@ __device__ __forceinline__ RecurConst recur_const(const Family<double>& fam, int
   return rc;
 }
 
+// Newton-Cotes integer coefficient of node j as a float, the rule chosen at
+// run time, without an integer-to-float conversion.
+__device__ __forceinline__ float nc_coef_f(int rule, int j, int n) {
+  if (j == 0 || j == n - 1) return rule == TQ_RULE_BOOLE ? 7.f : 1.f;
+  if (rule == TQ_RULE_TRAPEZOID) return 2.f;
+  if (rule == TQ_RULE_SIMPSON) return (j & 1) ? 4.f : 2.f;
+  const int m = j & 3;
+  return (m & 1) ? 32.f : (m == 2 ? 12.f : 14.f);
+}
+
 // Newton-Cotes integer coefficient of node j as a double, without an
 // integer-to-double conversion.
 template <int RULE>
