@@ -26,6 +26,16 @@ _LEGGAUSS = {}
 _GL_DEVICE = {}
 
 
+def _node_count(N):
+    """N as a Python int: ints as they are, 0-d tensors and numpy scalars
+    through ``item()`` (the reference's rule, gaussian.py:120-124)."""
+    if isinstance(N, int):
+        return N
+    if hasattr(N, "item"):
+        return N.item()
+    raise NotImplementedError(f"N {N} is not an int and lacks an `item` method")
+
+
 class Gaussian(GridIntegrator):
     """Gauss-Legendre on [-1, 1] by default; base of custom Gaussian rules.
 
@@ -73,36 +83,37 @@ class Gaussian(GridIntegrator):
         return roots
 
     def _cached_points_and_weights(self, N):
-        root_args = (N, *self._root_args)
-        if not isinstance(N, int):
-            if hasattr(N, "item"):
-                root_args = (N.item(), *self._root_args)
-            else:
-                raise NotImplementedError(f"N {N} is not an int and lacks an `item` method")
-        if root_args in self._cache:
-            return self._cache[root_args]
-        default = self._root_fn is numpy.polynomial.legendre.leggauss
-        if default and root_args[0] > 20000:
+        """(roots, weights) of this rule for N nodes per dimension, cached
+        under (N, *_root_args) as the reference's subclasses expect
+        (gaussian.py:109-128)."""
+        key = (_node_count(N), *self._root_args)
+        found = self._cache.get(key)
+        if found is None:
+            found = self._cache[key] = self._compute_roots(key)
+        return found
+
+    def _compute_roots(self, key):
+        if self._root_fn is not numpy.polynomial.legendre.leggauss:
+            return self._root_fn(*key)
+        if key[0] > 20000:
             raise ValueError(
-                f"{root_args[0]} Gauss-Legendre nodes per dimension: numpy.polynomial.legendre.leggauss "
+                f"{key[0]} Gauss-Legendre nodes per dimension: numpy.polynomial.legendre.leggauss "
                 "builds an n x n matrix; use at most 20000")
-        # leggauss is a pure function of n: its results are shared by all
-        # instances (the reference caches per instance)
-        if default and root_args in _LEGGAUSS:
-            self._cache[root_args] = _LEGGAUSS[root_args]
-        else:
-            self._cache[root_args] = self._root_fn(*root_args)
-            if default:
-                _LEGGAUSS[root_args] = self._cache[root_args]
-        return self._cache[root_args]
+        # leggauss is a pure function of n: one copy serves every instance
+        # (the reference keeps one per instance)
+        if key not in _LEGGAUSS:
+            _LEGGAUSS[key] = self._root_fn(*key)
+        return _LEGGAUSS[key]
 
     @staticmethod
     def _apply_composite_rule(cur_dim_areas, dim, hs, domain):
-        for cur_dim in range(dim):
-            cur_dim_areas = 0.5 * (domain[cur_dim][1] - domain[cur_dim][0]) * torch.sum(
-                cur_dim_areas, dim=len(cur_dim_areas.shape) - 1
-            )
-        return cur_dim_areas
+        """Collapse the trailing ``dim`` node axes: the plain sum of the
+        weighted values times the product of the half-widths (b - a) / 2
+        (the factor the roots on [-1, 1] leave out; gaussian.py:130-143
+        applies it one axis at a time)."""
+        node_axes = tuple(range(cur_dim_areas.dim() - dim, cur_dim_areas.dim()))
+        half_widths = torch.stack([0.5 * (domain[d][1] - domain[d][0]) for d in range(dim)])
+        return torch.prod(half_widths) * torch.sum(cur_dim_areas, dim=node_axes)
 
     # ---- kernel plumbing
     def _gl_tables(self, n, device):
