@@ -371,7 +371,8 @@ def measure_grid_cases(tq, dev, L, peaks, flush, reps=20):
                             "frac": bp / t_p / 1e9 / hbm, "bytes_per_node": 24},
             "weighted_sum": {"us": t_w * 1e6, "bytes": bw, "achieved_gbs": bw / t_w / 1e9, "peak_gbs": hbm,
                              "frac": bw / t_w / 1e9 / hbm, "bytes_per_node": 8,
-                             "fp64_pipe_frac": (tot / t_w / 1e12) * 2.0 / peaks["fp64"]},
+                             "arithmetic": "double-float products and sums on the FP32 pipe, each fp64 value "
+                                           "split into two floats by integer operations (no FP64 per node)"},
         }
         del pts, fv
     mat["peak_source"] = hbm_src

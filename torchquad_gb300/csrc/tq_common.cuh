@@ -160,6 +160,39 @@ __device__ __forceinline__ F2 f2_from_double(double x) {
 // The double-float rounded to the nearest float.
 __device__ __forceinline__ float f2_round(F2 a) { return __fadd_rn(a.hi, a.lo); }
 
+// A double split into two floats by integer operations alone (no FP64
+// instruction; on GB300 conversions also occupy the FP64 unit): hi takes the
+// sign, the exponent and the leading 24 significant bits (truncated), lo the
+// remaining 29 bits rounded to 23, so |x - (hi + lo)| <= 2^-47 |x|, without
+// bias.  lo comes from a float whose exponent is known, 2^(e-1046) + q
+// 2^(e-1069) with q the rounded top 23 of the 29 bits, minus 2^(e-1046)
+// (exact).  Branch-free; hi = lo = 0 when x lies outside 2^-74 <= |x| <
+// 2^128, and ok is false then unless x is a zero: tiny, subnormal, huge,
+// infinite and NaN values are the caller's to handle in fp64.
+struct F2Split {
+  F2 v;
+  bool ok;
+};
+__device__ __forceinline__ F2Split f2_split(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t bh = (uint32_t)(b >> 32), bl = (uint32_t)b;
+  const uint32_t em = bh & 0x7ff00000u;  // biased binary exponent e, << 20
+  const uint32_t sgn = bh & 0x80000000u;
+  F2Split r;
+  const bool in = em - (949u << 20) <= (201u << 20) + 0xfffffu;  // 949 <= e <= 1150
+  // bits 30..23: the low 8 bits of e, 22..0: fraction bits 51..29; the
+  // float exponent e - 896 is those 8 bits with the top one flipped
+  const uint32_t fs = __funnelshift_l(bl, bh, 3);
+  const float hi = __uint_as_float(((fs ^ 0x40000000u) & 0x7fffffffu) | sgn);
+  const uint32_t ex = em * 8u - (919u << 23);
+  const uint32_t q = ((bl & 0x1fffffffu) + 32u) >> 6;  // a carry into the exponent stays exact
+  const float lo = __fsub_rn(__uint_as_float(ex + q), __uint_as_float(ex));
+  r.v.hi = in ? hi : 0.f;
+  r.v.lo = in ? __uint_as_float(__float_as_uint(lo) | sgn) : 0.f;
+  r.ok = in || ((bh & 0x7fffffffu) | bl) == 0u;
+  return r;
+}
+
 // "Last CTA finishes" pattern: every CTA writes its partial, fences, takes a
 // ticket; the CTA that draws the last ticket reduces all partials in index
 // order (deterministic) and resets the ticket for the next launch.  No CTA
