@@ -32,7 +32,7 @@
 namespace tq {
 
 constexpr int kAdjTab = 256;  // last-dimension nodes the adjoint's table holds
-constexpr int kAdjP = 16;     // consecutive nodes per thread and strip
+constexpr int kAdjP = 32;     // consecutive nodes per thread and strip (a whole row at 32 nodes)
 
 // The function entries carry the node's weight w, so a node's weighted value
 // and derivative cost one or two fused multiply-adds.
@@ -43,7 +43,45 @@ struct AdjTab {
   double T2[kAdjTab];  // w sin t (oscillatory)
   double gp[kAdjTab], ga[kAdjTab], gu[kAdjTab];
   double gpt[kAdjTab];  // gp t (Gaussian, sum of sines; gp is a constant otherwise)
+  // the entries of the exponential and oscillatory node loops as
+  // double-floats (that loop runs on the FP32 pipe)
+  F2 T1f[kAdjTab], T2f[kAdjTab], tf[kAdjTab], gaf[kAdjTab], gpf[kAdjTab], gptf[kAdjTab];
 };
+
+// An unnormalised double-float accumulator hi + lo of the node loop.
+struct F2Acc {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(F2 v) {
+    const F2 t = two_sum(hi, v.hi);
+    hi = t.hi;
+    lo = __fadd_rn(lo, __fadd_rn(t.lo, v.lo));
+  }
+  // += a * b (TwoProduct through an FMA plus the cross terms)
+  __device__ __forceinline__ void add_prod(F2 a, F2 b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    const F2 t = two_sum(hi, p);
+    hi = t.hi;
+    lo = __fadd_rn(lo, __fadd_rn(t.lo, e));
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+// a*b + s*(c*d) for s = +-1, as a normalised double-float
+template <int S>
+__device__ __forceinline__ F2 f2_two_products(F2 a, F2 b, F2 c, F2 d) {
+  const float p1 = __fmul_rn(a.hi, b.hi);
+  float e1 = __fmaf_rn(a.hi, b.hi, -p1);
+  e1 = __fmaf_rn(a.hi, b.lo, e1);
+  e1 = __fmaf_rn(a.lo, b.hi, e1);
+  const float p2 = __fmul_rn(c.hi, d.hi);
+  float e2 = __fmaf_rn(c.hi, d.hi, -p2);
+  e2 = __fmaf_rn(c.hi, d.lo, e2);
+  e2 = __fmaf_rn(c.lo, d.hi, e2);
+  const F2 t = two_sum(p1, S > 0 ? p2 : -p2);
+  return two_sum(t.hi, __fadd_rn(t.lo, S > 0 ? __fadd_rn(e1, e2) : __fsub_rn(e1, e2)));
+}
 
 // Everything a thread needs to walk the nodes of one integral.
 template <typename T, bool GL, int DM>
@@ -158,6 +196,10 @@ __device__ bool adj_build_tab(const AdjCtx<T, GL, DM>& c) {
     c.tab->ga[j] = (double)ga;
     c.tab->gu[j] = (double)gu;
     c.tab->gpt[j] = (double)gp * c.tab->t[j];
+    c.tab->tf[j] = f2_from_double(c.tab->t[j]);
+    c.tab->gaf[j] = f2_from_double(c.tab->ga[j]);
+    c.tab->gpf[j] = f2_from_double(c.tab->gp[j]);
+    c.tab->gptf[j] = f2_from_double(c.tab->gpt[j]);
     const double tv = (double)fam_term<FAM, T>(*c.fam, last, x);
     if (FAM == TQ_FN_OSCILLATORY) {
       double sn, cs;
@@ -173,6 +215,8 @@ __device__ bool adj_build_tab(const AdjCtx<T, GL, DM>& c) {
       c.tab->T2[j] = 0.0;
       bad |= !normal_factor(e) || !normal_factor(w * e);
     }
+    c.tab->T1f[j] = f2_from_double(c.tab->T1[j]);
+    c.tab->T2f[j] = f2_from_double(c.tab->T2[j]);
   }
   return !__syncthreads_or(bad);
 }
@@ -222,18 +266,48 @@ __device__ void adj_accumulate(const AdjCtx<T, GL, DM>& c, int64_t first, int64_
           const AdjRow rf = adj_row<FAM>(fam, s_outer);
           if (rf.ok) {
             const AdjTab& tb = *c.tab;
-            for (int j = jl; j < seg_end; ++j) {
-              double WF, WFp;
-              adj_wvalue<FAM>(rf, tb, j, WF, WFp);
-              sF += WF;
-              sFp += WFp;
-              if (FAM == TQ_FN_GAUSSIAN || FAM == TQ_FN_SUM_SIN) {
+            if constexpr (FAM == TQ_FN_SUM_SIN) {
+              for (int j = jl; j < seg_end; ++j) {
+                double WF, WFp;
+                adj_wvalue<FAM>(rf, tb, j, WF, WFp);
+                sF += WF;
+                sFp += WFp;
                 sX = fma(WFp, tb.gp[j], sX);
                 sT = fma(WFp, tb.gpt[j], sT);
-              } else {
-                sT = fma(WFp, tb.t[j], sT);  // times the constant g' = a below
+                sA = fma(WFp, tb.ga[j], sA);
               }
-              sA = fma(WFp, tb.ga[j], sA);
+            } else {
+              // exponential and oscillatory families: the node terms and
+              // their sums as double-floats on the FP32 pipe (about 2^-47
+              // per operation); on GB300 the fp64 form of this loop (eight
+              // FP64 instructions a node) was bound by the FP64 unit
+              const F2 p = f2_from_double(rf.p), q = f2_from_double(rf.q);
+              F2Acc aF, aFp, aX, aT, aA;
+              for (int j = jl; j < seg_end; ++j) {
+                F2 WF, WFp;
+                if (FAM == TQ_FN_OSCILLATORY) {
+                  WF = f2_two_products<-1>(p, tb.T1f[j], q, tb.T2f[j]);   // w cos(p + t)
+                  const F2 sn = f2_two_products<1>(q, tb.T1f[j], p, tb.T2f[j]);  // w sin(p + t)
+                  WFp = F2{-sn.hi, -sn.lo};
+                } else {
+                  WF = f2_mul(p, tb.T1f[j]);
+                  WFp = FAM == TQ_FN_GAUSSIAN ? F2{-WF.hi, -WF.lo} : WF;
+                }
+                aF.add(WF);
+                if (FAM == TQ_FN_OSCILLATORY) aFp.add(WFp);
+                if (FAM == TQ_FN_GAUSSIAN) {
+                  aX.add_prod(WFp, tb.gpf[j]);
+                  aT.add_prod(WFp, tb.gptf[j]);
+                } else {
+                  aT.add_prod(WFp, tb.tf[j]);  // times the constant g' = a below
+                }
+                aA.add_prod(WFp, tb.gaf[j]);
+              }
+              sF = aF.value();
+              sFp = FAM == TQ_FN_OSCILLATORY ? aFp.value() : (FAM == TQ_FN_GAUSSIAN ? -sF : sF);
+              sX = aX.value();
+              sT = aT.value();
+              sA = aA.value();
             }
             if (FAM == TQ_FN_GAUSSIAN) {
               sU = -sX;  // g'_u = -g'_x
@@ -437,10 +511,13 @@ __device__ void batch_adj_dispatch(const BatchGradArgs& a, const tq_batch_desc& 
   }
 }
 
-// Gauss integrals and fp64 batches work in fp64; fp32 Newton-Cotes
-// integrals in fp32 (the node arithmetic of tq_grid_adjoint).
+// Gauss integrals and fp64 batches work in fp64 (their table rows as
+// double-floats); fp32 Newton-Cotes integrals in fp32 (the node arithmetic
+// of tq_grid_adjoint).  Up to four dimensions the kernel is held to 128
+// registers, two CTAs per SM (a few hundred bytes of spills, 20 % faster
+// than one CTA at 159 registers).
 template <typename D, int DM>
-__global__ void __launch_bounds__(kBlock) batch_adjoint_kernel(BatchGradArgs a) {
+__global__ void __launch_bounds__(kBlock, DM <= 4 ? 2 : 1) batch_adjoint_kernel(BatchGradArgs a) {
   __shared__ Geo<double> g64;
   __shared__ Family<double> fam64;
   __shared__ Geo<float> g32;
