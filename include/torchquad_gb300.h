@@ -174,6 +174,9 @@ size_t tq_grid_adjoint_workspace_size(int dim, int64_t total_points);
 /* Value and gradient of the fused tensor-product rule (dim <= 8):
  * out_value[0] = I, out_grad_domain[k][0|1] = dI/da_k | dI/db_k,
  * out_grad_params[i] = dI/dparams[i] (same layout as params: c, b, a_k, u_k).
+ * fp64 grids of the exponential and oscillatory families with a node table
+ * (dim >= 2, at most 256 nodes per dimension) sum their node terms as
+ * double-floats (about 2^-47 per operation), the rest in fp64.
  * Replaces torch autograd through the reference's materialised grid
  * (integration_grid.py:74-88, utils.py:36-52, gaussian.py:81-84,159-162);
  * the domain gradient is that of nodes a + t (b - a) with weights
@@ -228,7 +231,10 @@ size_t tq_weighted_sum_workspace_size(int64_t count, int64_t n_values);
 /* acc[2*s], acc[2*s+1] (a compensated fp64 running sum, s < n_values) +=
  * sum_i w_i * f[i][s] over the nodes [start, start+count) of the grid;
  * f is [count][n_values] of f_dtype (complex integrands are passed as their
- * real view).  For TQ_RULE_MC w_i = 1.  Replaces the weight multiply of
+ * real view).  For TQ_RULE_MC w_i = 1.  One fp64 component of a grid rule
+ * with 32 <= n_per_dim <= 2048 and (dim - 1) * n_per_dim <= 2048 is summed
+ * as double-floats within each CTA (each term to about 2^-46 relative, the
+ * sum's error bound of the order of an fp64 pairwise sum's).  Replaces the weight multiply of
  * base_integrator.py:77-89 and the per-dimension collapse of
  * grid_integrator.py:57-91 / the sum of monte_carlo.py:77. */
 int tq_weighted_sum(int dtype, int rule, int dim, int64_t n_per_dim,
