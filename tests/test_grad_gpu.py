@@ -131,3 +131,34 @@ def test_reference_gradient_cases(name, N1, N2, cuda, float64_default):
         r.backward()
         assert abs(r.item() - 34.0) < 0.2
         assert abs(c.grad.item() - 4.0) < 0.15
+
+
+@pytest.mark.parametrize("case", ["exp_steep_outer", "exp_steep_last", "gauss_narrow_outer", "gauss_narrow_last"])
+def test_adjoint_outside_the_double_float_range(case, cuda):
+    """Row factors or table entries beyond [2^-30, 2^30] (exp(60 x) up to
+    1e26, Gaussian tails below 1e-40): those rows leave the adjoint's
+    double-float node loop for its fp64 one.  Value and gradients against
+    the numpy restatement of the discrete rule's gradient (oracle/grad.py)."""
+    from oracle import grad as OGR
+
+    dim, n = 2, 32
+    if case.startswith("exp"):
+        a = [60.0, 0.5] if case == "exp_steep_outer" else [0.5, 60.0]
+        a_t = torch.tensor(a, dtype=F64, device=cuda, requires_grad=True)
+        f = tq.ExpSum(dim, a=a_t, b=0.1)
+    else:
+        a = [400.0, 1.0] if case == "gauss_narrow_outer" else [1.0, 400.0]
+        a_t = torch.tensor(a, dtype=F64, device=cuda, requires_grad=True)
+        f = tq.GaussianPeak(dim, a=a_t, u=[0.5, 0.3])
+    dom_l = [[0.0, 1.0], [-0.5, 1.0]]
+    dom = torch.tensor(dom_l, dtype=F64, device=cuda, requires_grad=True)
+    val = tq.GaussLegendre().integrate(f, dim, N=n**dim, integration_domain=dom)
+    assert "FusedGridFn" in type(val.grad_fn).__name__
+    val.backward()
+    I, gdom, gpar = OGR.value_and_grad(f.family, f.params_numpy(), OGR.GAUSS, dim, n, dom_l)
+    assert abs(val.item() - I) <= 1e-11 * abs(I)
+    gd = dom.grad.cpu().numpy()
+    assert np.allclose(gd, gdom, rtol=1e-10, atol=1e-10 * np.abs(gdom).max())
+    ga = a_t.grad.cpu().numpy()
+    want_a = gpar[2:2 + dim]
+    assert np.allclose(ga, want_a, rtol=1e-10, atol=1e-10 * np.abs(want_a).max())

@@ -2,9 +2,11 @@
 (tq_weighted_sum, rows of at least 32 nodes), which replaces the weight
 multiply of base_integrator.py:77-89 and the per-dimension collapse of
 grid_integrator.py:57-91.  Products and sums run as double-floats on the
-FP32 pipe, values outside the split's range as an fp64 side sum; each case
-is checked against the exact sum (math.fsum of the fp64 products) within
-2^-44 of the sum of |w_i f_i|, the order of an fp64 pairwise sum's bound."""
+FP32 pipe, values outside the split's range (2^-40 <= |f| < 2^40) as an
+fp64 side sum, grids whose node weights leave [2^-40, 2^40] in fp64; each
+case is checked against the exact sum (math.fsum of the fp64 products)
+within 2^-44 of the sum of |w_i f_i|, the order of an fp64 pairwise sum's
+bound."""
 import math
 
 import numpy as np
@@ -117,12 +119,13 @@ def test_values_outside_the_split_take_the_fp64_side_sum(cuda, kind):
         v = base * 1e200
     elif kind == "subnormal":
         v = base * 1e-310
-    else:  # a few values of each kind among ordinary ones
+    else:  # a few values of each kind among ordinary ones, and the split's range ends
         v = base.copy()
-        idx = rng.choice(n**dim, 30, replace=False)
+        idx = rng.choice(n**dim, 36, replace=False)
         v[idx[:10]] *= 1e-80
         v[idx[10:20]] *= 1e-310
-        v[idx[20:]] *= 1e30
+        v[idx[20:30]] *= 1e30
+        v[idx[30:]] = [2.0**40, 2.0**40 * (1 - 2.0**-52), -(2.0**-40), 2.0**-40 * (1 - 2.0**-52), 1e12, -1e-12]
     want, scale = _exact(w, v)
     got = _run(L.TQ_RULE_SIMPSON, dim, n, dom, v)
     # subnormal products: one subnormal spacing per term on top of the bound
@@ -150,3 +153,16 @@ def test_chunks_equal_one_launch(cuda):
     for chunks in (1, 3, 7):
         got = _run(L.TQ_RULE_SIMPSON, dim, n, dom, v, chunks=chunks)
         assert abs(got - want) <= TOL * scale, (chunks, got, want, scale)
+
+
+@pytest.mark.parametrize("width", [1e20, 1e-20])
+def test_extreme_node_weights_are_summed_in_fp64(cuda, width):
+    """Node weights far outside the float range (domains of width 1e20 and
+    1e-20): the kernel sums the grid in fp64."""
+    dim, n = 3, 65
+    rng = np.random.default_rng(9)
+    dom = [[0.0, width]] * dim
+    v = _mixed_values(rng, n**dim)
+    want, scale = _exact(_weights(L.TQ_RULE_SIMPSON, dim, n, dom), v)
+    got = _run(L.TQ_RULE_SIMPSON, dim, n, dom, v)
+    assert abs(got - want) <= TOL * scale, (got, want, scale)

@@ -166,9 +166,11 @@ __device__ __forceinline__ float f2_round(F2 a) { return __fadd_rn(a.hi, a.lo); 
 // remaining 29 bits rounded to 23, so |x - (hi + lo)| <= 2^-47 |x|, without
 // bias.  lo comes from a float whose exponent is known, 2^(e-1046) + q
 // 2^(e-1069) with q the rounded top 23 of the 29 bits, minus 2^(e-1046)
-// (exact).  Branch-free; hi = lo = 0 when x lies outside 2^-74 <= |x| <
-// 2^128, and ok is false then unless x is a zero: tiny, subnormal, huge,
-// infinite and NaN values are the caller's to handle in fp64.
+// (exact).  Branch-free.  Only 2^-40 <= |x| < 2^40 is split, so that
+// weighted products and long sums of such values stay far inside the float
+// range; otherwise hi = lo = 0, and ok is false unless x is a zero: other
+// values (small, large, subnormal, infinite, NaN) are the caller's to
+// handle in fp64.
 struct F2Split {
   F2 v;
   bool ok;
@@ -179,7 +181,7 @@ __device__ __forceinline__ F2Split f2_split(double x) {
   const uint32_t em = bh & 0x7ff00000u;  // biased binary exponent e, << 20
   const uint32_t sgn = bh & 0x80000000u;
   F2Split r;
-  const bool in = em - (949u << 20) <= (201u << 20) + 0xfffffu;  // 949 <= e <= 1150
+  const bool in = em - (983u << 20) <= (79u << 20) + 0xfffffu;  // 983 <= e <= 1062
   // bits 30..23: the low 8 bits of e, 22..0: fraction bits 51..29; the
   // float exponent e - 896 is those 8 bits with the top one flipped
   const uint32_t fs = __funnelshift_l(bl, bh, 3);

@@ -95,6 +95,7 @@ struct AdjCtx {
   const double* glw;
   AdjTab* tab;
   bool use_tab;
+  bool f2;  // every table entry within the double-float node loop's range
 };
 
 template <int DM>
@@ -177,13 +178,22 @@ __device__ __forceinline__ void adj_wvalue(const AdjRow& r, const AdjTab& tb, in
   }
 }
 
+// The double-float node loop takes factors that are zero or within
+// [2^-30, 2^30]: products of three such factors, and sums of a strip of
+// them, stay far inside the float range.
+__device__ __forceinline__ bool f2_factor_ok(double v) {
+  const double a = fabs(v);
+  return v == 0.0 || (a >= 0x1p-30 && a <= 0x1p30);
+}
+
 // Builds the last-dimension table (all threads of the CTA; ends with a
-// barrier); returns whether every entry is usable.
+// barrier); returns, in every thread, bit 0: every entry is usable, bit 1:
+// every entry is within the double-float loop's range.
 template <typename T, bool GL, int FAM, int DM>
-__device__ bool adj_build_tab(const AdjCtx<T, GL, DM>& c) {
+__device__ int adj_build_tab(const AdjCtx<T, GL, DM>& c) {
   const int last = c.dim - 1, n32 = (int)c.n;
   const T ustep = (T)1 / (T)(c.n - 1);
-  int bad = 0;
+  int bad = 0, f2bad = 0;
   for (int j = threadIdx.x; j < n32; j += blockDim.x) {
     const T x = node_at<T, GL>(*c.g, last, c.n, j, c.gln);
     const double w = GL ? __ldg(c.glw + j) : (double)nc_int(c.rule, j, c.n);
@@ -217,8 +227,11 @@ __device__ bool adj_build_tab(const AdjCtx<T, GL, DM>& c) {
     }
     c.tab->T1f[j] = f2_from_double(c.tab->T1[j]);
     c.tab->T2f[j] = f2_from_double(c.tab->T2[j]);
+    f2bad |= !f2_factor_ok(c.tab->T1[j]) || !f2_factor_ok(c.tab->T2[j]) || !f2_factor_ok(c.tab->t[j]) ||
+             !f2_factor_ok(c.tab->ga[j]) || !f2_factor_ok(c.tab->gp[j]) || !f2_factor_ok(c.tab->gpt[j]);
   }
-  return !__syncthreads_or(bad);
+  const int usable = !__syncthreads_or(bad);
+  return usable | (__syncthreads_or(f2bad) ? 0 : 2);
 }
 
 // Adds the nodes [first, end) visited in strips of kAdjP starting at
@@ -266,48 +279,57 @@ __device__ void adj_accumulate(const AdjCtx<T, GL, DM>& c, int64_t first, int64_
           const AdjRow rf = adj_row<FAM>(fam, s_outer);
           if (rf.ok) {
             const AdjTab& tb = *c.tab;
-            if constexpr (FAM == TQ_FN_SUM_SIN) {
+            bool done = false;
+            if constexpr (FAM != TQ_FN_SUM_SIN) {
+              if (c.f2 && f2_factor_ok(rf.p) && f2_factor_ok(rf.q)) {
+                // exponential and oscillatory families: the node terms and
+                // their sums as double-floats on the FP32 pipe (about 2^-47
+                // per operation); on GB300 the fp64 form of this loop (eight
+                // FP64 instructions a node) was bound by the FP64 unit
+                const F2 p = f2_from_double(rf.p), q = f2_from_double(rf.q);
+                F2Acc aF, aFp, aX, aT, aA;
+                for (int j = jl; j < seg_end; ++j) {
+                  F2 WF, WFp;
+                  if (FAM == TQ_FN_OSCILLATORY) {
+                    WF = f2_two_products<-1>(p, tb.T1f[j], q, tb.T2f[j]);          // w cos(p + t)
+                    const F2 sn = f2_two_products<1>(q, tb.T1f[j], p, tb.T2f[j]);  // w sin(p + t)
+                    WFp = F2{-sn.hi, -sn.lo};
+                  } else {
+                    WF = f2_mul(p, tb.T1f[j]);
+                    WFp = FAM == TQ_FN_GAUSSIAN ? F2{-WF.hi, -WF.lo} : WF;
+                  }
+                  aF.add(WF);
+                  if (FAM == TQ_FN_OSCILLATORY) aFp.add(WFp);
+                  if (FAM == TQ_FN_GAUSSIAN) {
+                    aX.add_prod(WFp, tb.gpf[j]);
+                    aT.add_prod(WFp, tb.gptf[j]);
+                  } else {
+                    aT.add_prod(WFp, tb.tf[j]);  // times the constant g' = a below
+                  }
+                  aA.add_prod(WFp, tb.gaf[j]);
+                }
+                sF = aF.value();
+                sFp = FAM == TQ_FN_OSCILLATORY ? aFp.value() : (FAM == TQ_FN_GAUSSIAN ? -sF : sF);
+                sX = aX.value();
+                sT = aT.value();
+                sA = aA.value();
+                done = true;
+              }
+            }
+            if (!done) {  // fp64: sums of sines, and factors outside the double-float range
               for (int j = jl; j < seg_end; ++j) {
                 double WF, WFp;
                 adj_wvalue<FAM>(rf, tb, j, WF, WFp);
                 sF += WF;
                 sFp += WFp;
-                sX = fma(WFp, tb.gp[j], sX);
-                sT = fma(WFp, tb.gpt[j], sT);
+                if (FAM == TQ_FN_GAUSSIAN || FAM == TQ_FN_SUM_SIN) {
+                  sX = fma(WFp, tb.gp[j], sX);
+                  sT = fma(WFp, tb.gpt[j], sT);
+                } else {
+                  sT = fma(WFp, tb.t[j], sT);  // times the constant g' = a below
+                }
                 sA = fma(WFp, tb.ga[j], sA);
               }
-            } else {
-              // exponential and oscillatory families: the node terms and
-              // their sums as double-floats on the FP32 pipe (about 2^-47
-              // per operation); on GB300 the fp64 form of this loop (eight
-              // FP64 instructions a node) was bound by the FP64 unit
-              const F2 p = f2_from_double(rf.p), q = f2_from_double(rf.q);
-              F2Acc aF, aFp, aX, aT, aA;
-              for (int j = jl; j < seg_end; ++j) {
-                F2 WF, WFp;
-                if (FAM == TQ_FN_OSCILLATORY) {
-                  WF = f2_two_products<-1>(p, tb.T1f[j], q, tb.T2f[j]);   // w cos(p + t)
-                  const F2 sn = f2_two_products<1>(q, tb.T1f[j], p, tb.T2f[j]);  // w sin(p + t)
-                  WFp = F2{-sn.hi, -sn.lo};
-                } else {
-                  WF = f2_mul(p, tb.T1f[j]);
-                  WFp = FAM == TQ_FN_GAUSSIAN ? F2{-WF.hi, -WF.lo} : WF;
-                }
-                aF.add(WF);
-                if (FAM == TQ_FN_OSCILLATORY) aFp.add(WFp);
-                if (FAM == TQ_FN_GAUSSIAN) {
-                  aX.add_prod(WFp, tb.gpf[j]);
-                  aT.add_prod(WFp, tb.gptf[j]);
-                } else {
-                  aT.add_prod(WFp, tb.tf[j]);  // times the constant g' = a below
-                }
-                aA.add_prod(WFp, tb.gaf[j]);
-              }
-              sF = aF.value();
-              sFp = FAM == TQ_FN_OSCILLATORY ? aFp.value() : (FAM == TQ_FN_GAUSSIAN ? -sF : sF);
-              sX = aX.value();
-              sT = aT.value();
-              sA = aA.value();
             }
             if (FAM == TQ_FN_GAUSSIAN) {
               sU = -sX;  // g'_u = -g'_x
@@ -423,9 +445,13 @@ __global__ void __launch_bounds__(kBlock) grid_adjoint_kernel(GradArgs args) {
   }
   __syncthreads();
   AdjCtx<T, GL, DM> c{&g, &fam, rstride, args.dim, args.rule, args.n, args.gl_nodes, args.gl_weights, &tab,
-                      false};
+                      false, false};
   if (std::is_same<T, double>::value && args.dim >= 2 && args.n <= kAdjTab)
-    c.use_tab = adj_build_tab<T, GL, FAM, DM>(c);
+  {
+    const int tb = adj_build_tab<T, GL, FAM, DM>(c);
+    c.use_tab = (tb & 1) != 0;
+    c.f2 = (tb & 2) != 0;
+  }
   AdjAcc<DM> acc;
   acc.zero();
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
@@ -478,9 +504,13 @@ __device__ void batch_adj_tile(const BatchGradArgs& a, const tq_batch_desc& d, i
                                const Geo<T>& g, const Family<T>& fam, const uint64_t* rstride, AdjTab* tab,
                                double (*sh)[2 + 4 * DM]) {
   AdjCtx<T, GL, DM> c{&g, &fam, rstride, d.dim, d.rule, d.n, a.gl_nodes + d.gl_off, a.gl_weights + d.gl_off,
-                      tab, false};
+                      tab, false, false};
   if (std::is_same<T, double>::value && d.dim >= 2 && d.n <= kAdjTab)
-    c.use_tab = adj_build_tab<T, GL, FAM, DM>(c);
+  {
+    const int tb = adj_build_tab<T, GL, FAM, DM>(c);
+    c.use_tab = (tb & 1) != 0;
+    c.f2 = (tb & 2) != 0;
+  }
   const int64_t begin = (tile - tile0) * a.tile_pts;
   const int64_t end = min(d.total, begin + a.tile_pts);
   AdjAcc<DM> acc;

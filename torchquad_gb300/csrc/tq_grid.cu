@@ -678,12 +678,13 @@ __global__ void __launch_bounds__(kBlock) weighted_sum_rows_kernel(WsumArgs args
 // (Newton-Cotes unit weights are small integers, exact in one float).  On
 // GB300 the FP64 unit is the limit of one fp64 fused multiply-add per value
 // (FP64 pipe 82 % active, a quarter of HBM bandwidth); this form issues
-// about 80 instructions per value on the other pipes and is 17 % faster.
+// about 75 instructions per value on the other pipes and is 19 % faster.
 // Each term is within about 2^-46 of w_i f_i and the sums are double-floats,
-// an error bound of the order of an fp64 pairwise sum's.  Values the split
-// cannot take (below 2^-74 or from 2^128 in magnitude, subnormal, infinite,
-// NaN) go to an fp64 side sum.  The CTA's sum becomes fp64 once, in
-// thread 0.
+// an error bound of the order of an fp64 pairwise sum's.  The float range
+// bounds where this holds: values outside 2^-40 <= |f| < 2^40 (and
+// subnormal, infinite, NaN ones) go to an fp64 side sum, and a grid whose
+// node weights leave [2^-40, 2^40] is summed in fp64 throughout.  The CTA's
+// sum becomes fp64 once, in thread 0.
 template <typename T, typename D, bool GL>
 __global__ void __launch_bounds__(kBlock) weighted_sum_rows_f2_kernel(WsumArgs args) {
   __shared__ Geo<T> g;
@@ -692,18 +693,43 @@ __global__ void __launch_bounds__(kBlock) weighted_sum_rows_f2_kernel(WsumArgs a
   __shared__ F2 wo[kRowTab];  // wo[k*n + j] = wscale_k * W_k(j), outer dimensions k
   __shared__ F2 ws[kMaxDim];
   __shared__ F2 red[kBlock / 32];
+  __shared__ unsigned umin_bits, umax_bits;  // extreme |unit weight| (Gauss), as float bits
+  __shared__ int use_f2;
   if (threadIdx.x == 0) {
     geo_setup<T, D>(g, args.rule, args.dim, args.n, (const D*)args.domain);
     fd_n = make_fastdiv((uint32_t)args.n);
+    umin_bits = 0x7f7fffffu;
+    umax_bits = 0u;
   }
   __syncthreads();
   const int dim = args.dim, rule = args.rule, last = dim - 1;
   const int64_t n = args.n;
   const int n32 = (int)n;
   if (threadIdx.x < dim) ws[threadIdx.x] = f2_from_double(g.wscale[threadIdx.x]);
-  for (int j = threadIdx.x; j < n32; j += blockDim.x)
-    wl[j] = GL ? f2_from_double(__ldg(args.gl_weights + j)) : F2{(float)nc_int(rule, j, n), 0.f};
+  for (int j = threadIdx.x; j < n32; j += blockDim.x) {
+    if (GL) {
+      const double u = __ldg(args.gl_weights + j);
+      wl[j] = f2_from_double(u);
+      const unsigned ub = __float_as_uint(fabsf((float)u));  // positive floats order as integers
+      atomicMin(&umin_bits, ub);
+      atomicMax(&umax_bits, ub);
+    } else {
+      wl[j] = F2{(float)nc_int(rule, j, n), 0.f};
+    }
+  }
   __syncthreads();
+  if (threadIdx.x == 0) {
+    // bounds of every node weight: prod_k |wscale_k| x (largest | smallest unit weight)
+    const double umax = GL ? (double)__uint_as_float(umax_bits)
+                           : (rule == TQ_RULE_TRAPEZOID ? 2.0 : (rule == TQ_RULE_SIMPSON ? 4.0 : 32.0));
+    const double umin = GL ? (double)__uint_as_float(umin_bits) : 1.0;
+    double hi = 1.0, lo = 1.0;
+    for (int k = 0; k < dim; ++k) {
+      hi *= fabs(g.wscale[k]) * umax;
+      lo *= fabs(g.wscale[k]) * umin;
+    }
+    use_f2 = hi <= 0x1p40 && lo >= 0x1p-40;  // false for NaN
+  }
   for (int e = threadIdx.x; e < last * n32; e += blockDim.x) {
     const int k = e / n32;
     wo[e] = f2_mul(ws[k], wl[e - k * n32]);
@@ -716,91 +742,114 @@ __global__ void __launch_bounds__(kBlock) weighted_sum_rows_f2_kernel(WsumArgs a
   const uint64_t row_end = ((uint64_t)end + (uint64_t)n - 1) / (uint64_t)n;
   const bool small = (uint64_t)end <= 0xffffffffull;
   const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  F2 lane_acc{0.f, 0.f};
-  double side = 0.0;  // fp64 sum of the values f2_split leaves out
-  int any_side = 0;
-  for (uint64_t r = row_begin + (uint64_t)blockIdx.x * (blockDim.x >> 5) + (uint64_t)warp; r < row_end;
-       r += (uint64_t)nwarps) {
-    F2 w = ws[last];
-    if (small) {
-      uint32_t q = (uint32_t)r;
-      for (int k = last - 1; k >= 0; --k) {
-        const uint32_t q2 = fdiv(q, fd_n);
-        w = f2_mul(w, wo[k * n32 + (int)(q - q2 * fd_n.d)]);
-        q = q2;
-      }
-    } else {
+  const uint64_t r_first = row_begin + (uint64_t)blockIdx.x * (blockDim.x >> 5) + (uint64_t)warp;
+  Acc acc{0.0, 0.0};
+  if (!use_f2) {
+    // node weights outside the double-float range: fp64 throughout
+    double lane_d = 0.0;
+    for (uint64_t r = r_first; r < row_end; r += (uint64_t)nwarps) {
+      double w = g.wscale[last];
       uint64_t q = r;
       for (int k = last - 1; k >= 0; --k) {
         const uint64_t q2 = q / (uint64_t)n;
-        w = f2_mul(w, wo[k * n32 + (int)(q - q2 * (uint64_t)n)]);
+        w *= g.wscale[k] * wunit_at<GL>(rule, n, (int64_t)(q - q2 * (uint64_t)n), args.gl_weights);
         q = q2;
       }
+      const int64_t r0 = (int64_t)r * n;
+      const int j0 = (int)max((int64_t)0, args.start - r0);
+      const int j1 = (int)min(n, end - r0);
+      const double* fr = f + (r0 - args.start);
+      double rsum = 0.0;
+      for (int j = j0 + lane; j < j1; j += 32)
+        rsum = fma(wunit_at<GL>(rule, n, j, args.gl_weights), __ldg(fr + j), rsum);
+      lane_d = fma(rsum, w, lane_d);
     }
-    const int64_t r0 = (int64_t)r * n;
-    const int j0 = (int)max((int64_t)0, args.start - r0);
-    const int j1 = (int)min(n, end - r0);
-    const double* fr = f + (r0 - args.start);
-    float sh = 0.f, sl = 0.f;  // the lane's row sum, hi + lo (lo unnormalised)
-    double rs = 0.0;
-    bool rside = false;
-    // four loads in flight per lane, then their sums
-    for (int jb = j0 + lane; jb < j1; jb += 128) {
-      double x[4];
-      int jj[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int j = jb + 32 * u;
-        jj[u] = j < j1 ? j : j0;
-        x[u] = j < j1 ? __ldg(fr + j) : 0.0;
+    acc = block_reduce<kBlock>(Acc{lane_d, 0.0});
+  } else {
+    F2 lane_acc{0.f, 0.f};
+    double side = 0.0;  // fp64 sum of the values f2_split leaves out
+    int any_side = 0;
+    for (uint64_t r = r_first; r < row_end; r += (uint64_t)nwarps) {
+      F2 w = ws[last];
+      if (small) {
+        uint32_t q = (uint32_t)r;
+        for (int k = last - 1; k >= 0; --k) {
+          const uint32_t q2 = fdiv(q, fd_n);
+          w = f2_mul(w, wo[k * n32 + (int)(q - q2 * fd_n.d)]);
+          q = q2;
+        }
+      } else {
+        uint64_t q = r;
+        for (int k = last - 1; k >= 0; --k) {
+          const uint64_t q2 = q / (uint64_t)n;
+          w = f2_mul(w, wo[k * n32 + (int)(q - q2 * (uint64_t)n)]);
+          q = q2;
+        }
       }
-      unsigned side_mask = 0u;
+      const int64_t r0 = (int64_t)r * n;
+      const int j0 = (int)max((int64_t)0, args.start - r0);
+      const int j1 = (int)min(n, end - r0);
+      const double* fr = f + (r0 - args.start);
+      float sh = 0.f, sl = 0.f;  // the lane's row sum, hi + lo (lo unnormalised)
+      double rs = 0.0;
+      bool rside = false;
+      // four loads in flight per lane, then their sums
+      for (int jb = j0 + lane; jb < j1; jb += 128) {
+        double x[4];
+        int jj[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const F2Split v = f2_split(x[u]);
-        side_mask |= (unsigned)(!v.ok) << u;
-        const F2 wj = wl[jj[u]];
-        const float p = __fmul_rn(wj.hi, v.v.hi);  // w_j f_j = p + e, e to about 2^-46
-        float e = __fmaf_rn(wj.hi, v.v.hi, -p);
-        e = __fmaf_rn(wj.hi, v.v.lo, e);
-        if (GL) e = __fmaf_rn(wj.lo, v.v.hi, e);
-        const F2 t = two_sum(sh, p);
-        sh = t.hi;
-        sl = __fadd_rn(sl, __fadd_rn(t.lo, e));
+        for (int u = 0; u < 4; ++u) {
+          const int j = jb + 32 * u;
+          jj[u] = j < j1 ? j : j0;
+          x[u] = j < j1 ? __ldg(fr + j) : 0.0;
+        }
+        unsigned side_mask = 0u;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const F2Split v = f2_split(x[u]);
+          side_mask |= (unsigned)(!v.ok) << u;
+          const F2 wj = wl[jj[u]];
+          const float p = __fmul_rn(wj.hi, v.v.hi);  // w_j f_j = p + e, e to about 2^-46
+          float e = __fmaf_rn(wj.hi, v.v.hi, -p);
+          e = __fmaf_rn(wj.hi, v.v.lo, e);
+          if (GL) e = __fmaf_rn(wj.lo, v.v.hi, e);
+          const F2 t = two_sum(sh, p);
+          sh = t.hi;
+          sl = __fadd_rn(sl, __fadd_rn(t.lo, e));
+        }
+        if (side_mask) {  // the rare values outside the split's range
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if ((side_mask >> u) & 1u) {
+              rs = fma(f2_value(wl[jj[u]]), x[u], rs);
+              rside = true;
+            }
+        }
       }
-      if (side_mask) {  // the rare values outside the split's range
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if ((side_mask >> u) & 1u) {
-            rs = fma(f2_value(wl[jj[u]]), x[u], rs);
-            rside = true;
-          }
+      lane_acc = f2_add(lane_acc, f2_mul(two_sum(sh, sl), w));
+      if (rside) {
+        side = fma(rs, f2_value(w), side);
+        any_side = 1;
       }
     }
-    lane_acc = f2_add(lane_acc, f2_mul(two_sum(sh, sl), w));
-    if (rside) {
-      side = fma(rs, f2_value(w), side);
-      any_side = 1;
-    }
-  }
-  // the CTA's double-float sum in a fixed tree; fp64 once per CTA
+    // the CTA's double-float sum in a fixed tree; fp64 once per CTA
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) lane_acc = f2_add(lane_acc, f2_shfl_down(lane_acc, o));
-  if (lane == 0) red[warp] = lane_acc;
-  const bool cta_side = __syncthreads_or(any_side) != 0;
-  Acc acc{0.0, 0.0};
-  if (warp == 0) {
-    F2 t = lane < kBlock / 32 ? red[lane] : F2{0.f, 0.f};
+    for (int o = 16; o > 0; o >>= 1) lane_acc = f2_add(lane_acc, f2_shfl_down(lane_acc, o));
+    if (lane == 0) red[warp] = lane_acc;
+    const bool cta_side = __syncthreads_or(any_side) != 0;
+    if (warp == 0) {
+      F2 t = lane < kBlock / 32 ? red[lane] : F2{0.f, 0.f};
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t = f2_add(t, f2_shfl_down(t, o));
-    if (lane == 0) {
-      acc_add(acc, (double)t.hi);
-      acc_add(acc, (double)t.lo);
+      for (int o = 16; o > 0; o >>= 1) t = f2_add(t, f2_shfl_down(t, o));
+      if (lane == 0) {
+        acc_add(acc, (double)t.hi);
+        acc_add(acc, (double)t.lo);
+      }
     }
-  }
-  if (cta_side) {  // rare: the side sums in fp64
-    const Acc sa = block_reduce<kBlock>(Acc{side, 0.0});
-    if (threadIdx.x == 0) acc_merge(acc, sa);
+    if (cta_side) {  // rare: the side sums in fp64
+      const Acc sa = block_reduce<kBlock>(Acc{side, 0.0});
+      if (threadIdx.x == 0) acc_merge(acc, sa);
+    }
   }
   if (threadIdx.x == 0) args.partials[blockIdx.x] = acc;
   if (last_block_arrives(args.ticket)) {
