@@ -203,3 +203,40 @@ def test_host_domain_values():
         _host_domain_values(2, [[0, 1, 2], [0, 1]], None)
     with pytest.raises(ValueError):
         _host_domain_values(2, [[0, 1], [0, 1]], "jax")
+
+
+def test_gaussian_root_cache_and_composite_rule():
+    """The Gaussian extension points a custom rule relies on
+    (gaussian.py:109-143): roots cached under (N, *_root_args), N given as an
+    int, a numpy integer or a 0-d tensor, anything else rejected; the
+    composite rule collapses the trailing node axes and scales by the
+    half-widths, as the reference's one-axis-at-a-time loop does."""
+    g = tq.Gaussian()
+    r3, w3 = g._cached_points_and_weights(3)
+    assert np.allclose(r3, [-np.sqrt(0.6), 0.0, np.sqrt(0.6)]) and np.isclose(w3.sum(), 2.0)
+    assert g._cached_points_and_weights(np.int64(3)) is g._cached_points_and_weights(3)
+    assert g._cached_points_and_weights(torch.tensor(3)) is g._cached_points_and_weights(3)
+    with pytest.raises(NotImplementedError):
+        g._cached_points_and_weights(3.0)
+
+    calls = []
+
+    class Tagged(tq.Gaussian):
+        def __init__(self):
+            super().__init__()
+            self._root_args = ("tag",)
+            self._root_fn = lambda n, tag: calls.append((n, tag)) or np.polynomial.legendre.leggauss(n)
+
+    t = Tagged()
+    t._cached_points_and_weights(4)
+    t._cached_points_and_weights(4)
+    assert calls == [(4, "tag")]
+
+    v = torch.rand(2, 5, 5, 5, dtype=torch.float64)
+    dom = torch.tensor([[-1.0, 2.0], [0.0, 0.5], [1.0, 3.0]], dtype=torch.float64)
+    want = v
+    for d in range(3):  # the reference's order: last axis first, dimension d's half-width
+        want = 0.5 * (dom[d][1] - dom[d][0]) * torch.sum(want, dim=want.dim() - 1)
+    got = tq.Gaussian._apply_composite_rule(v, 3, None, dom)
+    assert got.shape == want.shape == (2,)
+    assert torch.allclose(got, want, rtol=1e-14, atol=0)
