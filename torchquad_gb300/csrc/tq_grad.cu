@@ -33,6 +33,8 @@ namespace tq {
 
 constexpr int kAdjTab = 256;  // last-dimension nodes the adjoint's table holds
 constexpr int kAdjP = 32;     // consecutive nodes per thread and strip (a whole row at 32 nodes)
+constexpr int kOutDims = 3;   // outer dimensions the adjoint's outer tables hold (dim <= 4)
+constexpr int kOutTab = 64;   // nodes per dimension the outer tables hold
 
 // The function entries carry the node's weight w, so a node's weighted value
 // and derivative cost one or two fused multiply-adds.
@@ -46,6 +48,11 @@ struct AdjTab {
   // the entries of the exponential and oscillatory node loops as
   // double-floats (that loop runs on the FP32 pipe)
   F2 T1f[kAdjTab], T2f[kAdjTab], tf[kAdjTab], gaf[kAdjTab], gpf[kAdjTab], gptf[kAdjTab];
+  // outer dimensions (dim - 1 <= kOutDims, n <= kOutTab): each node's term,
+  // weight factor, derivative terms and unit coordinate, computed once per
+  // table and looked up by every row instead of recomputed (same values)
+  double otv[kOutDims][kOutTab], ow[kOutDims][kOutTab], ogp[kOutDims][kOutTab];
+  double oga[kOutDims][kOutTab], ogu[kOutDims][kOutTab], ot[kOutDims][kOutTab];
 };
 
 // An unnormalised double-float accumulator hi + lo of the node loop.
@@ -95,7 +102,8 @@ struct AdjCtx {
   const double* glw;
   AdjTab* tab;
   bool use_tab;
-  bool f2;  // every table entry within the double-float node loop's range
+  bool f2;    // every table entry within the double-float node loop's range
+  bool otab;  // the outer tables hold this integral's outer dimensions
 };
 
 template <int DM>
@@ -230,6 +238,21 @@ __device__ int adj_build_tab(const AdjCtx<T, GL, DM>& c) {
     f2bad |= !f2_factor_ok(c.tab->T1[j]) || !f2_factor_ok(c.tab->T2[j]) || !f2_factor_ok(c.tab->t[j]) ||
              !f2_factor_ok(c.tab->ga[j]) || !f2_factor_ok(c.tab->gp[j]) || !f2_factor_ok(c.tab->gpt[j]);
   }
+  if (c.dim - 1 <= kOutDims && c.n <= kOutTab) {
+    for (int e = threadIdx.x; e < (c.dim - 1) * n32; e += blockDim.x) {
+      const int k = e / n32, j = e - k * n32;
+      const T x = node_at<T, GL>(*c.g, k, c.n, j, c.gln);
+      c.tab->otv[k][j] = (double)fam_term<FAM, T>(*c.fam, k, x);
+      c.tab->ow[k][j] = c.g->wscale[k] * (GL ? __ldg(c.glw + j) : (double)nc_int(c.rule, j, c.n));
+      T gp, ga, gu;
+      fam_term_d<FAM, T>(*c.fam, k, x, gp, ga, gu);
+      c.tab->ogp[k][j] = (double)gp;
+      c.tab->oga[k][j] = (double)ga;
+      c.tab->ogu[k][j] = (double)gu;
+      c.tab->ot[k][j] = GL ? (double)(T)((__ldg(c.gln + j) + 1.0) * 0.5)
+                           : (double)linspace_node<T>((T)0, (T)1, ustep, c.n, j);
+    }
+  }
   const int usable = !__syncthreads_or(bad);
   return usable | (__syncthreads_or(f2bad) ? 0 : 2);
 }
@@ -261,14 +284,27 @@ __device__ void adj_accumulate(const AdjCtx<T, GL, DM>& c, int64_t first, int64_
       // live registers across the node loop)
       T s_outer = T(0);
       double w_outer = 1.0;
+      if (c.otab) {
+        const AdjTab& tb = *c.tab;
 #pragma unroll
-      for (int k = 0; k < DM; ++k) {
-        if (k < dim - 1) {
-          const int64_t digit = (int64_t)((row / c.rstride[k]) % (uint64_t)n);
-          const T x = node_at<T, GL>(g, k, n, digit, c.gln);
-          const T tv = fam_term<FAM, T>(fam, k, x);
-          s_outer = (k == 0) ? tv : s_outer + tv;
-          w_outer *= g.wscale[k] * wunit(digit);
+        for (int k = 0; k < kOutDims; ++k) {
+          if (k < dim - 1) {
+            const int d = (int)((row / c.rstride[k]) % (uint64_t)n);
+            const T tv = (T)tb.otv[k][d];
+            s_outer = (k == 0) ? tv : s_outer + tv;
+            w_outer *= tb.ow[k][d];
+          }
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < DM; ++k) {
+          if (k < dim - 1) {
+            const int64_t digit = (int64_t)((row / c.rstride[k]) % (uint64_t)n);
+            const T x = node_at<T, GL>(g, k, n, digit, c.gln);
+            const T tv = fam_term<FAM, T>(fam, k, x);
+            s_outer = (k == 0) ? tv : s_outer + tv;
+            w_outer *= g.wscale[k] * wunit(digit);
+          }
         }
       }
       const int seg_end = (int)min((int64_t)n32, (int64_t)jl + left);
@@ -364,7 +400,16 @@ __device__ void adj_accumulate(const AdjCtx<T, GL, DM>& c, int64_t first, int64_
       const double fo = sc * sFp;
 #pragma unroll
       for (int k = 0; k < DM; ++k) {
-        if (k < dim - 1) {
+        if (k < dim - 1 && c.otab) {
+          const int kk = k < kOutDims ? k : 0;  // k < dim - 1 <= kOutDims here
+          const int d = (int)((row / c.rstride[kk]) % (uint64_t)n);
+          const AdjTab& tb = *c.tab;
+          const double gp_o = tb.ogp[kk][d];
+          acc.Sx[k] += fo * gp_o;
+          acc.St[k] += fo * gp_o * tb.ot[kk][d];
+          acc.Pa[k] += fo * tb.oga[kk][d];
+          acc.Pu[k] += fo * tb.ogu[kk][d];
+        } else if (k < dim - 1) {
           const int64_t digit = (int64_t)((row / c.rstride[k]) % (uint64_t)n);
           const T x = node_at<T, GL>(g, k, n, digit, c.gln);
           T gp_o, ga_o, gu_o;
@@ -445,12 +490,13 @@ __global__ void __launch_bounds__(kBlock) grid_adjoint_kernel(GradArgs args) {
   }
   __syncthreads();
   AdjCtx<T, GL, DM> c{&g, &fam, rstride, args.dim, args.rule, args.n, args.gl_nodes, args.gl_weights, &tab,
-                      false, false};
+                      false, false, false};
   if (std::is_same<T, double>::value && args.dim >= 2 && args.n <= kAdjTab)
   {
     const int tb = adj_build_tab<T, GL, FAM, DM>(c);
     c.use_tab = (tb & 1) != 0;
     c.f2 = (tb & 2) != 0;
+    c.otab = c.use_tab && c.dim - 1 <= kOutDims && c.n <= kOutTab;
   }
   AdjAcc<DM> acc;
   acc.zero();
@@ -504,12 +550,13 @@ __device__ void batch_adj_tile(const BatchGradArgs& a, const tq_batch_desc& d, i
                                const Geo<T>& g, const Family<T>& fam, const uint64_t* rstride, AdjTab* tab,
                                double (*sh)[2 + 4 * DM]) {
   AdjCtx<T, GL, DM> c{&g, &fam, rstride, d.dim, d.rule, d.n, a.gl_nodes + d.gl_off, a.gl_weights + d.gl_off,
-                      tab, false, false};
+                      tab, false, false, false};
   if (std::is_same<T, double>::value && d.dim >= 2 && d.n <= kAdjTab)
   {
     const int tb = adj_build_tab<T, GL, FAM, DM>(c);
     c.use_tab = (tb & 1) != 0;
     c.f2 = (tb & 2) != 0;
+    c.otab = c.use_tab && c.dim - 1 <= kOutDims && c.n <= kOutTab;
   }
   const int64_t begin = (tile - tile0) * a.tile_pts;
   const int64_t end = min(d.total, begin + a.tile_pts);
